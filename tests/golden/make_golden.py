@@ -1,0 +1,192 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs only where the reference tree is present (it reads it from
+/root/reference).  Three sources:
+
+1. The reference's crossbarHspice V1 ``sim``, compiled from its own sources by
+   ``make -C oracle ref`` into ``oracle/_ref/sim``, run on seeded configs written
+   as explicit per-cell ``setCellR`` lines (its ``randSetR`` is unseeded).
+2. The reference's PimTorch modules, imported through a throw-away package in a
+   temporary directory: the six ``fixedPoint/nn`` files are copied there
+   unchanged except that the import-time JIT build and ``chdir`` in
+   ``commonConst.py`` are removed (the CUDA source does not compile against this
+   torch and there is no GPU here).  Nothing from that copy is kept.
+3. Their outputs, saved as small .npz files next to this script.
+
+Usage: python tests/golden/make_golden.py
+"""
+import os
+import re
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+REF = "/root/reference"
+NN = os.path.join(REF, "pimtorch", "pimfixedpoint", "fixedPoint", "nn")
+SIM = os.path.join(REPO, "oracle", "_ref", "sim")
+
+from oracle import intstages  # noqa: E402
+
+
+def sim_run(states, Rset, vin, r_wire, iters, w, tol):
+    n, m = states.shape
+    lines = ["useRtypeReRAMCell yes",
+             "cellRstates %d %s" % (len(Rset), " ".join("%.17g" % r for r in Rset)),
+             "arraySize %d %d" % (n, m), "selector no", "line_resistance %.17g" % r_wire]
+    for i in range(n):
+        for j in range(m):
+            lines.append("setCellR %d %d %d" % (i, j, states[i, j]))
+    lines += ["setUseLine left -1", "setUseLine down -1"]
+    for i in range(n):
+        lines.append("setLineV left %d %.17g" % (i, vin[i]))
+    lines += ["setLineV down -1 0", "senseBitlineI down -1",
+              "nodebasedGSMethod %d %.17g 0 yes %.17g" % (iters, w, tol)]
+    with tempfile.TemporaryDirectory() as td:
+        with open(os.path.join(td, "cfg"), "w") as f:
+            f.write("\n".join(lines) + "\n")
+        out = subprocess.run([SIM, "cfg"], cwd=td, capture_output=True, text=True, check=True).stdout
+        with open(os.path.join(td, "fastmode_nodebasedGS.out")) as f:
+            txt = f.read()
+    vup_s, rest = txt.split("vup = ")[1].split("vdown = ")
+    vdn_s, iout_s = rest.split("iout = ")
+    arr = lambda s: np.array([float(x) for x in s.split()])
+    rec = re.findall(r"iter times =\s+(\d+)", out)
+    sweeps = int(rec[-1]) + 1 if rec else iters
+    return arr(vup_s).reshape(n, m), arr(vdn_s).reshape(n, m), arr(iout_s), sweeps
+
+
+def sim_fixtures():
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref"], check=True)
+    Rset = np.array([2e6, 1.6e6, 1.3e6, 1e6])
+    w = float(np.float32(1.95))  # the reference parses omega with stof
+    # small non-square tile, mixed wordline voltages, converged hard
+    rng = np.random.default_rng(7)
+    st = rng.integers(0, 4, (16, 24))
+    vin = rng.integers(0, 2, 16) * 0.2 + 0.05
+    u, d, io, sw = sim_run(st, Rset, vin, 2.93, 100000, w, 1e-11)
+    np.savez_compressed(os.path.join(HERE, "sim_v1_16x24.npz"), states=st, Rset=Rset, vin=vin, r_wire=2.93,
+                        omega=w, tol=1e-11, vup=u, vdown=d, iout=io, sweeps=sw)
+    # 128x128, four states drawn uniformly from seed 1, 1 V on every row
+    st = np.random.default_rng(1).integers(0, 4, (128, 128))
+    vin = np.ones(128)
+    for tol, tag in [(1e-8, "tol1e-8"), (1e-11, "tol1e-11")]:
+        u, d, io, sw = sim_run(st, Rset, vin, 2.93, 100000, w, tol)
+        rows = np.arange(0, 128, 8)
+        np.savez_compressed(os.path.join(HERE, "sim_v1_128_%s.npz" % tag), states=st, Rset=Rset, vin=vin,
+                            r_wire=2.93, omega=w, tol=tol, sample_rows=rows, vup_rows=u[rows], vdown_rows=d[rows],
+                            iout=io, sweeps=sw)
+    # the README's example: every cell in state 2
+    st = np.full((128, 128), 2)
+    u, d, io, sw = sim_run(st, Rset, vin, 2.93, 100000, w, 1e-8)
+    np.savez_compressed(os.path.join(HERE, "sim_v1_128_readme.npz"), states=st, Rset=Rset, vin=vin, r_wire=2.93,
+                        omega=w, tol=1e-8, iout=io, sweeps=sw)
+
+
+def import_pimtorch():
+    td = tempfile.mkdtemp(prefix="pimtorch_shim_")
+    pkg = os.path.join(td, "fixedPoint")
+    os.makedirs(os.path.join(pkg, "nn"))
+    open(os.path.join(pkg, "__init__.py"), "w").close()
+    open(os.path.join(pkg, "nn", "__init__.py"), "w").close()
+    for f in ["conductance_variation.py", "fixedPointArithmetic.py", "ir_drop_solve.py",
+              "splitArrayArithmetic.py", "ir_drop_compensate.py"]:
+        shutil.copy(os.path.join(NN, f), os.path.join(pkg, "nn", f))
+    with open(os.path.join(NN, "commonConst.py")) as f:
+        src = f.read()
+    # drop the import-time chdir and JIT build of the CUDA extension
+    src = re.sub(r"\n    print\(\"now the working dir is \{\}\.\"\.format\(os\.getcwd\(\)\)\)\n"
+                 r"    if os\.getcwd\(\)\[-5:\]!=\"point\":\n        os\.chdir\(\"\.\./\"\)\n"
+                 r"    cpp_ir_drop_accelerate = load\(.*?verbose = True\)\n",
+                 "\n    cpp_ir_drop_accelerate = None\n", src, flags=re.S)
+    assert "cpp_ir_drop_accelerate = None" in src, "commonConst.py layout changed"
+    with open(os.path.join(pkg, "nn", "commonConst.py"), "w") as f:
+        f.write(src)
+    sys.path.insert(0, td)
+    import fixedPoint.nn.commonConst as cc
+    import fixedPoint.nn.ir_drop_solve as ids
+    import fixedPoint.nn.splitArrayArithmetic as sa
+    return td, cc, ids, sa
+
+
+def set_params(cc, p):
+    P = cc.phyArrParams
+    for k in ["Ron", "Roff", "cellMaxConduct", "cellMinConduct", "cellBits", "arrRowSize", "arrColSize",
+              "inputMaxVoltage", "r_wire", "cellDeltaConduct", "adcUseI"]:
+        setattr(P, k, getattr(p, k))
+    P.crx_size = p.arrRowSize * p.arrColSize
+
+
+class _DroopSolve:
+    """Stand-in for the extension module: returns oracle.intstages.droop_solver."""
+
+    def ir_drop_gs(self, in_b, G, bsize, rows, cols, numX, numY, *rest):
+        import torch
+        return torch.from_numpy(intstages.droop_solver(in_b.numpy(), G.numpy(), bsize, rows, cols, numX, numY))
+
+
+def pimtorch_fixtures():
+    import torch
+    td, cc, ids, sa = import_pimtorch()
+    try:
+        # (a) the PimTorch GS sweep order, batchBybatch, fixed sweeps (and with break)
+        P = cc.phyArrParams
+        out = {}
+        rng = np.random.default_rng(11)
+        B, X, Y, n, m = 3, 2, 2, 8, 6
+        inp = (rng.integers(0, 2, (B, X, n)) * 0.2).astype(np.float64)
+        G = 1.0 / rng.choice([1e3, 2e4, 3e5, 1e6], size=(X, n, Y * m))
+        P.arrRowSize = n
+        P.ir_drop_GS_method_beta_scale = 1.9
+        P.ir_drop_GS_method_mode = cc.GS_method.batchBybatch
+        P.r_wire = 2.93
+        for dt, tag in [(torch.float64, "f64"), (torch.float32, "f32")]:
+            P.ir_drop_iter_time = 40
+            P.ir_drop_less_than_thresholdBreak_enable = False
+            r = ids.ir_drop_accurate_GSMethod(torch.tensor(inp, dtype=dt), torch.tensor(G, dtype=dt), B, X, Y, m)
+            out["fixed_" + tag] = r.numpy()
+            P.ir_drop_iter_time = 5000
+            P.ir_drop_less_than_thresholdBreak_enable = True
+            P.ir_drop_less_than_threshold = 1e-9 if tag == "f64" else 1e-6
+            r = ids.ir_drop_accurate_GSMethod(torch.tensor(inp, dtype=dt), torch.tensor(G, dtype=dt), B, X, Y, m)
+            out["break_" + tag] = r.numpy()
+        np.savez_compressed(os.path.join(HERE, "pimtorch_gs_8x6.npz"), input=inp, G=G, B=B, numX=X, numY=Y, rows=n,
+                            cols=m, omega=1.9, r_wire=2.93, fixed_iters=40, break_thr_f64=1e-9, break_thr_f32=1e-6,
+                            **out)
+        # (b) integer stages through splitArr_matmul_nn with a deterministic solve
+        P.cpp_ir_drop_accelerate_flag = True
+        P.cpp_ir_drop_accelerate = _DroopSolve()
+        P.IRdropMode = cc.ir_drop_mode.accurate_GS_math
+        P.useOUSize = False
+        P.sigma = 0
+        cases = [
+            ("c3like", dict(Ron=1e3, Roff=1e6, cellBits=2, rows=32, cols=32, inputMaxVoltage=0.2, adc_bits=8),
+             lambda r: r.integers(0, 256, (5, 100)).astype(np.float32),
+             lambda r: (r.standard_normal((100, 70)) * 0.05).astype(np.float32)),
+            ("signed", dict(Ron=1e3, Roff=1e6, cellBits=1, rows=64, cols=64, inputMaxVoltage=1.0, adc_bits=10),
+             lambda r: r.standard_normal((4, 150)).astype(np.float32),
+             lambda r: (r.standard_normal((150, 90)) * 0.1).astype(np.float32)),
+        ]
+        for name, kw, mkx, mkw in cases:
+            p = intstages.ArrayParams(**kw)
+            set_params(cc, p)
+            r = np.random.default_rng(len(name))
+            x, w = mkx(r), mkw(r)
+            cc.variations.reset_all()
+            y = sa.splitArr_matmul_nn(torch.from_numpy(x), torch.from_numpy(w), 8, 1, p.adc_bits, 10, 8,
+                                      cc.phyArrMode.PN, torch.float32)
+            np.savez_compressed(os.path.join(HERE, "pimtorch_split_%s.npz" % name), x=x, w=w, y=y.numpy(),
+                                **{k: v for k, v in kw.items()})
+    finally:
+        shutil.rmtree(td, ignore_errors=True)
+
+
+if __name__ == "__main__":
+    sim_fixtures()
+    pimtorch_fixtures()
+    print("fixtures written to", HERE)

@@ -1,0 +1,118 @@
+"""The CPU oracle against fixtures produced by the reference itself."""
+import numpy as np
+import pytest
+
+from oracle import augs, intstages, nodal, sweeps
+
+GW = 1 / 2.93
+
+
+def test_port_reproduces_reference_sim(gold):
+    z = gold("sim_v1_16x24.npz")
+    g = 1.0 / z["Rset"][z["states"]]
+    up, dn, io, sw = augs.solve(g, z["vin"], float(z["r_wire"]), 100000, float(z["omega"]), True, float(z["tol"]))
+    # the reference prints 13 significant digits
+    np.testing.assert_allclose(up, z["vup"], rtol=2e-12, atol=1e-15)
+    np.testing.assert_allclose(dn, z["vdown"], rtol=2e-12, atol=1e-17)
+    np.testing.assert_allclose(io, z["iout"], rtol=2e-11)
+    assert sw == int(z["sweeps"])
+
+
+def test_port_readme_config_sweeps(gold):
+    z = gold("sim_v1_128_readme.npz")
+    g = 1.0 / z["Rset"][z["states"]]
+    _, _, io, sw = augs.solve(g, z["vin"], 2.93, 100000, float(z["omega"]), True, 1e-8)
+    assert sw == int(z["sweeps"]) == 1513
+    np.testing.assert_allclose(io, z["iout"], rtol=2e-11)
+
+
+def test_direct_solve_matches_converged_reference(gold):
+    z = gold("sim_v1_16x24.npz")
+    g = 1.0 / z["Rset"][z["states"]]
+    u, d = nodal.solve(g, GW, z["vin"])
+    assert np.abs(u - z["vup"]).max() < 1e-9
+    assert np.abs(d - z["vdown"]).max() < 1e-9
+    z = gold("sim_v1_128_tol1e-11.npz")
+    g = 1.0 / z["Rset"][z["states"]]
+    u, d = nodal.solve(g, GW, z["vin"])
+    r = z["sample_rows"]
+    assert np.abs(u[r] - z["vup_rows"]).max() < 3e-9
+    assert np.abs(d[r] - z["vdown_rows"]).max() < 3e-9
+    np.testing.assert_allclose(nodal.currents(g, u, d), z["iout"], rtol=5e-8)
+
+
+def test_reference_delta_stop_is_loose(gold):
+    """At its own settings (tol 1e-8 on the sweep delta) the reference stops ~1e-6 V short."""
+    z = gold("sim_v1_128_tol1e-8.npz")
+    g = 1.0 / z["Rset"][z["states"]]
+    u, d = nodal.solve(g, GW, z["vin"])
+    r = z["sample_rows"]
+    err = max(np.abs(u[r] - z["vup_rows"]).max(), np.abs(d[r] - z["vdown_rows"]).max())
+    assert 5e-7 < err < 5e-6
+    assert int(z["sweeps"]) == 1509
+
+
+def test_dense_and_sparse_direct_agree():
+    rng = np.random.default_rng(3)
+    g = 1.0 / rng.choice([1e3, 1e4, 1e6], size=(12, 9))
+    vin = rng.random(12)
+    u1, d1 = nodal.solve(g, GW, vin)
+    u2, d2 = nodal.solve(g, GW, vin, dense=True)
+    assert np.abs(u1 - u2).max() < 1e-13 and np.abs(d1 - d2).max() < 1e-13
+    # several vectors at once give the same answer
+    V = rng.random((3, 12))
+    U, D = nodal.solve(g, GW, V)
+    u3, d3 = nodal.solve(g, GW, V[2])
+    assert np.abs(U[2] - u3).max() < 1e-14
+
+
+def test_direct_solve_kcl_residual():
+    rng = np.random.default_rng(4)
+    g = 1.0 / rng.choice([1e3, 1e6], size=(7, 5))
+    vin = rng.random(7)
+    A, b = nodal.assemble(g, GW, vin)
+    u, d = nodal.solve(g, GW, vin)
+    x = np.empty(2 * 35)
+    x[0::2] = u.ravel()
+    x[1::2] = d.ravel()
+    assert np.abs(A @ x - b).max() < 1e-14
+    # current into the array equals current out through the bitline terminals
+    i_in = (GW * (vin - u[:, 0])).sum()
+    i_out = (GW * d[-1, :]).sum()
+    assert abs(i_in - i_out) < 1e-12 * abs(i_in) + 1e-18
+
+
+@pytest.mark.parametrize("dt,tol", [(np.float64, 1e-13), (np.float32, 5e-6)])
+def test_sweep_order_matches_pimtorch(gold, dt, tol):
+    z = gold("pimtorch_gs_8x6.npz")
+    B, X, Y, n, m = [int(z[k]) for k in ["B", "numX", "numY", "rows", "cols"]]
+    tag = "f64" if dt == np.float64 else "f32"
+    r = sweeps.ir_drop_gs(z["input"].astype(dt), z["G"].astype(dt), B, n, m, X, Y, int(z["fixed_iters"]), GW,
+                          float(z["omega"]))
+    ref = z["fixed_" + tag]
+    assert np.abs(r - ref).max() <= tol * np.abs(ref).max()
+    r = sweeps.ir_drop_gs(z["input"].astype(dt), z["G"].astype(dt), B, n, m, X, Y, 5000, GW, float(z["omega"]),
+                          True, float(z["break_thr_" + tag]))
+    ref = z["break_" + tag]
+    assert np.abs(r - ref).max() <= 4 * tol * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["c3like", "signed"])
+def test_integer_stages_bit_exact(gold, name):
+    z = gold("pimtorch_split_%s.npz" % name)
+    kw = {k: z[k].item() for k in ["Ron", "Roff", "cellBits", "rows", "cols", "inputMaxVoltage", "adc_bits"]}
+    p = intstages.ArrayParams(**kw)
+    y = intstages.split_matmul(z["x"], z["w"], p, intstages.droop_solver)
+    assert y.dtype == np.float32
+    assert np.array_equal(y, z["y"])
+
+
+def test_converged_sweeps_reach_direct_solution():
+    """The sweep-order restatement converges to the direct solve (same system)."""
+    rng = np.random.default_rng(5)
+    n, m = 6, 5
+    g = 1.0 / rng.choice([1e3, 3e3, 1e4], size=(n, m))
+    vin = rng.random(n)
+    r = sweeps.ir_drop_gs(vin.reshape(1, 1, n), g.reshape(1, n, m), 1, n, m, 1, 1, 4000, GW, 1.5, ret_V=False)
+    u, d = nodal.solve(g, GW, vin)
+    np.testing.assert_allclose(r.reshape(m), nodal.currents(g, u, d), rtol=1e-10)
