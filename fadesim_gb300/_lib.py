@@ -1,0 +1,64 @@
+"""ctypes binding of ``libfadesim_gb300.so`` (the C ABI in include/fadesim_gb300.h).
+
+The library is built in-tree by ``fadesim_gb300.build``.  There is no fallback:
+if the library cannot be loaded every solve raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfadesim_gb300.so")
+
+F32 = 0
+F64 = 1
+METHOD_AUTO, METHOD_LINE, METHOD_RBSOR, METHOD_SWEEPS = 0, 1, 2, 3
+ST_CONVERGED, ST_MAXITER, ST_NONFINITE = 1, 2, 4
+
+
+class SolveOpts(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int), ("tol_v", ctypes.c_double), ("max_iters", ctypes.c_int),
+                ("residual_period", ctypes.c_int), ("omega", ctypes.c_double), ("vectors_per_cta", ctypes.c_int)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("solves", ctypes.c_int64), ("iters_sum", ctypes.c_int64), ("iters_max", ctypes.c_int),
+                ("status_or", ctypes.c_int)]
+
+
+_lib = None
+
+_vp = ctypes.c_void_p
+_i = ctypes.c_int
+_d = ctypes.c_double
+
+EXPORTS = {
+    "fadesim_ir_drop_gs_f32": [_vp, _vp, _i, _i, _i, _i, _i, _i, _d, _d, _i, _d, _i, _vp, _i, _i, _vp, _vp],
+    "fadesim_ir_drop_gs_f64": [_vp, _vp, _i, _i, _i, _i, _i, _i, _d, _d, _i, _d, _i, _vp, _i, _i, _vp, _vp],
+    "fadesim_ir_drop_gs_ex": [_i, _vp, _vp, _i, _i, _i, _i, _i, _i, _d, _d, _i, _d, _i, _vp, _i, _i, _vp,
+                              ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _vp, _vp],
+    "fadesim_last_error": [],
+    "fadesim_version": [],
+}
+
+
+def load():
+    """Load the library once; raise ImportError with the reason if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libfadesim_gb300.so is not built (run fadesim_gb300.build.build()); "
+                          "there is no CPU fallback")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, args in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_char_p if name in ("fadesim_last_error", "fadesim_version") else ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def check(rc):
+    if rc != 0:
+        msg = load().fadesim_last_error().decode()
+        raise RuntimeError(msg or ("fadesim call failed with code %d" % rc))

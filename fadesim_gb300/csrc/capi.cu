@@ -1,0 +1,238 @@
+// C ABI of the solver (include/fadesim_gb300.h): argument checks, method
+// choice, scratch and launches.  Scratch is stream-ordered (cudaMallocAsync /
+// cudaFreeAsync on the caller's stream), so a call never synchronises unless
+// the caller asks for stats or the reference's delta break.
+#include <math.h>
+#include <stdio.h>
+
+#include <string>
+
+#include "kernels.h"
+
+using namespace fadesim;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(x)                                                                            \
+    do {                                                                                       \
+        cudaError_t e_ = (x);                                                                  \
+        if (e_ != cudaSuccess) return fail(FADESIM_E_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" const char *fadesim_last_error(void) { return g_err.c_str(); }
+extern "C" const char *fadesim_version(void) { return "fadesim_gb300 0.1 (sm_103a)"; }
+
+namespace {
+
+struct Scratch {
+    void *p = nullptr;
+    cudaStream_t st = nullptr;
+    ~Scratch() {
+        if (p) cudaFreeAsync(p, st);
+    }
+};
+
+int device_sms() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+// Work split: whole tiles per item when there are enough tiles, else vectors
+// of one tile spread over several items.
+void plan_items(SolveArgs &a, int grid, int vectors_per_cta) {
+    const long long tiles = (long long)a.numX * a.numY;
+    int vchunk;
+    if (vectors_per_cta > 0) {
+        vchunk = vectors_per_cta;
+    } else {
+        long long want_items = 2LL * grid;
+        long long chunks = (want_items + tiles - 1) / tiles;
+        if (chunks < 1) chunks = 1;
+        if (chunks > a.B) chunks = a.B;
+        vchunk = (int)((a.B + chunks - 1) / chunks);
+    }
+    if (vchunk < 1) vchunk = 1;
+    if (vchunk > a.B) vchunk = a.B;
+    a.vchunk = vchunk;
+    a.nchunks = (a.B + vchunk - 1) / vchunk;
+    a.nitems = tiles * a.nchunks;
+}
+
+int finish_stats(DevStats *dst, fadesim_solve_stats *stats, cudaStream_t st) {
+    if (!stats) return FADESIM_OK;
+    DevStats h;
+    CUDA_TRY(cudaMemcpyAsync(&h, dst, sizeof(h), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    stats->solves = (int64_t)h.solves;
+    stats->iters_sum = (int64_t)h.iters_sum;
+    stats->iters_max = h.iters_max;
+    stats->status_or = h.status_or;
+    return FADESIM_OK;
+}
+
+int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts *opts, fadesim_solve_stats *stats,
+                   cudaStream_t st) {
+    const int L = a.n > a.m ? a.n : a.m;
+    a.ctl.tol_v = (opts && opts->tol_v > 0) ? (float)opts->tol_v : 1e-8f;
+    a.ctl.residual_period = (opts && opts->residual_period > 0) ? opts->residual_period : 4;
+    const int sms = device_sms();
+    int grid = 0, ld = 0;
+    size_t scratch_floats = 0;
+    if (method == FADESIM_METHOD_LINE) {
+        ld = line_relax_ld(a.n, a.m);
+        if (!ld) return fail(FADESIM_E_UNSUPPORTED, "line relaxation in this build handles rows, cols <= 128");
+        a.ctl.max_iters = (opts && opts->max_iters > 0) ? opts->max_iters : 400;
+        a.ctl.omega = (opts && opts->omega > 0) ? (float)opts->omega : 0.f;
+        CUDA_TRY(line_relax_prepare(ld, dtype));
+        int per_sm = 0;
+        CUDA_TRY(line_relax_occupancy(ld, dtype, &per_sm));
+        if (per_sm < 1) return fail(FADESIM_E_CUDA, "line relaxation kernel does not fit on this device");
+        grid = per_sm * sms;
+        plan_items(a, grid, opts ? opts->vectors_per_cta : 0);
+        if ((long long)grid > a.nitems) grid = (int)a.nitems;
+        scratch_floats = line_relax_scratch_floats_per_cta(ld) * grid;
+    } else {
+        if (L > 128) return fail(FADESIM_E_UNSUPPORTED, "red-black SOR in this build handles rows, cols <= 128");
+        a.ctl.max_iters = (opts && opts->max_iters > 0) ? opts->max_iters : 20000;
+        a.ctl.omega = (opts && opts->omega > 0) ? (float)opts->omega
+                                                : (float)(2.0 / (1.0 + sin(M_PI / (2.0 * L + 1.0))));
+        CUDA_TRY(rbsor_prepare(dtype));
+        grid = sms;
+        plan_items(a, grid, opts ? opts->vectors_per_cta : 0);
+        if ((long long)grid > a.nitems) grid = (int)a.nitems;
+    }
+    Scratch scr;
+    scr.st = st;
+    const size_t bytes = scratch_floats * sizeof(float) + sizeof(DevStats) + 256;
+    CUDA_TRY(cudaMallocAsync(&scr.p, bytes, st));
+    DevStats *dst = reinterpret_cast<DevStats *>(scr.p);
+    a.stats = dst;
+    a.scratch = reinterpret_cast<float *>(reinterpret_cast<char *>(scr.p) + 256);
+    CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(DevStats), st));
+    if (method == FADESIM_METHOD_LINE) {
+        CUDA_TRY(launch_line_relax(a, ld, dtype, grid, st));
+    } else {
+        CUDA_TRY(launch_rbsor(a, dtype, grid, st));
+    }
+    return finish_stats(dst, stats, st);
+}
+
+int run_sweeps(int dtype, SolveArgs a, int iter_times, double gw, double beta, int enable_break, double thr,
+               fadesim_solve_stats *stats, int *iters_out, cudaStream_t st) {
+    if (a.n > 1024 || a.m > 1024) return fail(FADESIM_E_ARG, "row_size and col_size must be <= 1024");
+    const size_t es = dtype == FADESIM_F64 ? 8 : 4;
+    const size_t plane = (size_t)a.B * a.numX * a.numY * a.n * a.m * es;
+    Scratch scr;
+    scr.st = st;
+    CUDA_TRY(cudaMallocAsync(&scr.p, 2 * plane + 256, st));
+    unsigned int *moved = reinterpret_cast<unsigned int *>(scr.p);
+    void *U = reinterpret_cast<char *>(scr.p) + 256;
+    void *D = reinterpret_cast<char *>(U) + plane;
+    CUDA_TRY(launch_sweep_init(a, dtype, U, D, st));
+    int done = 0;
+    for (int it = 0; it < iter_times; ++it) {
+        if (enable_break) CUDA_TRY(cudaMemsetAsync(moved, 0, sizeof(unsigned int), st));
+        CUDA_TRY(launch_sweep(a, dtype, U, D, gw, beta, thr, enable_break ? moved : nullptr, st));
+        ++done;
+        if (enable_break) {
+            unsigned int h = 0;
+            CUDA_TRY(cudaMemcpyAsync(&h, moved, sizeof(h), cudaMemcpyDeviceToHost, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+            if (h == 0) break;
+        }
+    }
+    CUDA_TRY(launch_sweep_output(a, dtype, U, D, st));
+    if (iters_out) {
+        // every solve ran the same number of sweeps
+        const size_t nsol = (size_t)a.B * a.numX * a.numY;
+        std::string tmp(nsol * sizeof(int), '\0');
+        int *h = reinterpret_cast<int *>(&tmp[0]);
+        for (size_t k = 0; k < nsol; ++k) h[k] = done;
+        CUDA_TRY(cudaMemcpyAsync(iters_out, h, nsol * sizeof(int), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    if (stats) {
+        stats->solves = (int64_t)a.B * a.numX * a.numY;
+        stats->iters_sum = stats->solves * done;
+        stats->iters_max = done;
+        stats->status_or = (enable_break && done < iter_times) ? FADESIM_ST_CONVERGED : FADESIM_ST_MAXITER;
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    return FADESIM_OK;
+}
+
+}  // namespace
+
+extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G, int batch_size, int row_size,
+                                     int col_size, int numX, int numY, int iter_times, double g_wire, double beta,
+                                     int enable_break, double break_threshould, int nonlinear_cell_enable,
+                                     const double *nonlinear_params, int n_nonlinear_params, int ret_V, void *out,
+                                     const fadesim_solve_opts *opts, fadesim_solve_stats *stats,
+                                     int *per_solve_iters, void *stream) {
+    g_err.clear();
+    if (dtype != FADESIM_F32 && dtype != FADESIM_F64) return fail(FADESIM_E_ARG, "dtype must be f32 or f64");
+    if (!input || !G || !out) return fail(FADESIM_E_ARG, "input, G and out must be device pointers");
+    if (row_size < 2) return fail(FADESIM_E_ARG, "row_size should be >=2");
+    if (col_size < 2) return fail(FADESIM_E_ARG, "col_size should be >=2");
+    if (batch_size < 0 || numX < 1 || numY < 1) return fail(FADESIM_E_ARG, "batch_size >= 0, numX >= 1, numY >= 1");
+    if (!(g_wire > 0) || !isfinite(g_wire)) return fail(FADESIM_E_ARG, "g_wire must be positive and finite");
+    if (nonlinear_cell_enable) {
+        (void)nonlinear_params;
+        (void)n_nonlinear_params;
+        return fail(FADESIM_E_UNSUPPORTED, "nonlinear cells are not implemented in this build");
+    }
+    if (stats) *stats = fadesim_solve_stats{0, 0, 0, 0};
+    if (batch_size == 0) return FADESIM_OK;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    SolveArgs a{};
+    a.input = input;
+    a.G = G;
+    a.out = out;
+    a.B = batch_size;
+    a.n = row_size;
+    a.m = col_size;
+    a.numX = numX;
+    a.numY = numY;
+    a.gw = (float)g_wire;
+    a.ret_V = ret_V == 2 ? 2 : (ret_V ? 1 : 0);
+    a.iters_out = per_solve_iters;
+    int method = opts ? opts->method : FADESIM_METHOD_AUTO;
+    if (method == FADESIM_METHOD_AUTO) method = line_relax_ld(row_size, col_size) ? FADESIM_METHOD_LINE : FADESIM_METHOD_SWEEPS;
+    switch (method) {
+        case FADESIM_METHOD_LINE:
+        case FADESIM_METHOD_RBSOR:
+            return run_converging(method, dtype, a, opts, stats, st);
+        case FADESIM_METHOD_SWEEPS:
+            if (iter_times < 0) return fail(FADESIM_E_ARG, "iter_times must be >= 0");
+            return run_sweeps(dtype, a, iter_times, g_wire, beta, enable_break, break_threshould, stats,
+                              per_solve_iters, st);
+    }
+    return fail(FADESIM_E_ARG, "unknown method");
+}
+
+extern "C" int fadesim_ir_drop_gs_f32(const float *input, const float *G, int batch_size, int row_size, int col_size,
+                                      int numX, int numY, int iter_times, double g_wire, double beta,
+                                      int enable_break, double break_threshould, int nonlinear_cell_enable,
+                                      const double *nonlinear_params, int n_nonlinear_params, int ret_V, float *out,
+                                      void *stream) {
+    return fadesim_ir_drop_gs_ex(FADESIM_F32, input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire,
+                                 beta, enable_break, break_threshould, nonlinear_cell_enable, nonlinear_params,
+                                 n_nonlinear_params, ret_V, out, nullptr, nullptr, nullptr, stream);
+}
+
+extern "C" int fadesim_ir_drop_gs_f64(const double *input, const double *G, int batch_size, int row_size,
+                                      int col_size, int numX, int numY, int iter_times, double g_wire, double beta,
+                                      int enable_break, double break_threshould, int nonlinear_cell_enable,
+                                      const double *nonlinear_params, int n_nonlinear_params, int ret_V, double *out,
+                                      void *stream) {
+    return fadesim_ir_drop_gs_ex(FADESIM_F64, input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire,
+                                 beta, enable_break, break_threshould, nonlinear_cell_enable, nonlinear_params,
+                                 n_nonlinear_params, ret_V, out, nullptr, nullptr, nullptr, stream);
+}

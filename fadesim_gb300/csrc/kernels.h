@@ -1,0 +1,48 @@
+// Host-side launch interface of the solver kernels (internal to the library).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace fadesim {
+
+// Arguments common to the per-(tile, vector) solve kernels.  Layouts are the
+// reference extension's (split_arr_matmul.cu:200-203,238,310-332).
+struct SolveArgs {
+    const void *input;  // [B, numX, n]
+    const void *G;      // [numX, n, numY*m]
+    void *out;          // [B, numX, numY*m] or, with ret_V, [B, numX, numY, n, m]
+    int B, n, m, numX, numY;
+    float gw;           // wire conductance 1/r_wire
+    int ret_V;
+    int vchunk;         // vectors per work item
+    int nchunks;        // work items per tile
+    long long nitems;   // tiles * nchunks
+    SolveCtl ctl;
+    float *scratch;     // per-CTA scratch (kernel specific)
+    int *iters_out;     // optional [B, numX, numY]
+    DevStats *stats;    // optional
+};
+
+// Block line relaxation, planes resident in shared memory (n, m <= 128).
+// Returns the LD (32/64/128) used, or 0 if the shape does not fit.
+int line_relax_ld(int n, int m);
+size_t line_relax_smem(int ld);
+int line_relax_threads(int ld);
+size_t line_relax_scratch_floats_per_cta(int ld);
+cudaError_t line_relax_prepare(int ld, int dtype);
+cudaError_t line_relax_occupancy(int ld, int dtype, int *ctas_per_sm);
+cudaError_t launch_line_relax(const SolveArgs &a, int ld, int dtype, int grid, cudaStream_t st);
+
+// Plain red-black point SOR, planes resident in shared memory (n, m <= 128).
+size_t rbsor_smem(int n, int m);
+cudaError_t rbsor_prepare(int dtype);
+cudaError_t launch_rbsor(const SolveArgs &a, int dtype, int grid, cudaStream_t st);
+
+// The reference's sweep order (split_arr_matmul.cu:27-119), one sweep per launch.
+cudaError_t launch_sweep(const SolveArgs &a, int dtype, void *U, void *D, double gw, double beta,
+                         double thr, unsigned int *moved, cudaStream_t st);
+cudaError_t launch_sweep_init(const SolveArgs &a, int dtype, void *U, void *D, cudaStream_t st);
+cudaError_t launch_sweep_output(const SolveArgs &a, int dtype, const void *U, const void *D, cudaStream_t st);
+
+}  // namespace fadesim

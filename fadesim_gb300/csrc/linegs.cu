@@ -1,0 +1,439 @@
+// Block line relaxation for the crossbar nodal system (sm_103a).
+//
+// The reference relaxes one node at a time (split_arr_matmul.cu:27-119,
+// crossbarHspice/2dArray.cc:1551-1590).  Its two planes are coupled only
+// through the cell conductance, which is 1e-6..1e-3 of the wire conductance,
+// so the natural blocks are whole lines: every wordline row is a tridiagonal
+// system in its own unknowns once the bitline plane is fixed, and every
+// bitline column is one once the wordline plane is fixed.  One iteration here
+// solves all wordlines exactly, then all bitlines exactly (block Gauss-Seidel,
+// optionally over-relaxed).  It converges to the same fixed point as the
+// reference's point sweeps: the nodal solution.
+//
+// Numerics.  Unknowns are deviations from the ideal state (wordline u - vin,
+// bitline d), so FP32 resolves ~1e-9 V.  Each line solve is a correction
+// x += omega * T^-1 r with r the line's residual computed from differences of
+// neighbouring values (FP32, or FP64 every residual_period iterations and for
+// the final convergence test) and T the line's tridiagonal matrix factored
+// once per tile (FP64 pivots rounded to FP32).  Forming T's diagonal in FP32
+// loses the cell term, so a direct (non-residual) FP32 line solve would stall
+// near 1e-5 V; in residual form that rounding only slows convergence.
+//
+// Mapping.  One CTA owns one tile at a time and solves its input vectors one
+// after another with the tile's conductances and both deviation planes in
+// shared memory (3 x LD x LD floats).  A warp handles 8 lines x 4 segments of
+// SEG = LD/4 nodes; a thread keeps its segment in registers, folds the Thomas
+// recurrences locally and joins segments with a 2-step affine scan over the
+// 4 lanes of its line (__shfl at stride 8).  Planes are stored row-major with
+// an XOR swizzle so that both the row walk (wordline pass) and the column walk
+// (bitline pass) hit 32 distinct banks.
+#include <math.h>
+
+#include "kernels.h"
+
+namespace fadesim {
+
+template <int LD>
+struct LineCfg {
+    static constexpr int T = LD * 4;    // threads per CTA
+    static constexpr int SEG = LD / 4;  // nodes per thread segment
+    static constexpr int NW = LD / 8;   // warps
+};
+
+template <int LD>
+__device__ __forceinline__ int swz(int r, int c) {
+    constexpr int SEG = LD / 4;
+    const int s = ((((r / SEG) ^ (c / SEG)) & 3) << 3) | (r & 7);
+    return r * LD + (c ^ s);
+}
+
+template <typename T>
+__device__ __forceinline__ T ldg_t(const T *p) { return __ldg(p); }
+
+// One pass over all lines of one plane.  WORD: wordline rows (own plane = U
+// deviations, other = D); else bitline columns (own = D, other = U).
+template <int LD, bool WORD, bool RES64>
+__device__ __forceinline__ void line_pass(float *__restrict__ own, const float *__restrict__ oth,
+                                          const float *__restrict__ Gs, const float *__restrict__ vin_s,
+                                          const float *__restrict__ piv, int L, int NL, float gw, float omega,
+                                          float &dmax, float &vmax) {
+    constexpr int SEG = LineCfg<LD>::SEG;
+    constexpr int T = LineCfg<LD>::T;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int s = lane >> 3;
+    const int line = (tid >> 5) * 8 + (lane & 7);
+    const bool line_ok = line < NL;
+    const int p0 = s * SEG;
+    auto at = [&](int p) { return WORD ? swz<LD>(line, p) : swz<LD>(p, line); };
+
+    float x[SEG];
+    // ---- residual of the line equations at the current iterate -------------
+    {
+        const float vl = (WORD && line_ok) ? vin_s[line] : 0.f;
+        float prev = (line_ok && p0 > 0 && p0 - 1 < L) ? own[at(p0 - 1)] : 0.f;
+        float cur = (line_ok && p0 < L) ? own[at(p0)] : 0.f;
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) {
+            const int p = p0 + k;
+            const bool valid = line_ok && p < L;
+            const float nxt = (line_ok && p + 1 < L) ? own[at(p + 1)] : 0.f;
+            float r = 0.f;
+            if (valid) {
+                const int q = at(p);
+                const float g = Gs[q];
+                const float o = oth[q];
+                // WORD: left link always present (the source at p == 0, deviation 0),
+                //       right link absent at the open end.
+                // BIT:  upper link absent at the open top, lower link always present
+                //       (ground below the last node, deviation 0).
+                const float gl = WORD ? gw : (p > 0 ? gw : 0.f);
+                const float gr = WORD ? (p + 1 < L ? gw : 0.f) : gw;
+                if (RES64) {
+                    const double src = WORD ? ((double)o - (double)vl) - (double)cur
+                                            : ((double)o + (double)vin_s[p]) - (double)cur;
+                    const double rr = (double)gl * ((double)prev - (double)cur) +
+                                      (double)gr * ((double)nxt - (double)cur) + (double)g * src;
+                    r = (float)rr;
+                } else {
+                    const float src = WORD ? (o - vl) - cur : (o + vin_s[p]) - cur;
+                    r = gl * (prev - cur) + gr * (nxt - cur) + g * src;
+                }
+            }
+            x[k] = r;
+            prev = cur;
+            cur = nxt;
+        }
+    }
+    // ---- T^-1 r by Thomas, segmented over 4 lanes ---------------------------
+    float ip[SEG];
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) ip[k] = piv[k * T + tid];
+    // forward elimination: y_p = ip_p r_p + (gw ip_p) y_{p-1}
+    float y = 0.f, A = 1.f;
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) {
+        const float a = (p0 + k == 0) ? 0.f : gw * ip[k];
+        y = fmaf(a, y, ip[k] * x[k]);
+        x[k] = y;
+        A *= a;
+    }
+    float Ai = A, Yi = y;
+#pragma unroll
+    for (int off = 1; off < 4; off <<= 1) {
+        const float Ap = __shfl_up_sync(0xffffffffu, Ai, 8 * off);
+        const float Yp = __shfl_up_sync(0xffffffffu, Yi, 8 * off);
+        if (s >= off) {
+            Yi = fmaf(Ai, Yp, Yi);
+            Ai *= Ap;
+        }
+    }
+    float yin = __shfl_up_sync(0xffffffffu, Yi, 8);
+    if (s == 0) yin = 0.f;
+    {
+        float P = 1.f;
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) {
+            const float a = (p0 + k == 0) ? 0.f : gw * ip[k];
+            P *= a;
+            x[k] = fmaf(P, yin, x[k]);
+        }
+    }
+    // back substitution: x_p = y_p + (gw ip_p) x_{p+1}
+    float X = 0.f, Bm = 1.f;
+#pragma unroll
+    for (int k = SEG - 1; k >= 0; --k) {
+        const float b = (p0 + k + 1 >= L) ? 0.f : gw * ip[k];
+        X = fmaf(b, X, x[k]);
+        x[k] = X;
+        Bm *= b;
+    }
+    float Bi = Bm, Xi = X;
+#pragma unroll
+    for (int off = 1; off < 4; off <<= 1) {
+        const float Bn = __shfl_down_sync(0xffffffffu, Bi, 8 * off);
+        const float Xn = __shfl_down_sync(0xffffffffu, Xi, 8 * off);
+        if (s + off < 4) {
+            Xi = fmaf(Bi, Xn, Xi);
+            Bi *= Bn;
+        }
+    }
+    float xin = __shfl_down_sync(0xffffffffu, Xi, 8);
+    if (s == 3) xin = 0.f;
+    {
+        float Q = 1.f;
+#pragma unroll
+        for (int k = SEG - 1; k >= 0; --k) {
+            const float b = (p0 + k + 1 >= L) ? 0.f : gw * ip[k];
+            Q *= b;
+            x[k] = fmaf(Q, xin, x[k]);
+        }
+    }
+    // ---- apply the correction ----------------------------------------------
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) {
+        const int p = p0 + k;
+        if (line_ok && p < L) {
+            const int q = at(p);
+            const float dx = omega * x[k];
+            const float nv = own[q] + dx;
+            own[q] = nv;
+            dmax = fmaxf(dmax, fabsf(dx));
+            vmax = fmaxf(vmax, fabsf(nv));
+        }
+    }
+}
+
+// FP64 pivots of every line of the tile, written in the order each pass thread
+// reads them (k * T + tid).
+template <int LD>
+__device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ piv, int n, int m, float gwf) {
+    constexpr int SEG = LineCfg<LD>::SEG;
+    constexpr int T = LineCfg<LD>::T;
+    const double gw = gwf;
+    const int tid = threadIdx.x;
+    if (tid < 2 * LD) {
+        const bool word = tid < LD;
+        const int line = word ? tid : tid - LD;
+        const int L = word ? m : n;
+        const int NL = word ? n : m;
+        float *dst = word ? piv : piv + SEG * T;
+        const int tw_base = (line >> 3) * 32 + (line & 7);
+        double p = 1.0;
+        for (int q = 0; q < LD; ++q) {
+            double ipv = 0.0;
+            if (line < NL && q < L) {
+                const double g = word ? Gs[swz<LD>(line, q)] : Gs[swz<LD>(q, line)];
+                // wordline: source link + right link (absent at the end) + cell
+                // bitline:  upper link (absent at the top) + lower link + cell
+                const double diag = word ? gw + (q + 1 < L ? gw : 0.0) + g : (q > 0 ? gw : 0.0) + gw + g;
+                p = (q == 0) ? diag : diag - gw * gw / p;
+                ipv = 1.0 / p;
+            }
+            const int tw = tw_base + (q / SEG) * 8;
+            dst[(q % SEG) * T + tw] = (float)ipv;
+        }
+    }
+}
+
+template <int LD, typename TIO>
+__global__ void __launch_bounds__(LD * 4, (LD >= 128 ? 1 : (LD == 64 ? 2 : 4))) line_relax_kernel(SolveArgs a) {
+    constexpr int T = LineCfg<LD>::T;
+    constexpr int NW = LineCfg<LD>::NW;
+    constexpr int SEG = LineCfg<LD>::SEG;
+    extern __shared__ float4 smem4[];
+    float *Gs = reinterpret_cast<float *>(smem4);
+    float *U = Gs + LD * LD;
+    float *D = U + LD * LD;
+    float *vin_s = D + LD * LD;
+    float *red = vin_s + LD;  // [2][2][NW]
+
+    const int tid = threadIdx.x;
+    const int n = a.n, m = a.m;
+    const int ldG = a.numY * m;
+    const TIO *inp = static_cast<const TIO *>(a.input);
+    const TIO *Gg = static_cast<const TIO *>(a.G);
+    TIO *out = static_cast<TIO *>(a.out);
+    float *piv = a.scratch + (size_t)blockIdx.x * (2 * SEG * T);
+    const float gw = a.gw;
+    const float tol = a.ctl.tol_v;
+    const int kres = a.ctl.residual_period;
+    const int maxit = a.ctl.max_iters;
+    long long cached_tile = -1;
+
+    for (long long item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+        const long long tile = item / a.nchunks;
+        const int chunk = (int)(item % a.nchunks);
+        const int x = (int)(tile / a.numY), y = (int)(tile % a.numY);
+        const int b0 = chunk * a.vchunk;
+        const int b1 = min(a.B, b0 + a.vchunk);
+        if (tile != cached_tile) {
+            __syncthreads();
+            for (int e = tid; e < n * m; e += T) {
+                const int i = e / m, j = e - i * m;
+                Gs[swz<LD>(i, j)] = (float)Gg[((size_t)x * n + i) * ldG + (size_t)y * m + j];
+            }
+            __syncthreads();
+            line_pivots<LD>(Gs, piv, n, m, gw);
+            __syncthreads();
+            cached_tile = tile;
+        }
+        for (int b = b0; b < b1; ++b) {
+            __syncthreads();
+            for (int e = tid; e < LD * LD; e += T) {
+                U[e] = 0.f;
+                D[e] = 0.f;
+            }
+            if (tid < LD) vin_s[tid] = (tid < n) ? (float)inp[((size_t)b * a.numX + x) * n + tid] : 0.f;
+            __syncthreads();
+            float omega = a.ctl.omega > 0.f ? a.ctl.omega : 1.f;
+            const bool adapt = !(a.ctl.omega > 0.f);
+            float prev_delta = 0.f;
+            bool res64 = false;
+            int status = 0, it = 0, par = 0;
+            while (true) {
+                float dmax = 0.f, vmax = 0.f;
+                if (res64) line_pass<LD, true, true>(U, D, Gs, vin_s, piv, m, n, gw, omega, dmax, vmax);
+                else line_pass<LD, true, false>(U, D, Gs, vin_s, piv, m, n, gw, omega, dmax, vmax);
+                __syncthreads();
+                if (res64) line_pass<LD, false, true>(D, U, Gs, vin_s, piv + SEG * T, n, m, gw, omega, dmax, vmax);
+                else line_pass<LD, false, false>(D, U, Gs, vin_s, piv + SEG * T, n, m, gw, omega, dmax, vmax);
+                dmax = warp_max(dmax);
+                vmax = warp_max(vmax);
+                if ((tid & 31) == 0) {
+                    red[(par * 2 + 0) * NW + (tid >> 5)] = dmax;
+                    red[(par * 2 + 1) * NW + (tid >> 5)] = vmax;
+                }
+                __syncthreads();
+                float delta = 0.f, vm = 0.f;
+#pragma unroll
+                for (int w = 0; w < NW; ++w) {
+                    delta = fmaxf(delta, red[(par * 2 + 0) * NW + w]);
+                    vm = fmaxf(vm, red[(par * 2 + 1) * NW + w]);
+                }
+                par ^= 1;
+                ++it;
+                if (!isfinite(delta) || !isfinite(vm)) {
+                    status = FADESIM_ST_NONFINITE;
+                    break;
+                }
+                // stop test: delta * rho / (1 - rho) below the target, rho the
+                // observed contraction (bounded below by omega-1, the SOR rate)
+                // FP32 resolution of the deviation planes: changes below a few
+                // ulps of the largest deviation are rounding, not progress
+                const float floor_v = 4.f * 1.1920929e-07f * vm;
+                bool small;
+                if (it == 1) {
+                    small = delta <= 0.f;
+                } else {
+                    const float ratio = prev_delta > 0.f ? delta / prev_delta : 0.f;
+                    const float rho = fmaxf(ratio, omega - 1.f);
+                    const float est = rho < 0.999f ? delta * rho / (1.f - rho) : INFINITY;
+                    const bool stalled = delta <= 8.f * floor_v && ratio >= 0.5f;
+                    small = est <= fmaxf(tol, floor_v) || stalled;
+                    if (adapt && it == 3 && ratio > 0.05f && ratio < 1.f) {
+                        omega = fminf(1.9f, 2.f / (1.f + sqrtf(1.f - ratio)));
+                    }
+                }
+                if (small) {
+                    if (res64) {
+                        status = FADESIM_ST_CONVERGED;
+                        break;
+                    }
+                    res64 = true;
+                } else {
+                    res64 = (kres > 0) && (it % kres == 0);
+                }
+                if (it >= maxit) {
+                    status = FADESIM_ST_MAXITER;
+                    break;
+                }
+                prev_delta = delta;
+            }
+            // ---- outputs ------------------------------------------------------
+            if (a.ret_V) {
+                for (int e = tid; e < n * m; e += T) {
+                    const int i = e / m, j = e - i * m;
+                    const int q = swz<LD>(i, j);
+                    const TIO uu = (TIO)U[q] + (TIO)vin_s[i];
+                    const size_t sol = ((size_t)b * a.numX + x) * a.numY + y;
+                    if (a.ret_V == 2) {
+                        out[(sol * 2 + 0) * n * m + (size_t)i * m + j] = uu;
+                        out[(sol * 2 + 1) * n * m + (size_t)i * m + j] = (TIO)D[q];
+                    } else {
+                        out[(sol * n + i) * m + j] = uu - (TIO)D[q];
+                    }
+                }
+            } else {
+                // bitline current I_j = sum_i g_ij (u_ij - d_ij), in the bitline mapping
+                const int lane = tid & 31;
+                const int s = lane >> 3;
+                const int j = (tid >> 5) * 8 + (lane & 7);
+                TIO acc = 0;
+                if (j < m) {
+                    for (int k = 0; k < SEG; ++k) {
+                        const int i = s * SEG + k;
+                        if (i < n) {
+                            const int q = swz<LD>(i, j);
+                            acc += (TIO)Gs[q] * (((TIO)U[q] + (TIO)vin_s[i]) - (TIO)D[q]);
+                        }
+                    }
+                }
+                acc += __shfl_down_sync(0xffffffffu, acc, 8);
+                acc += __shfl_down_sync(0xffffffffu, acc, 16);
+                if (s == 0 && j < m) out[((size_t)b * a.numX + x) * ldG + (size_t)y * m + j] = acc;
+            }
+            if (tid == 0) {
+                record_solve(a.stats, a.iters_out, ((long long)b * a.numX + x) * a.numY + y, it, status);
+            }
+        }
+    }
+}
+
+int line_relax_ld(int n, int m) {
+    const int L = n > m ? n : m;
+    if (L <= 32) return 32;
+    if (L <= 64) return 64;
+    if (L <= 128) return 128;
+    return 0;
+}
+
+size_t line_relax_smem(int ld) { return (size_t)(3 * ld * ld + ld + 4 * (ld / 8)) * sizeof(float); }
+int line_relax_threads(int ld) { return ld * 4; }
+size_t line_relax_scratch_floats_per_cta(int ld) { return (size_t)2 * (ld / 4) * (ld * 4); }
+
+template <int LD, typename TIO>
+static cudaError_t prep_one() {
+    return cudaFuncSetAttribute(line_relax_kernel<LD, TIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)line_relax_smem(LD));
+}
+
+cudaError_t line_relax_prepare(int ld, int dtype) {
+    switch (ld * 2 + dtype) {
+        case 64: return prep_one<32, float>();
+        case 65: return prep_one<32, double>();
+        case 128: return prep_one<64, float>();
+        case 129: return prep_one<64, double>();
+        case 256: return prep_one<128, float>();
+        case 257: return prep_one<128, double>();
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int LD, typename TIO>
+static cudaError_t occ_one(int *n) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, line_relax_kernel<LD, TIO>, LD * 4,
+                                                         line_relax_smem(LD));
+}
+
+cudaError_t line_relax_occupancy(int ld, int dtype, int *ctas) {
+    switch (ld * 2 + dtype) {
+        case 64: return occ_one<32, float>(ctas);
+        case 65: return occ_one<32, double>(ctas);
+        case 128: return occ_one<64, float>(ctas);
+        case 129: return occ_one<64, double>(ctas);
+        case 256: return occ_one<128, float>(ctas);
+        case 257: return occ_one<128, double>(ctas);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <int LD, typename TIO>
+static cudaError_t launch_one(const SolveArgs &a, int grid, cudaStream_t st) {
+    line_relax_kernel<LD, TIO><<<grid, LD * 4, line_relax_smem(LD), st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_line_relax(const SolveArgs &a, int ld, int dtype, int grid, cudaStream_t st) {
+    switch (ld * 2 + dtype) {
+        case 64: return launch_one<32, float>(a, grid, st);
+        case 65: return launch_one<32, double>(a, grid, st);
+        case 128: return launch_one<64, float>(a, grid, st);
+        case 129: return launch_one<64, double>(a, grid, st);
+        case 256: return launch_one<128, float>(a, grid, st);
+        case 257: return launch_one<128, double>(a, grid, st);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace fadesim

@@ -1,0 +1,105 @@
+/*
+ * fadesim_gb300: C ABI of the GB300 (sm_103a) crossbar IR-drop solver.
+ *
+ * All pointers passed to the solve entry points are DEVICE pointers (CUDA
+ * global memory on the current device) unless the comment says otherwise.
+ * Every call is asynchronous on the given CUDA stream (NULL = legacy default
+ * stream) and returns 0 on success or a negative FADESIM_E* code;
+ * fadesim_last_error() then gives a message.  Argument checks mirror the
+ * reference's TORCH_CHECKs (split_arr_matmul.cu:21-24,222-225).
+ *
+ * Layouts follow the reference extension (split_arr_matmul.cu:200-203,238):
+ *   input  [batch, numX, rows]              wordline drive voltages
+ *   G      [numX, rows, numY*cols]          cell conductances
+ *   out    [batch, numX, numY*cols]         bitline currents, or, with ret_V,
+ *          [batch, numX, numY, rows, cols]  cell voltages u - d
+ */
+#ifndef FADESIM_GB300_H
+#define FADESIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FADESIM_OK 0
+#define FADESIM_E_ARG (-1)       /* bad argument (size, pointer, option) */
+#define FADESIM_E_CUDA (-2)      /* a CUDA call failed */
+#define FADESIM_E_UNSUPPORTED (-3) /* valid request this build does not implement */
+
+/* dtype codes */
+#define FADESIM_F32 0
+#define FADESIM_F64 1
+
+/* solver methods */
+#define FADESIM_METHOD_AUTO 0      /* line relaxation where it fits, else sweep order */
+#define FADESIM_METHOD_LINE 1      /* block line relaxation, residual form, to tolerance */
+#define FADESIM_METHOD_RBSOR 2     /* plain red-black point SOR, residual form, to tolerance */
+#define FADESIM_METHOD_SWEEPS 3    /* the reference's sweep order for exactly iter_times sweeps */
+
+/* per-solve status bits (fadesim_solve_stats.status_or, per_solve_status) */
+#define FADESIM_ST_CONVERGED 1
+#define FADESIM_ST_MAXITER 2
+#define FADESIM_ST_NONFINITE 4
+
+typedef struct fadesim_solve_opts {
+    int method;            /* FADESIM_METHOD_* */
+    double tol_v;          /* target max node error in volts (converging methods); <=0: 1e-8 */
+    int max_iters;         /* cap on line iterations / point sweeps; <=0: method default */
+    int residual_period;   /* FP64 residual every k line iterations (and always for the final test); <=0: 4 */
+    double omega;          /* relaxation factor; <=0: adaptive (line) or autotuned table (rbsor) */
+    int vectors_per_cta;   /* input vectors one CTA solves per work item; <=0: automatic */
+} fadesim_solve_opts;
+
+typedef struct fadesim_solve_stats {
+    int64_t solves;        /* (tile, vector) solves run */
+    int64_t iters_sum;     /* sum over solves of iterations (line) or sweeps (rbsor, sweeps) */
+    int iters_max;
+    int status_or;         /* OR of per-solve status bits */
+} fadesim_solve_stats;
+
+/* Drop-in for the reference's ir_drop_gs (split_arr_matmul.cu:204-220, bound
+ * by PYBIND11_MODULE at :1429-1437 and called from
+ * pimtorch/.../nn/splitArrayArithmetic.py:488-511).  Same arguments, same
+ * meaning, same output.  The default method solves each (tile, vector) pair to
+ * tol_v = 1e-8 V against the converged nodal solution; iter_times, beta,
+ * enable_break and break_threshould keep their reference meaning only under
+ * FADESIM_METHOD_SWEEPS (see fadesim_ir_drop_gs_ex).  nonlinear_params holds
+ * [R_on, R_off, a_on, b_on, a_off, b_off] (commonConst.py:207) and is read only
+ * when nonlinear_cell_enable != 0. */
+int fadesim_ir_drop_gs_f32(const float *input, const float *G, int batch_size, int row_size, int col_size,
+                           int numX, int numY, int iter_times, double g_wire, double beta, int enable_break,
+                           double break_threshould, int nonlinear_cell_enable, const double *nonlinear_params,
+                           int n_nonlinear_params, int ret_V, float *out, void *stream);
+
+int fadesim_ir_drop_gs_f64(const double *input, const double *G, int batch_size, int row_size, int col_size,
+                           int numX, int numY, int iter_times, double g_wire, double beta, int enable_break,
+                           double break_threshould, int nonlinear_cell_enable, const double *nonlinear_params,
+                           int n_nonlinear_params, int ret_V, double *out, void *stream);
+
+/* Extended form of the same boundary (the optional entry the reference's
+ * interface leaves room for next to ir_drop_gs): explicit method and
+ * tolerance, ret_V = 2 for both node planes [batch, numX, numY, 2, rows, cols]
+ * (wordline u then bitline d), optional stats (HOST pointer, filled after a stream sync when not
+ * NULL) and optional per-solve iteration counts (DEVICE int32
+ * [batch, numX, numY]).  dtype is FADESIM_F32 or FADESIM_F64 and types input,
+ * G and out. */
+int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
+                          int numX, int numY, int iter_times, double g_wire, double beta, int enable_break,
+                          double break_threshould, int nonlinear_cell_enable, const double *nonlinear_params,
+                          int n_nonlinear_params, int ret_V, void *out, const fadesim_solve_opts *opts,
+                          fadesim_solve_stats *stats, int *per_solve_iters, void *stream);
+
+/* Message for the last failing call on this thread. */
+const char *fadesim_last_error(void);
+
+/* Library version string. */
+const char *fadesim_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FADESIM_GB300_H */

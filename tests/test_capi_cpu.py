@@ -1,0 +1,47 @@
+"""The C-ABI library loads and exports every function include/*.h declares (no GPU needed)."""
+import ctypes
+import glob
+import os
+import re
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s*(fadesim_[a-z0-9_]+)\s*\(", src,
+                             flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    assert {"fadesim_ir_drop_gs_f32", "fadesim_ir_drop_gs_f64", "fadesim_ir_drop_gs_ex",
+            "fadesim_last_error"} <= names
+
+
+def test_library_exports_declared_symbols():
+    from fadesim_gb300 import _lib
+    from fadesim_gb300.build import build
+    build()
+    lib = _lib.load()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+    assert b"sm_103a" in lib.fadesim_version()
+
+
+def test_argument_errors_without_gpu():
+    """Argument checks run before any CUDA call and report like the reference's TORCH_CHECKs."""
+    from fadesim_gb300 import _lib
+    lib = _lib.load()
+    fake = ctypes.c_void_p(16)
+    rc = lib.fadesim_ir_drop_gs_f32(fake, fake, 1, 1, 8, 1, 1, 10, 0.34, 1.9, 0, 0.0, 0, None, 0, 0, fake, None)
+    assert rc == -1 and b"row_size" in lib.fadesim_last_error()
+    rc = lib.fadesim_ir_drop_gs_f32(fake, fake, 1, 8, 8, 1, 1, 10, -1.0, 1.9, 0, 0.0, 0, None, 0, 0, fake, None)
+    assert rc == -1 and b"g_wire" in lib.fadesim_last_error()
+    rc = lib.fadesim_ir_drop_gs_f32(None, fake, 1, 8, 8, 1, 1, 10, 0.34, 1.9, 0, 0.0, 0, None, 0, 0, fake, None)
+    assert rc == -1

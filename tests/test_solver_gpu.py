@@ -1,0 +1,189 @@
+"""Parity of the CUDA solver with the oracle, through the drop-in module.
+
+Every converging method must land within 1e-6 V of the FP64 direct solve on
+every node of both planes and within 1e-4 relative on bitline currents (the
+contract); the line solver is held to a tighter 2e-8 V / 1e-6 where the cells
+are weak.  The reference-order method must reproduce the reference's own
+iterates (FP64 to 1e-12 relative).
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from oracle import nodal, sweeps  # noqa: E402
+
+GW = 1 / 2.93
+V_TOL = 1e-6       # max node error vs the FP64 oracle (V)
+I_RTOL = 1e-4      # bitline current, relative to the largest current
+
+
+@pytest.fixture(scope="module")
+def acc():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fadesim_gb300 import cpp_ir_drop_accelerate as m
+    return m
+
+
+def make_case(seed, B, X, Y, n, m, Rset, vmax, bern=True):
+    rng = np.random.default_rng(seed)
+    G = 1.0 / np.asarray(Rset)[rng.integers(0, len(Rset), (X, n, Y * m))]
+    if bern:
+        inp = rng.integers(0, 2, (B, X, n)) * vmax
+    else:
+        inp = rng.random((B, X, n)) * vmax
+    return inp.astype(np.float64), G
+
+
+def oracle_planes(inp, G, B, X, Y, n, m):
+    out, U, D = nodal.solve_layer(inp, G, n, m, X, Y, GW, return_planes=True)
+    return out, U, D
+
+
+def run(acc, inp, G, B, X, Y, n, m, dtype=torch.float32, ret_V=2, **kw):
+    ti = torch.tensor(inp, dtype=dtype, device="cuda").contiguous()
+    tg = torch.tensor(G, dtype=dtype, device="cuda").contiguous()
+    out, stats, iters = acc.ir_drop_gs_ex(ti, tg, B, n, m, X, Y, ret_V=ret_V, return_iters=True, **kw)
+    torch.cuda.synchronize()
+    return out.double().cpu().numpy(), stats, iters.cpu().numpy()
+
+
+CFG1 = [2e6, 1.6e6, 1.3e6, 1e6]
+STRONG = [1e6, 1 / (1e-6 + (1e-3 - 1e-6) / 3), 1 / (1e-6 + 2 * (1e-3 - 1e-6) / 3), 1e3]
+
+SHAPES = [(1, 1, 1, 5, 7), (2, 2, 3, 16, 24), (3, 1, 2, 32, 32), (2, 2, 1, 64, 64), (2, 1, 1, 100, 77),
+          (2, 1, 2, 128, 128), (1, 1, 1, 128, 3), (1, 1, 1, 2, 128)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
+@pytest.mark.parametrize("cells", ["cfg1", "strong"])
+def test_line_solver_matches_oracle(acc, shape, cells):
+    B, X, Y, n, m = shape
+    Rset, vmax = (CFG1, 1.0) if cells == "cfg1" else (STRONG, 0.2)
+    inp, G = make_case(sum(shape) * 7 + (cells == "strong"), B, X, Y, n, m, Rset, vmax)
+    cur, U, D = oracle_planes(inp, G, B, X, Y, n, m)
+    planes, stats, iters = run(acc, inp, G, B, X, Y, n, m, method="line")
+    assert stats["status_or"] == 1, stats
+    err_u = np.abs(planes[:, :, :, 0] - U).max()
+    err_d = np.abs(planes[:, :, :, 1] - D).max()
+    tol = 2e-8 if cells == "cfg1" else V_TOL
+    assert max(err_u, err_d) < tol, (err_u, err_d, stats)
+    got, _, _ = run(acc, inp, G, B, X, Y, n, m, method="line", ret_V=False)
+    assert np.abs(got - cur).max() <= (1e-6 if cells == "cfg1" else I_RTOL) * np.abs(cur).max()
+
+
+def test_line_solver_config1_tile(acc, gold):
+    """The 128x128 four-state tile of the reference's own config (seed 1, 1 V on every row)."""
+    z = gold("sim_v1_128_tol1e-11.npz")
+    g = 1.0 / z["Rset"][z["states"]]
+    inp = np.ones((1, 1, 128))
+    planes, stats, _ = run(acc, inp, g.reshape(1, 128, 128), 1, 1, 1, 128, 128, method="line")
+    u, d = nodal.solve(g, GW, z["vin"])
+    assert np.abs(planes[0, 0, 0, 0] - u).max() < 1e-8
+    assert np.abs(planes[0, 0, 0, 1] - d).max() < 1e-8
+    assert stats["iters_max"] <= 6
+    # and the reference's converged sim output on the stored rows
+    r = z["sample_rows"]
+    assert np.abs(planes[0, 0, 0, 0][r] - z["vup_rows"]).max() < 1e-8
+    cur, _, _ = run(acc, inp, g.reshape(1, 128, 128), 1, 1, 1, 128, 128, method="line", ret_V=False)
+    np.testing.assert_allclose(cur[0, 0], z["iout"], rtol=1e-6)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_line_solver_dtypes(acc, dtype):
+    B, X, Y, n, m = 3, 2, 2, 64, 48
+    inp, G = make_case(9, B, X, Y, n, m, CFG1, 0.2, bern=False)
+    cur = nodal.solve_layer(inp, G, n, m, X, Y, GW)
+    got, _, _ = run(acc, inp, G, B, X, Y, n, m, dtype=dtype, ret_V=False, method="line")
+    assert np.abs(got - cur).max() <= 1e-6 * np.abs(cur).max()
+
+
+@pytest.mark.parametrize("shape", [(2, 1, 1, 16, 24), (1, 2, 1, 64, 64), (1, 1, 1, 128, 128)])
+def test_rbsor_matches_oracle(acc, shape):
+    B, X, Y, n, m = shape
+    inp, G = make_case(21, B, X, Y, n, m, CFG1, 0.2)
+    cur, U, D = oracle_planes(inp, G, B, X, Y, n, m)
+    planes, stats, iters = run(acc, inp, G, B, X, Y, n, m, method="rbsor")
+    assert stats["status_or"] == 1, stats
+    err = max(np.abs(planes[:, :, :, 0] - U).max(), np.abs(planes[:, :, :, 1] - D).max())
+    assert err < V_TOL, (err, stats)
+
+
+@pytest.mark.parametrize("dt,rtol", [(np.float64, 1e-12), (np.float32, 2e-5)])
+def test_sweep_order_matches_reference_iterates(acc, gold, dt, rtol):
+    """Reference order: same iterates as the reference's PimTorch GS (golden) and
+    as the oracle restatement, fixed sweeps and with the delta break."""
+    z = gold("pimtorch_gs_8x6.npz")
+    B, X, Y, n, m = [int(z[k]) for k in ["B", "numX", "numY", "rows", "cols"]]
+    tdt = torch.float64 if dt == np.float64 else torch.float32
+    tag = "f64" if dt == np.float64 else "f32"
+    ti = torch.tensor(z["input"], dtype=tdt, device="cuda")
+    tg = torch.tensor(z["G"], dtype=tdt, device="cuda")
+    out, stats, _ = acc.ir_drop_gs_ex(ti, tg, B, n, m, X, Y, iter_times=int(z["fixed_iters"]), g_wire=GW,
+                                      beta=float(z["omega"]), method="sweeps")
+    ref = z["fixed_" + tag]
+    assert np.abs(out.cpu().numpy() - ref).max() <= rtol * np.abs(ref).max()
+    thr = float(z["break_thr_" + tag])
+    out, stats, _ = acc.ir_drop_gs_ex(ti, tg, B, n, m, X, Y, iter_times=5000, g_wire=GW, beta=float(z["omega"]),
+                                      enable_break=True, break_threshould=thr, method="sweeps")
+    ref = z["break_" + tag]
+    _, it = sweeps.ir_drop_gs(z["input"].astype(dt), z["G"].astype(dt), B, n, m, X, Y, 5000, GW,
+                              float(z["omega"]), True, thr, return_iters=True)
+    assert abs(stats["iters_max"] - it) <= (0 if dt == np.float64 else 2)
+    assert np.abs(out.cpu().numpy() - ref).max() <= 4 * rtol * np.abs(ref).max()
+
+
+def test_sweep_order_ret_v_and_larger(acc):
+    B, X, Y, n, m = 2, 2, 1, 24, 40
+    inp, G = make_case(5, B, X, Y, n, m, STRONG, 0.2)
+    ti = torch.tensor(inp, device="cuda")
+    tg = torch.tensor(G, device="cuda")
+    out, _, _ = acc.ir_drop_gs_ex(ti, tg, B, n, m, X, Y, iter_times=37, beta=1.9, ret_V=True, method="sweeps")
+    ref = sweeps.ir_drop_gs(inp, G, B, n, m, X, Y, 37, GW, 1.9, ret_V=True)
+    assert np.abs(out.cpu().numpy() - ref).max() < 1e-12
+
+
+def test_dropin_signature_and_errors(acc):
+    B, X, Y, n, m = 2, 1, 1, 8, 8
+    inp, G = make_case(1, B, X, Y, n, m, CFG1, 1.0)
+    ti = torch.tensor(inp, dtype=torch.float32, device="cuda")
+    tg = torch.tensor(G, dtype=torch.float32, device="cuda")
+    out = acc.ir_drop_gs(ti, tg, B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
+    assert out.shape == (B, X, Y * m) and out.dtype == torch.float32 and out.is_cuda
+    v = acc.ir_drop_gs(ti, tg, B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], True)
+    assert v.shape == (B, X, Y, n, m)
+    with pytest.raises(RuntimeError):
+        acc.ir_drop_gs(ti.cpu(), tg, B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
+    with pytest.raises(RuntimeError):
+        acc.ir_drop_gs(ti, tg.t(), B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
+    with pytest.raises(RuntimeError):
+        acc.ir_drop_gs(ti, tg, B, 1, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
+    with pytest.raises(RuntimeError):
+        acc.ir_drop_gs(ti, tg.double(), B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
+    with pytest.raises(NotImplementedError):
+        acc.ir2s(ti, tg)
+    empty = acc.ir_drop_gs(ti[:0], tg, 0, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
+    assert empty.shape == (0, X, Y * m)
+
+
+def test_line_solver_deterministic_and_stream(acc):
+    B, X, Y, n, m = 4, 2, 2, 128, 128
+    inp, G = make_case(77, B, X, Y, n, m, CFG1, 0.2)
+    ti = torch.tensor(inp, dtype=torch.float32, device="cuda")
+    tg = torch.tensor(G, dtype=torch.float32, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        a = acc.ir_drop_gs(ti, tg, B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
+    s.synchronize()
+    b = acc.ir_drop_gs(ti, tg, B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
+    assert torch.equal(a, b)
+
+
+def test_nonfinite_input_reports_status(acc):
+    B, X, Y, n, m = 1, 1, 1, 16, 16
+    inp, G = make_case(3, B, X, Y, n, m, CFG1, 1.0)
+    G[0, 3, 4] = np.nan
+    _, stats, _ = run(acc, inp, G, B, X, Y, n, m, method="line")
+    assert stats["status_or"] & 4
