@@ -1,0 +1,328 @@
+"""Throughput of the crossbar IR-drop solve on GB300.
+
+Workload (one step): 4096 independent 128x128 crossbar tiles, 64 input vectors
+each (262,144 tile x vector solves), four-state cells R in {2e6, 1.6e6, 1.3e6,
+1e6} ohm drawn uniformly, 2.93 ohm wire segments, wordline inputs
+Bernoulli(0.5) in {0, 0.2} V, bitlines grounded, FP32.  Every solve is driven
+to 1e-8 V (estimated) of the nodal solution; a seeded sample is checked against
+the FP64 oracle before timing.  Data are synthetic (seeded numpy generators).
+
+Metric: 128x128 crossbar solves per second, whole job.  ``value`` is measured
+with inputs resident in HBM; ``e2e`` through the public drop-in call with
+pinned host buffers and host<->device copies inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank solves its own 4096 tiles (weak scaling, no
+collective on the data path); rank 0 prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_TILES = 4096
+N_VEC = 64
+ROWS = COLS = 128
+R_STATES = np.array([2e6, 1.6e6, 1.3e6, 1e6])
+R_WIRE = 2.93
+V_READ = 0.2
+METRIC = "128x128 crossbar solves/s (<=1e-6 V node error)"
+UNIT = "solves/s"
+# algorithmic HBM bytes per solve: G amortised over the tile's vectors, the
+# input vector and the output currents, FP32
+BYTES_PER_SOLVE = (ROWS * COLS * 4) / N_VEC + ROWS * 4 + COLS * 4
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """Per-solve DRAM bytes of the line kernel from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "line_relax_f32_128x128.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_solve"):
+            return float(line.split("=")[1].split()[0])
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampler over the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4) if s[3 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_workload(seed, n_tiles=N_TILES, n_vec=N_VEC):
+    rng = np.random.default_rng(seed)
+    states = rng.integers(0, 4, (n_tiles, ROWS, COLS), dtype=np.int8)
+    G = (1.0 / R_STATES)[states].astype(np.float32)                  # [numX=tiles, rows, cols]
+    vin = (rng.integers(0, 2, (n_vec, n_tiles, ROWS)) * V_READ).astype(np.float32)  # [B, numX, rows]
+    return G, vin
+
+
+def cpu_baseline(seconds=12.0, max_solves=4096):
+    """The reference's Au solve (C restatement of V1 nodeBasedGS) on all host
+    cores over a bounded sample of the same workload."""
+    from oracle import augs
+    augs.build()
+    threads = augs.max_threads()
+    G, vin = make_workload(12345, n_tiles=64, n_vec=1)
+    w = float(np.float32(1.95))
+    done, t0 = 0, time.perf_counter()
+    batch = threads
+    while True:
+        k0 = done % 64
+        idx = [(k0 + q) % 64 for q in range(batch)]
+        augs.solve_many(G[idx].astype(np.float64), vin[0, idx].astype(np.float64), R_WIRE, 100000, w, True, 1e-9)
+        done += batch
+        el = time.perf_counter() - t0
+        if el >= seconds or done >= max_solves:
+            break
+    return {"value": done / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d solves of 128x128 (Au lexicographic GS, omega 1.95, delta tol 1e-9 which meets "
+                      "1e-6 V) over %d threads in %.1f s" % (done, threads, el)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    steps = []
+    for _ in range(args.warmup):
+        cpu_baseline(seconds=2.0)
+    for _ in range(args.steps):
+        steps.append(cpu_baseline(seconds=6.0))
+    v = statistics.median(s["value"] for s in steps)
+    cb = dict(steps[-1])
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "128x128 crossbar solves, 4-state cells, 2.93 ohm wires, Bernoulli 0.2 V inputs",
+                       "solver": "reference Au GS (V1 nodeBasedGS, C restatement) on host cores"},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def check_accuracy(acc, G, vin, torch):
+    """A seeded sample of solves against the FP64 oracle (both planes)."""
+    from oracle import nodal
+    k = 4
+    tg = torch.from_numpy(G[:k]).cuda()
+    ti = torch.from_numpy(np.ascontiguousarray(vin[:16, :k])).cuda()
+    planes, _, _ = acc.ir_drop_gs_ex(ti, tg, 16, ROWS, COLS, k, 1, g_wire=1 / R_WIRE, ret_V=2, method="line")
+    planes = planes.double().cpu().numpy()
+    err = 0.0
+    for x in range(k):
+        u, d = nodal.solve(G[x].astype(np.float64), 1 / R_WIRE, vin[:16, x].astype(np.float64))
+        err = max(err, np.abs(planes[:, x, 0, 0] - u).max(), np.abs(planes[:, x, 0, 1] - d).max())
+    return err
+
+
+def run_ours(args):
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from fadesim_gb300 import cpp_ir_drop_accelerate as acc
+    from fadesim_gb300.build import build
+    build()
+
+    G, vin = make_workload(1000 + rank, n_tiles=args.tiles)
+    tg = torch.from_numpy(G).cuda()
+    ti = torch.from_numpy(vin).cuda()
+    B, X, Y = N_VEC, args.tiles, 1
+    gw = 1 / R_WIRE
+    err = check_accuracy(acc, G, vin, torch)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return acc.ir_drop_gs(ti, tg, B, ROWS, COLS, X, Y, 600, gw, 1.9, False, 1e-7, False, [], False)
+
+    for _ in range(max(3, args.warmup)):
+        out = step()
+    torch.cuda.synchronize()
+    _, stats, _ = acc.ir_drop_gs_ex(ti, tg, B, ROWS, COLS, X, Y, g_wire=gw, method="line")
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for s in range(args.steps):
+            ev[s][0].record(stream)
+            out = step()
+            ev[s][1].record(stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ms = t0.elapsed_time(t1)
+    kern_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    if dist:
+        tt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    solves_per_step = B * X * Y
+    value = solves_per_step * args.steps * world / (ms / 1e3)
+    if args.quick:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "quick": True, "tiles": X,
+                              "kernel_ms": kern_ms, "line_iters_mean": stats["iters_sum"] / max(1, stats["solves"]),
+                              "max_node_err_v_sample": err, "clocks": clk.summary()}))
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    # end to end through the public call: pinned host inputs in, currents out
+    hG = torch.from_numpy(G).pin_memory()
+    hv = torch.from_numpy(vin).pin_memory()
+    hout = torch.empty((B, X, Y * COLS), dtype=torch.float32).pin_memory()
+    del out
+    for _ in range(2):
+        hout.copy_(acc.ir_drop_gs(hv.cuda(non_blocking=True), hG.cuda(non_blocking=True), B, ROWS, COLS, X, Y, 600,
+                                  gw, 1.9, False, 1e-7, False, [], False), non_blocking=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        dG = hG.cuda(non_blocking=True)
+        dv = hv.cuda(non_blocking=True)
+        o = acc.ir_drop_gs(dv, dG, B, ROWS, COLS, X, Y, 600, gw, 1.9, False, 1e-7, False, [], False)
+        hout.copy_(o, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1)
+    e2e_value = solves_per_step * args.steps * world / (e2e_ms / 1e3)
+
+    # the plain red-black SOR kernel on a bounded sample of the same workload
+    nps = 256
+    tgs = tg[:nps // 16].contiguous()
+    tis = ti[:16, :nps // 16].contiguous()
+    acc.ir_drop_gs_ex(tis[:, :2].contiguous(), tgs[:2].contiguous(), 16, ROWS, COLS, 2, 1, g_wire=gw, method="rbsor")
+    torch.cuda.synchronize()
+    p0 = time.perf_counter()
+    _, rb_stats, _ = acc.ir_drop_gs_ex(tis, tgs, 16, ROWS, COLS, nps // 16, 1, g_wire=gw, method="rbsor")
+    torch.cuda.synchronize()
+    rb_value = nps / (time.perf_counter() - p0)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    hbm_peak, peak_kind = peaks()
+    achieved = BYTES_PER_SOLVE * solves_per_step / (kern_ms / 1e3) / 1e9
+    traffic = profiled_traffic()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "%d tiles x %d vectors of 128x128 per rank (ir_drop_gs layout B=%d, numX=%d, "
+                               "numY=1), 4-state cells, 2.93 ohm wires, Bernoulli 0.2 V inputs"
+                               % (N_TILES, N_VEC, B, X),
+                   "solver": "block line relaxation (residual form, FP32 + FP64 final residual), tol 1e-8 V",
+                   "l2": "inputs %.0f MB vs 129 MB L2, no flush" % ((G.nbytes + vin.nbytes) / 1e6),
+                   "max_node_err_v_sample": err, "line_iters_mean": stats["iters_sum"] / max(1, stats["solves"]),
+                   "line_iters_max": stats["iters_max"],
+                   "plain_rbsor_solves_per_s": rb_value,
+                   "plain_rbsor_sweeps_mean": rb_stats["iters_sum"] / max(1, rb_stats["solves"]),
+                   "speedup_vs_plain_rbsor": value / world / rb_value},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_kind": peak_kind,
+                     "traffic": traffic * solves_per_step if traffic else None,
+                     "algorithmic_bytes_per_launch": BYTES_PER_SOLVE * solves_per_step,
+                     "kernel": "line_relax_kernel<128,float>", "kernel_ms": kern_ms},
+        "e2e": {"value": e2e_value, "unit": UNIT,
+                "h2d_bytes_per_step": int(G.nbytes + vin.nbytes), "d2h_bytes_per_step": int(hout.numel() * 4)},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline()
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--tiles", type=int, default=N_TILES, help="128x128 tiles per rank (64 vectors each)")
+    ap.add_argument("--quick", action="store_true",
+                    help="time the device-resident solve only (no e2e, comparator or CPU baseline); for profiling")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -81,7 +81,7 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
                    cudaStream_t st) {
     const int L = a.n > a.m ? a.n : a.m;
     a.ctl.tol_v = (opts && opts->tol_v > 0) ? (float)opts->tol_v : 1e-8f;
-    a.ctl.residual_period = (opts && opts->residual_period > 0) ? opts->residual_period : 4;
+    a.ctl.residual_period = (opts && opts->residual_period != 0) ? opts->residual_period : 4;
     const int sms = device_sms();
     int grid = 0, ld = 0;
     size_t scratch_floats = 0;
@@ -178,6 +178,10 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
                                      int *per_solve_iters, void *stream) {
     g_err.clear();
     if (dtype != FADESIM_F32 && dtype != FADESIM_F64) return fail(FADESIM_E_ARG, "dtype must be f32 or f64");
+    if (batch_size == 0 && row_size >= 2 && col_size >= 2) {
+        if (stats) *stats = fadesim_solve_stats{0, 0, 0, 0};
+        return FADESIM_OK;  // nothing to solve; empty tensors may carry null pointers
+    }
     if (!input || !G || !out) return fail(FADESIM_E_ARG, "input, G and out must be device pointers");
     if (row_size < 2) return fail(FADESIM_E_ARG, "row_size should be >=2");
     if (col_size < 2) return fail(FADESIM_E_ARG, "col_size should be >=2");

@@ -40,10 +40,14 @@ struct LineCfg {
     static constexpr int NW = LD / 8;   // warps
 };
 
+// Node (r, c) of an LD x LD plane.  The XOR touches only the low 5 bits of c
+// and depends on c only through c >> 5, so it permutes each 32-column block of
+// a row.  At LD = 128 (segments of 32) both walks are conflict-free: 8 rows x 4
+// segments (wordline pass) and 8 columns x 4 segments (bitline pass) land on
+// 32 distinct banks at every step.
 template <int LD>
 __device__ __forceinline__ int swz(int r, int c) {
-    constexpr int SEG = LD / 4;
-    const int s = ((((r / SEG) ^ (c / SEG)) & 3) << 3) | (r & 7);
+    const int s = ((((r >> 5) ^ (c >> 5)) & 3) << 3) | (r & 7);
     return r * LD + (c ^ s);
 }
 
@@ -69,40 +73,59 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
 
     float x[SEG];
     // ---- residual of the line equations at the current iterate -------------
+    // WORD: left link always present (the source at p == 0, deviation 0), right
+    //       link absent at the open end.
+    // BIT:  upper link absent at the open top, lower link always present
+    //       (ground below the last node, deviation 0).
     {
         const float vl = (WORD && line_ok) ? vin_s[line] : 0.f;
-        float prev = (line_ok && p0 > 0 && p0 - 1 < L) ? own[at(p0 - 1)] : 0.f;
-        float cur = (line_ok && p0 < L) ? own[at(p0)] : 0.f;
+        const float prev0 = (line_ok && p0 > 0 && p0 - 1 < L) ? own[at(p0 - 1)] : 0.f;
+        const float cur0 = (line_ok && p0 < L) ? own[at(p0)] : 0.f;
+        if (RES64) {
+            // FP64 residual: every FP32 value is widened once (sliding window)
+            const double gwd = (double)gw, vld = (double)vl;
+            double dp = (double)prev0, dc = (double)cur0;
 #pragma unroll
-        for (int k = 0; k < SEG; ++k) {
-            const int p = p0 + k;
-            const bool valid = line_ok && p < L;
-            const float nxt = (line_ok && p + 1 < L) ? own[at(p + 1)] : 0.f;
-            float r = 0.f;
-            if (valid) {
-                const int q = at(p);
-                const float g = Gs[q];
-                const float o = oth[q];
-                // WORD: left link always present (the source at p == 0, deviation 0),
-                //       right link absent at the open end.
-                // BIT:  upper link absent at the open top, lower link always present
-                //       (ground below the last node, deviation 0).
-                const float gl = WORD ? gw : (p > 0 ? gw : 0.f);
-                const float gr = WORD ? (p + 1 < L ? gw : 0.f) : gw;
-                if (RES64) {
-                    const double src = WORD ? ((double)o - (double)vl) - (double)cur
-                                            : ((double)o + (double)vin_s[p]) - (double)cur;
-                    const double rr = (double)gl * ((double)prev - (double)cur) +
-                                      (double)gr * ((double)nxt - (double)cur) + (double)g * src;
+            for (int k = 0; k < SEG; ++k) {
+                const int p = p0 + k;
+                const bool valid = line_ok && p < L;
+                const double dn = (line_ok && p + 1 < L) ? (double)own[at(p + 1)] : 0.0;
+                float r = 0.f;
+                if (valid) {
+                    const int q = at(p);
+                    const double g = (double)Gs[q];
+                    const double o = (double)oth[q];
+                    const double src = WORD ? (o - vld) - dc : (o + (double)vin_s[p]) - dc;
+                    double rr = g * src;
+                    if (WORD || p > 0) rr = fma(gwd, dp - dc, rr);
+                    if (!WORD || p + 1 < L) rr = fma(gwd, dn - dc, rr);
                     r = (float)rr;
-                } else {
+                }
+                x[k] = r;
+                dp = dc;
+                dc = dn;
+            }
+        } else {
+            float prev = prev0, cur = cur0;
+#pragma unroll
+            for (int k = 0; k < SEG; ++k) {
+                const int p = p0 + k;
+                const bool valid = line_ok && p < L;
+                const float nxt = (line_ok && p + 1 < L) ? own[at(p + 1)] : 0.f;
+                float r = 0.f;
+                if (valid) {
+                    const int q = at(p);
+                    const float g = Gs[q];
+                    const float o = oth[q];
+                    const float gl = WORD ? gw : (p > 0 ? gw : 0.f);
+                    const float gr = WORD ? (p + 1 < L ? gw : 0.f) : gw;
                     const float src = WORD ? (o - vl) - cur : (o + vin_s[p]) - cur;
                     r = gl * (prev - cur) + gr * (nxt - cur) + g * src;
                 }
+                x[k] = r;
+                prev = cur;
+                cur = nxt;
             }
-            x[k] = r;
-            prev = cur;
-            cur = nxt;
         }
     }
     // ---- T^-1 r by Thomas, segmented over 4 lanes ---------------------------
@@ -178,7 +201,8 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
             const float dx = omega * x[k];
             const float nv = own[q] + dx;
             own[q] = nv;
-            dmax = fmaxf(dmax, fabsf(dx));
+            // fmaxf drops NaN: force a non-finite update to show as +inf
+            dmax = isfinite(nv) ? fmaxf(dmax, fabsf(dx)) : INFINITY;
             vmax = fmaxf(vmax, fabsf(nv));
         }
     }
@@ -199,7 +223,7 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
         const int NL = word ? n : m;
         float *dst = word ? piv : piv + SEG * T;
         const int tw_base = (line >> 3) * 32 + (line & 7);
-        double p = 1.0;
+        double p = 1.0, ipv_prev = 0.0;
         for (int q = 0; q < LD; ++q) {
             double ipv = 0.0;
             if (line < NL && q < L) {
@@ -207,8 +231,12 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
                 // wordline: source link + right link (absent at the end) + cell
                 // bitline:  upper link (absent at the top) + lower link + cell
                 const double diag = word ? gw + (q + 1 < L ? gw : 0.0) + g : (q > 0 ? gw : 0.0) + gw + g;
-                p = (q == 0) ? diag : diag - gw * gw / p;
-                ipv = 1.0 / p;
+                p = (q == 0) ? diag : fma(-gw * gw, ipv_prev, diag);
+                // 1/p: correctly rounded FP32 reciprocal refined by one Newton
+                // step in FP64 (~1e-14 relative; FP64 division is slow here)
+                const double r0 = (double)__frcp_rn((float)p);
+                ipv = r0 * fma(-p, r0, 2.0);
+                ipv_prev = ipv;
             }
             const int tw = tw_base + (q / SEG) * 8;
             dst[(q % SEG) * T + tw] = (float)ipv;
@@ -309,14 +337,17 @@ __global__ void __launch_bounds__(LD * 4, (LD >= 128 ? 1 : (LD == 64 ? 2 : 4))) 
                     const float ratio = prev_delta > 0.f ? delta / prev_delta : 0.f;
                     const float rho = fmaxf(ratio, omega - 1.f);
                     const float est = rho < 0.999f ? delta * rho / (1.f - rho) : INFINITY;
-                    const bool stalled = delta <= 8.f * floor_v && ratio >= 0.5f;
+                    // stalled: the change no longer shrinks and is at rounding level
+                    const bool stalled = delta <= floor_v && ratio >= 0.9f;
                     small = est <= fmaxf(tol, floor_v) || stalled;
                     if (adapt && it == 3 && ratio > 0.05f && ratio < 1.f) {
                         omega = fminf(1.9f, 2.f / (1.f + sqrtf(1.f - ratio)));
                     }
                 }
                 if (small) {
-                    if (res64) {
+                    // the final test must pass on an iteration whose residual was
+                    // FP64 (kres < 0: FP32 only, the FP32 test is final)
+                    if (res64 || kres < 0) {
                         status = FADESIM_ST_CONVERGED;
                         break;
                     }

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(RB_THREADS, 1) rbsor_kernel(SolveArgs a) {
                         const float dv = __fdividef(omega * r, g1 + g2 + g);
                         const float nv = v + dv;
                         self[q] = nv;
-                        dmax = fmaxf(dmax, fabsf(dv));
+                        dmax = isfinite(nv) ? fmaxf(dmax, fabsf(dv)) : INFINITY;
                         vmax = fmaxf(vmax, fabsf(nv));
                     }
                     __syncthreads();
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(RB_THREADS, 1) rbsor_kernel(SolveArgs a) {
                         const float ratio = prev_check > 0.f ? powf(delta / prev_check, 1.f / RB_CHECK) : 0.f;
                         const float rho = fmaxf(ratio, omega - 1.f);
                         const float est = rho < 0.9999f ? delta * rho / (1.f - rho) : INFINITY;
-                        const bool stalled = delta <= 8.f * floor_v && ratio >= 0.999f;
+                        const bool stalled = delta <= floor_v && ratio >= 0.999f;
                         if (est <= fmaxf(a.ctl.tol_v, floor_v) || stalled) {
                             status = FADESIM_ST_CONVERGED;
                             break;

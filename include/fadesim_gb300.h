@@ -48,7 +48,8 @@ typedef struct fadesim_solve_opts {
     int method;            /* FADESIM_METHOD_* */
     double tol_v;          /* target max node error in volts (converging methods); <=0: 1e-8 */
     int max_iters;         /* cap on line iterations / point sweeps; <=0: method default */
-    int residual_period;   /* FP64 residual every k line iterations (and always for the final test); <=0: 4 */
+    int residual_period;   /* FP64 residual every k line iterations and for the final test; 0: 4;
+                              <0: FP32 residuals only (the final test is FP32 too) */
     double omega;          /* relaxation factor; <=0: adaptive (line) or autotuned table (rbsor) */
     int vectors_per_cta;   /* input vectors one CTA solves per work item; <=0: automatic */
 } fadesim_solve_opts;

@@ -2,8 +2,8 @@
 
 Every converging method must land within 1e-6 V of the FP64 direct solve on
 every node of both planes and within 1e-4 relative on bitline currents (the
-contract); the line solver is held to a tighter 2e-8 V / 1e-6 where the cells
-are weak.  The reference-order method must reproduce the reference's own
+contract); the line solver is held to a tighter 1e-7 V (FP32 output rounding
+of ~1 V nodes) / 1e-6 where the cells are weak.  The reference-order method must reproduce the reference's own
 iterates (FP64 to 1e-12 relative).
 """
 import numpy as np
@@ -68,7 +68,9 @@ def test_line_solver_matches_oracle(acc, shape, cells):
     assert stats["status_or"] == 1, stats
     err_u = np.abs(planes[:, :, :, 0] - U).max()
     err_d = np.abs(planes[:, :, :, 1] - D).max()
-    tol = 2e-8 if cells == "cfg1" else V_TOL
+    # weak cells converge to ~1e-9 V; the returned FP32 planes then round a
+    # 1 V wordline node to 6e-8 V
+    tol = 1e-7 if cells == "cfg1" else V_TOL
     assert max(err_u, err_d) < tol, (err_u, err_d, stats)
     got, _, _ = run(acc, inp, G, B, X, Y, n, m, method="line", ret_V=False)
     assert np.abs(got - cur).max() <= (1e-6 if cells == "cfg1" else I_RTOL) * np.abs(cur).max()
@@ -81,12 +83,12 @@ def test_line_solver_config1_tile(acc, gold):
     inp = np.ones((1, 1, 128))
     planes, stats, _ = run(acc, inp, g.reshape(1, 128, 128), 1, 1, 1, 128, 128, method="line")
     u, d = nodal.solve(g, GW, z["vin"])
-    assert np.abs(planes[0, 0, 0, 0] - u).max() < 1e-8
+    assert np.abs(planes[0, 0, 0, 0] - u).max() < 1e-7
     assert np.abs(planes[0, 0, 0, 1] - d).max() < 1e-8
     assert stats["iters_max"] <= 6
     # and the reference's converged sim output on the stored rows
     r = z["sample_rows"]
-    assert np.abs(planes[0, 0, 0, 0][r] - z["vup_rows"]).max() < 1e-8
+    assert np.abs(planes[0, 0, 0, 0][r] - z["vup_rows"]).max() < 1e-7
     cur, _, _ = run(acc, inp, g.reshape(1, 128, 128), 1, 1, 1, 128, 128, method="line", ret_V=False)
     np.testing.assert_allclose(cur[0, 0], z["iout"], rtol=1e-6)
 
