@@ -33,26 +33,49 @@
 
 namespace fadesim {
 
+// Per-size launch shape.  A warp holds LPW lines x NSEG segments of SEG nodes;
+// T threads cover all LD lines of one pass with one segment each.
 template <int LD>
-struct LineCfg {
-    static constexpr int T = LD * 4;    // threads per CTA
-    static constexpr int SEG = LD / 4;  // nodes per thread segment
-    static constexpr int NW = LD / 8;   // warps
+struct LineCfg;
+template <>
+struct LineCfg<128> {
+    static constexpr int NSEG = 8, SEG = 16, LPW = 4, T = 1024, NW = 32, MINB = 1;
+};
+template <>
+struct LineCfg<64> {
+    static constexpr int NSEG = 4, SEG = 16, LPW = 8, T = 256, NW = 8, MINB = 3;
+};
+template <>
+struct LineCfg<32> {
+    static constexpr int NSEG = 4, SEG = 8, LPW = 8, T = 128, NW = 4, MINB = 8;
 };
 
-// Node (r, c) of an LD x LD plane.  The XOR touches only the low 5 bits of c
-// and depends on c only through c >> 5, so it permutes each 32-column block of
-// a row.  At LD = 128 (segments of 32) both walks are conflict-free: 8 rows x 4
-// segments (wordline pass) and 8 columns x 4 segments (bitline pass) land on
-// 32 distinct banks at every step.
+// Node (r, c) of an LD x LD plane in shared memory.  The XOR term touches only
+// the low 5 bits of c and depends on c only through c >> 5, so it permutes
+// every 32-column block of a row.  For each size it is chosen so that both
+// walks -- LPW rows x NSEG segments at one step of the wordline pass, LPW
+// columns x NSEG segments at one step of the bitline pass -- hit 32 distinct
+// banks (checked exhaustively when the layouts were designed).
 template <int LD>
 __device__ __forceinline__ int swz(int r, int c) {
-    const int s = ((((r >> 5) ^ (c >> 5)) & 3) << 3) | (r & 7);
-    return r * LD + (c ^ s);
+    int x;
+    if (LD == 128) x = (((((r & 3) ^ ((r >> 4) & 3)) | (((r >> 6) & 1) << 2)) << 2) | ((c >> 5) & 3));
+    else if (LD == 64) x = (r & 7) | (((((c >> 5) & 1) ^ ((r >> 4) & 1))) << 3) | (((r >> 5) & 1) << 4);
+    else x = r & 31;
+    return r * LD + (c ^ x);
 }
 
-template <typename T>
-__device__ __forceinline__ T ldg_t(const T *p) { return __ldg(p); }
+// float -> double on the integer pipe (exact for normal numbers, zero, inf and
+// NaN; FP32 subnormals, which the solve never produces, widen to ~2^-127).
+__device__ __forceinline__ double widen_f64(float f) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int mag = b & 0x7fffffffu;
+    unsigned int hi;
+    if (mag == 0u) hi = b;                                                // signed zero
+    else if (mag >= 0x7f800000u) hi = (b & 0x80000000u) | 0x7ff00000u | (mag & 0x007fffffu) >> 3 | (mag > 0x7f800000u ? 0x00080000u : 0u);
+    else hi = (b & 0x80000000u) | ((mag >> 3) + (896u << 20));
+    return __hiloint2double((int)hi, (int)((b & 7u) << 29));
+}
 
 // One pass over all lines of one plane.  WORD: wordline rows (own plane = U
 // deviations, other = D); else bitline columns (own = D, other = U).
@@ -63,10 +86,12 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
                                           float &dmax, float &vmax) {
     constexpr int SEG = LineCfg<LD>::SEG;
     constexpr int T = LineCfg<LD>::T;
+    constexpr int LPW = LineCfg<LD>::LPW;
+    constexpr int NSEG = LineCfg<LD>::NSEG;
     const int tid = threadIdx.x;
     const int lane = tid & 31;
-    const int s = lane >> 3;
-    const int line = (tid >> 5) * 8 + (lane & 7);
+    const int s = lane / LPW;
+    const int line = (tid >> 5) * LPW + (lane % LPW);
     const bool line_ok = line < NL;
     const int p0 = s * SEG;
     auto at = [&](int p) { return WORD ? swz<LD>(line, p) : swz<LD>(p, line); };
@@ -82,24 +107,26 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
         const float prev0 = (line_ok && p0 > 0 && p0 - 1 < L) ? own[at(p0 - 1)] : 0.f;
         const float cur0 = (line_ok && p0 < L) ? own[at(p0)] : 0.f;
         if (RES64) {
-            // FP64 residual: every FP32 value is widened once (sliding window)
-            const double gwd = (double)gw, vld = (double)vl;
-            double dp = (double)prev0, dc = (double)cur0;
+            // FP64 residual.  FP32 values are widened on the integer pipe
+            // (widen_f64) and each node costs 6 FP64 operations: GB300's FP64
+            // rate is a small fraction of its FP32 rate.
+            const double gwd = (double)gw, vld = widen_f64(vl);
+            double dp = widen_f64(prev0), dc = widen_f64(cur0);
 #pragma unroll
             for (int k = 0; k < SEG; ++k) {
                 const int p = p0 + k;
                 const bool valid = line_ok && p < L;
-                const double dn = (line_ok && p + 1 < L) ? (double)own[at(p + 1)] : 0.0;
+                const double dn = widen_f64((line_ok && p + 1 < L) ? own[at(p + 1)] : 0.f);
                 float r = 0.f;
                 if (valid) {
                     const int q = at(p);
-                    const double g = (double)Gs[q];
-                    const double o = (double)oth[q];
-                    const double src = WORD ? (o - vld) - dc : (o + (double)vin_s[p]) - dc;
-                    double rr = g * src;
-                    if (WORD || p > 0) rr = fma(gwd, dp - dc, rr);
-                    if (!WORD || p + 1 < L) rr = fma(gwd, dn - dc, rr);
-                    r = (float)rr;
+                    const double g = widen_f64(Gs[q]);
+                    const double o = widen_f64(oth[q]);
+                    const double src = WORD ? (o - vld) - dc : (o + widen_f64(vin_s[p])) - dc;
+                    const bool has_l = WORD || p > 0, has_r = !WORD || p + 1 < L;
+                    // second difference along the line (exact: widened FP32 inputs)
+                    const double lap = (has_l && has_r) ? fma(-2.0, dc, dp + dn) : (has_l ? dp - dc : dn - dc);
+                    r = __double2float_rn(fma(gwd, lap, g * src));
                 }
                 x[k] = r;
                 dp = dc;
@@ -143,15 +170,15 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     }
     float Ai = A, Yi = y;
 #pragma unroll
-    for (int off = 1; off < 4; off <<= 1) {
-        const float Ap = __shfl_up_sync(0xffffffffu, Ai, 8 * off);
-        const float Yp = __shfl_up_sync(0xffffffffu, Yi, 8 * off);
+    for (int off = 1; off < NSEG; off <<= 1) {
+        const float Ap = __shfl_up_sync(0xffffffffu, Ai, LPW * off);
+        const float Yp = __shfl_up_sync(0xffffffffu, Yi, LPW * off);
         if (s >= off) {
             Yi = fmaf(Ai, Yp, Yi);
             Ai *= Ap;
         }
     }
-    float yin = __shfl_up_sync(0xffffffffu, Yi, 8);
+    float yin = __shfl_up_sync(0xffffffffu, Yi, LPW);
     if (s == 0) yin = 0.f;
     {
         float P = 1.f;
@@ -173,16 +200,16 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     }
     float Bi = Bm, Xi = X;
 #pragma unroll
-    for (int off = 1; off < 4; off <<= 1) {
-        const float Bn = __shfl_down_sync(0xffffffffu, Bi, 8 * off);
-        const float Xn = __shfl_down_sync(0xffffffffu, Xi, 8 * off);
-        if (s + off < 4) {
+    for (int off = 1; off < NSEG; off <<= 1) {
+        const float Bn = __shfl_down_sync(0xffffffffu, Bi, LPW * off);
+        const float Xn = __shfl_down_sync(0xffffffffu, Xi, LPW * off);
+        if (s + off < NSEG) {
             Xi = fmaf(Bi, Xn, Xi);
             Bi *= Bn;
         }
     }
-    float xin = __shfl_down_sync(0xffffffffu, Xi, 8);
-    if (s == 3) xin = 0.f;
+    float xin = __shfl_down_sync(0xffffffffu, Xi, LPW);
+    if (s == NSEG - 1) xin = 0.f;
     {
         float Q = 1.f;
 #pragma unroll
@@ -214,6 +241,7 @@ template <int LD>
 __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ piv, int n, int m, float gwf) {
     constexpr int SEG = LineCfg<LD>::SEG;
     constexpr int T = LineCfg<LD>::T;
+    constexpr int LPW = LineCfg<LD>::LPW;
     const double gw = gwf;
     const int tid = threadIdx.x;
     if (tid < 2 * LD) {
@@ -222,7 +250,7 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
         const int L = word ? m : n;
         const int NL = word ? n : m;
         float *dst = word ? piv : piv + SEG * T;
-        const int tw_base = (line >> 3) * 32 + (line & 7);
+        const int tw_base = (line / LPW) * 32 + (line % LPW);
         double p = 1.0, ipv_prev = 0.0;
         for (int q = 0; q < LD; ++q) {
             double ipv = 0.0;
@@ -238,14 +266,14 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
                 ipv = r0 * fma(-p, r0, 2.0);
                 ipv_prev = ipv;
             }
-            const int tw = tw_base + (q / SEG) * 8;
+            const int tw = tw_base + (q / SEG) * LPW;
             dst[(q % SEG) * T + tw] = (float)ipv;
         }
     }
 }
 
 template <int LD, typename TIO>
-__global__ void __launch_bounds__(LD * 4, (LD >= 128 ? 1 : (LD == 64 ? 2 : 4))) line_relax_kernel(SolveArgs a) {
+__global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_kernel(SolveArgs a) {
     constexpr int T = LineCfg<LD>::T;
     constexpr int NW = LineCfg<LD>::NW;
     constexpr int SEG = LineCfg<LD>::SEG;
@@ -377,9 +405,11 @@ __global__ void __launch_bounds__(LD * 4, (LD >= 128 ? 1 : (LD == 64 ? 2 : 4))) 
                 }
             } else {
                 // bitline current I_j = sum_i g_ij (u_ij - d_ij), in the bitline mapping
+                constexpr int LPW = LineCfg<LD>::LPW;
+                constexpr int NSEG = LineCfg<LD>::NSEG;
                 const int lane = tid & 31;
-                const int s = lane >> 3;
-                const int j = (tid >> 5) * 8 + (lane & 7);
+                const int s = lane / LPW;
+                const int j = (tid >> 5) * LPW + (lane % LPW);
                 TIO acc = 0;
                 if (j < m) {
                     for (int k = 0; k < SEG; ++k) {
@@ -390,8 +420,8 @@ __global__ void __launch_bounds__(LD * 4, (LD >= 128 ? 1 : (LD == 64 ? 2 : 4))) 
                         }
                     }
                 }
-                acc += __shfl_down_sync(0xffffffffu, acc, 8);
-                acc += __shfl_down_sync(0xffffffffu, acc, 16);
+#pragma unroll
+                for (int off = LPW; off < 32; off <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
                 if (s == 0 && j < m) out[((size_t)b * a.numX + x) * ldG + (size_t)y * m + j] = acc;
             }
             if (tid == 0) {
@@ -409,9 +439,11 @@ int line_relax_ld(int n, int m) {
     return 0;
 }
 
-size_t line_relax_smem(int ld) { return (size_t)(3 * ld * ld + ld + 4 * (ld / 8)) * sizeof(float); }
-int line_relax_threads(int ld) { return ld * 4; }
-size_t line_relax_scratch_floats_per_cta(int ld) { return (size_t)2 * (ld / 4) * (ld * 4); }
+static int nwarps(int ld) { return ld == 128 ? LineCfg<128>::NW : (ld == 64 ? LineCfg<64>::NW : LineCfg<32>::NW); }
+int line_relax_threads(int ld) { return nwarps(ld) * 32; }
+size_t line_relax_smem(int ld) { return (size_t)(3 * ld * ld + ld + 4 * nwarps(ld)) * sizeof(float); }
+// pivots of both passes: 2 x SEG x T = 2 x LD x LD floats
+size_t line_relax_scratch_floats_per_cta(int ld) { return (size_t)2 * ld * ld; }
 
 template <int LD, typename TIO>
 static cudaError_t prep_one() {
@@ -433,7 +465,7 @@ cudaError_t line_relax_prepare(int ld, int dtype) {
 
 template <int LD, typename TIO>
 static cudaError_t occ_one(int *n) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, line_relax_kernel<LD, TIO>, LD * 4,
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, line_relax_kernel<LD, TIO>, LineCfg<LD>::T,
                                                          line_relax_smem(LD));
 }
 
@@ -451,7 +483,7 @@ cudaError_t line_relax_occupancy(int ld, int dtype, int *ctas) {
 
 template <int LD, typename TIO>
 static cudaError_t launch_one(const SolveArgs &a, int grid, cudaStream_t st) {
-    line_relax_kernel<LD, TIO><<<grid, LD * 4, line_relax_smem(LD), st>>>(a);
+    line_relax_kernel<LD, TIO><<<grid, LineCfg<LD>::T, line_relax_smem(LD), st>>>(a);
     return cudaGetLastError();
 }
 
