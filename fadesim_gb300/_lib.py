@@ -38,6 +38,9 @@ EXPORTS = {
                               ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _vp, _vp],
     "fadesim_last_error": [],
     "fadesim_version": [],
+    "fadesim_ir_drop_gs_noalloc_f32": [_vp, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp],
+    "fadesim_noalloc_scratch_bytes": [],
+    "fadesim_noalloc_last_error": [],
 }
 
 
@@ -53,7 +56,12 @@ def load():
     for name, args in EXPORTS.items():
         fn = getattr(lib, name)
         fn.argtypes = args
-        fn.restype = ctypes.c_char_p if name in ("fadesim_last_error", "fadesim_version") else ctypes.c_int
+        if name in ("fadesim_last_error", "fadesim_version", "fadesim_noalloc_last_error"):
+            fn.restype = ctypes.c_char_p
+        elif name == "fadesim_noalloc_scratch_bytes":
+            fn.restype = ctypes.c_size_t
+        else:
+            fn.restype = ctypes.c_int
     _lib = lib
     return lib
 

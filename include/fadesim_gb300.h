@@ -93,6 +93,23 @@ int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G, int batch
                           int n_nonlinear_params, int ret_V, void *out, const fadesim_solve_opts *opts,
                           fadesim_solve_stats *stats, int *per_solve_iters, void *stream);
 
+/* Allocation-free variant of the line solve (FP32, bitline currents only).
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc -- code running inside someone else's stream capture, host
+ * callbacks or real-time loops that forbid allocation, programs with a fixed
+ * device-memory budget.  Inputs and outputs as fadesim_ir_drop_gs_f32 (method
+ * FADESIM_METHOD_LINE, tol 1e-8 V).  Its scratch is one static device array of
+ * fadesim_noalloc_scratch_bytes() bytes (24 MiB) that every GPU loading the
+ * library holds until exit.  The first call on a device sets up that array's
+ * address and should come before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race.  Tiles larger than 128 x 128 are
+ * rejected with FADESIM_E_ARG; fadesim_noalloc_last_error() gives the message.
+ * It calls no cudaMalloc, cudaFree or allocating library routine. */
+int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G, int batch_size, int row_size, int col_size,
+                                   int numX, int numY, double g_wire, float *out, void *stream);
+size_t fadesim_noalloc_scratch_bytes(void);
+const char *fadesim_noalloc_last_error(void);
+
 /* Message for the last failing call on this thread. */
 const char *fadesim_last_error(void);
 
