@@ -34,16 +34,19 @@ class SolverOptions:
     method: str = os.environ.get("FADESIM_METHOD", "auto")
     tol_v: float = 1e-8
     max_iters: int = 0           # 0: method default
-    residual_period: int = 4     # FP64 residual every k line iterations
+    residual_period: int = 1     # precise residual every k line iterations (-1: FP32 only)
     omega: float = 0.0           # 0: adaptive (line) / size formula (rbsor)
     vectors_per_cta: int = 0     # 0: automatic
+    residual: str = "ff"         # precise residual: "ff" (float-float on the FP32 pipe) or "fp64"
 
     def to_c(self, method=None):
         m = method if method is not None else self.method
         if m not in _METHODS:
             raise ValueError("unknown method %r (one of %s)" % (m, sorted(_METHODS)))
+        if self.residual not in ("fp64", "ff"):
+            raise ValueError("residual must be 'fp64' or 'ff'")
         return _lib.SolveOpts(_METHODS[m], float(self.tol_v), int(self.max_iters), int(self.residual_period),
-                              float(self.omega), int(self.vectors_per_cta))
+                              float(self.omega), int(self.vectors_per_cta), 1 if self.residual == "fp64" else 0)
 
 
 options = SolverOptions()
@@ -116,14 +119,14 @@ def ir_drop_gs(input, G, batch_size, row_size, col_size, numX, numY, iter_times,
 def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_times=600, g_wire=1 / 2.93, beta=1.9,
                   enable_break=False, break_threshould=1e-7, nonlinear_cell_enable=False, nonlinear_params=(),
                   ret_V=False, method=None, tol_v=None, max_iters=None, residual_period=None, omega=None,
-                  vectors_per_cta=None, return_stats=True, return_iters=False):
+                  vectors_per_cta=None, residual=None, return_stats=True, return_iters=False):
     """``ir_drop_gs`` with explicit solver options (``ret_V=2`` returns both node
     planes, [batch, numX, numY, 2, rows, cols]).  Returns (out, stats, iters):
     stats is a dict (solves, iters_sum, iters_max, status_or) and iters an int32
     [batch, numX, numY] tensor of per-solve iterations (None unless asked)."""
     o = SolverOptions(**{k: v for k, v in vars(options).items()})
     for k, v in dict(tol_v=tol_v, max_iters=max_iters, residual_period=residual_period, omega=omega,
-                     vectors_per_cta=vectors_per_cta).items():
+                     vectors_per_cta=vectors_per_cta, residual=residual).items():
         if v is not None:
             setattr(o, k, v)
     out, st, it = _solve(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, beta,

@@ -19,8 +19,9 @@ struct DevStats {
 struct SolveCtl {
     float tol_v;          // target max node error (V)
     int max_iters;        // iteration / sweep cap
-    int residual_period;  // FP64 residual every k iterations
+    int residual_period;  // precise residual every k iterations (<0: never)
     float omega;          // <= 0: adaptive
+    int residual_ff;      // precise residual in float-float (FP32 pipe) instead of FP64
 };
 
 __device__ __forceinline__ float warp_max(float v) {

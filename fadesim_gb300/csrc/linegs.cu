@@ -65,6 +65,13 @@ __device__ __forceinline__ int swz(int r, int c) {
     return r * LD + (c ^ x);
 }
 
+// Knuth's error-free sum: s + e == a + b exactly (round-to-nearest).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
 // float -> double on the integer pipe (exact for normal numbers, zero, inf and
 // NaN; FP32 subnormals, which the solve never produces, widen to ~2^-127).
 __device__ __forceinline__ double widen_f64(float f) {
@@ -79,11 +86,11 @@ __device__ __forceinline__ double widen_f64(float f) {
 
 // One pass over all lines of one plane.  WORD: wordline rows (own plane = U
 // deviations, other = D); else bitline columns (own = D, other = U).
-template <int LD, bool WORD, bool RES64>
+template <int LD, bool WORD, int RES>
 __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *__restrict__ oth,
                                           const float *__restrict__ Gs, const float *__restrict__ vin_s,
-                                          const float *__restrict__ piv, int L, int NL, float gw, float omega,
-                                          float &dmax, float &vmax) {
+                                          const float *__restrict__ piv, const float *__restrict__ segprod, int L,
+                                          int NL, float gw, float omega, float &dmax, float &vmax) {
     constexpr int SEG = LineCfg<LD>::SEG;
     constexpr int T = LineCfg<LD>::T;
     constexpr int LPW = LineCfg<LD>::LPW;
@@ -106,7 +113,7 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
         const float vl = (WORD && line_ok) ? vin_s[line] : 0.f;
         const float prev0 = (line_ok && p0 > 0 && p0 - 1 < L) ? own[at(p0 - 1)] : 0.f;
         const float cur0 = (line_ok && p0 < L) ? own[at(p0)] : 0.f;
-        if (RES64) {
+        if (RES == 1) {
             // FP64 residual.  FP32 values are widened on the integer pipe
             // (widen_f64) and each node costs 6 FP64 operations: GB300's FP64
             // rate is a small fraction of its FP32 rate.
@@ -127,6 +134,43 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
                     // second difference along the line (exact: widened FP32 inputs)
                     const double lap = (has_l && has_r) ? fma(-2.0, dc, dp + dn) : (has_l ? dp - dc : dn - dc);
                     r = __double2float_rn(fma(gwd, lap, g * src));
+                }
+                x[k] = r;
+                dp = dc;
+                dc = dn;
+            }
+        } else if (RES == 2) {
+            // float-float residual: error-free FP32 transforms (two_sum,
+            // two_prod) carry every difference and product exactly; only the
+            // final collection of the small error terms rounds.  Accuracy is
+            // that of the FP64 form at FP32-pipe cost.
+            float dp = prev0, dc = cur0;
+#pragma unroll
+            for (int k = 0; k < SEG; ++k) {
+                const int p = p0 + k;
+                const bool valid = line_ok && p < L;
+                const float dn = (line_ok && p + 1 < L) ? own[at(p + 1)] : 0.f;
+                float r = 0.f;
+                if (valid) {
+                    const int q = at(p);
+                    const float g = Gs[q];
+                    const float o = oth[q];
+                    const bool has_l = WORD || p > 0, has_r = !WORD || p + 1 < L;
+                    float sh, sl, th, tl, a1h, a1l, a2h, a2l, lh, ll;
+                    two_sum(o, WORD ? -vl : vin_s[p], sh, sl);       // o -/+ vin
+                    two_sum(sh, -dc, th, tl);                         // ... - own
+                    two_sum(has_l ? dp : dc, -dc, a1h, a1l);          // left difference (0 if absent)
+                    two_sum(has_r ? dn : dc, -dc, a2h, a2l);          // right difference (0 if absent)
+                    two_sum(a1h, a2h, lh, ll);
+                    const float lap_lo = __fadd_rn(ll, __fadd_rn(a1l, a2l));
+                    const float src_lo = __fadd_rn(tl, sl);
+                    const float p1h = __fmul_rn(gw, lh), p1l = __fmaf_rn(gw, lh, -p1h);
+                    const float p2h = __fmul_rn(g, th), p2l = __fmaf_rn(g, th, -p2h);
+                    float rh, rl;
+                    two_sum(p1h, p2h, rh, rl);
+                    const float lo = __fadd_rn(__fadd_rn(rl, __fadd_rn(p1l, p2l)),
+                                               __fmaf_rn(gw, lap_lo, __fmul_rn(g, src_lo)));
+                    r = __fadd_rn(rh, lo);
                 }
                 x[k] = r;
                 dp = dc;
@@ -155,84 +199,72 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
             }
         }
     }
-    // ---- T^-1 r by Thomas, segmented over 4 lanes ---------------------------
+    // ---- T^-1 r by Thomas, segmented over NSEG lanes ------------------------
+    // y_p = ip_p (r_p + gw y_{p-1}),  x_p = y_p + gw ip_p x_{p+1}.  A segment
+    // maps its incoming value v to (prod_seg gw ip) v + (result with v = 0); the
+    // product is a tile constant (segprod).  Padding nodes carry ip = 0 and
+    // r = 0, which breaks both chains at the line end; the first segment's
+    // incoming y and the last segment's incoming x are zero.
     float ip[SEG];
 #pragma unroll
     for (int k = 0; k < SEG; ++k) ip[k] = piv[k * T + tid];
-    // forward elimination: y_p = ip_p r_p + (gw ip_p) y_{p-1}
-    float y = 0.f, A = 1.f;
+    const float C = segprod[tid];
+    float Y = 0.f;
 #pragma unroll
-    for (int k = 0; k < SEG; ++k) {
-        const float a = (p0 + k == 0) ? 0.f : gw * ip[k];
-        y = fmaf(a, y, ip[k] * x[k]);
-        x[k] = y;
-        A *= a;
-    }
-    float Ai = A, Yi = y;
+    for (int k = 0; k < SEG; ++k) Y = ip[k] * fmaf(gw, Y, x[k]);
+    float Ci = C, Yi = Y;
 #pragma unroll
     for (int off = 1; off < NSEG; off <<= 1) {
-        const float Ap = __shfl_up_sync(0xffffffffu, Ai, LPW * off);
+        const float Cp = __shfl_up_sync(0xffffffffu, Ci, LPW * off);
         const float Yp = __shfl_up_sync(0xffffffffu, Yi, LPW * off);
         if (s >= off) {
-            Yi = fmaf(Ai, Yp, Yi);
-            Ai *= Ap;
+            Yi = fmaf(Ci, Yp, Yi);
+            Ci *= Cp;
         }
     }
-    float yin = __shfl_up_sync(0xffffffffu, Yi, LPW);
-    if (s == 0) yin = 0.f;
-    {
-        float P = 1.f;
+    float y = __shfl_up_sync(0xffffffffu, Yi, LPW);
+    if (s == 0) y = 0.f;
 #pragma unroll
-        for (int k = 0; k < SEG; ++k) {
-            const float a = (p0 + k == 0) ? 0.f : gw * ip[k];
-            P *= a;
-            x[k] = fmaf(P, yin, x[k]);
-        }
+    for (int k = 0; k < SEG; ++k) {
+        y = ip[k] * fmaf(gw, y, x[k]);
+        x[k] = y;
     }
-    // back substitution: x_p = y_p + (gw ip_p) x_{p+1}
-    float X = 0.f, Bm = 1.f;
+    float X = 0.f;
 #pragma unroll
-    for (int k = SEG - 1; k >= 0; --k) {
-        const float b = (p0 + k + 1 >= L) ? 0.f : gw * ip[k];
-        X = fmaf(b, X, x[k]);
-        x[k] = X;
-        Bm *= b;
-    }
-    float Bi = Bm, Xi = X;
+    for (int k = SEG - 1; k >= 0; --k) X = fmaf(gw * ip[k], X, x[k]);
+    Ci = C;
+    float Xi = X;
 #pragma unroll
     for (int off = 1; off < NSEG; off <<= 1) {
-        const float Bn = __shfl_down_sync(0xffffffffu, Bi, LPW * off);
+        const float Cn = __shfl_down_sync(0xffffffffu, Ci, LPW * off);
         const float Xn = __shfl_down_sync(0xffffffffu, Xi, LPW * off);
         if (s + off < NSEG) {
-            Xi = fmaf(Bi, Xn, Xi);
-            Bi *= Bn;
+            Xi = fmaf(Ci, Xn, Xi);
+            Ci *= Cn;
         }
     }
-    float xin = __shfl_down_sync(0xffffffffu, Xi, LPW);
-    if (s == NSEG - 1) xin = 0.f;
-    {
-        float Q = 1.f;
+    X = __shfl_down_sync(0xffffffffu, Xi, LPW);
+    if (s == NSEG - 1) X = 0.f;
 #pragma unroll
-        for (int k = SEG - 1; k >= 0; --k) {
-            const float b = (p0 + k + 1 >= L) ? 0.f : gw * ip[k];
-            Q *= b;
-            x[k] = fmaf(Q, xin, x[k]);
-        }
+    for (int k = SEG - 1; k >= 0; --k) {
+        X = fmaf(gw * ip[k], X, x[k]);
+        x[k] = X;
     }
     // ---- apply the correction ----------------------------------------------
+    // (a NaN correction is not seen by fmaxf; the output stage flags it)
+    float dm = 0.f;
 #pragma unroll
     for (int k = 0; k < SEG; ++k) {
         const int p = p0 + k;
         if (line_ok && p < L) {
             const int q = at(p);
-            const float dx = omega * x[k];
-            const float nv = own[q] + dx;
+            const float nv = fmaf(omega, x[k], own[q]);
             own[q] = nv;
-            // fmaxf drops NaN: force a non-finite update to show as +inf
-            dmax = isfinite(nv) ? fmaxf(dmax, fabsf(dx)) : INFINITY;
+            dm = fmaxf(dm, fabsf(x[k]));
             vmax = fmaxf(vmax, fabsf(nv));
         }
     }
+    dmax = fmaxf(dmax, omega * dm);
 }
 
 // FP64 pivots of every line of the tile, written in the order each pass thread
@@ -250,8 +282,11 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
         const int L = word ? m : n;
         const int NL = word ? n : m;
         float *dst = word ? piv : piv + SEG * T;
+        float *prod = piv + 2 * SEG * T + (word ? 0 : T);
         const int tw_base = (line / LPW) * 32 + (line % LPW);
+        const float gwf32 = gwf;
         double p = 1.0, ipv_prev = 0.0;
+        float seg_prod = 1.f;
         for (int q = 0; q < LD; ++q) {
             double ipv = 0.0;
             if (line < NL && q < L) {
@@ -267,7 +302,14 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
                 ipv_prev = ipv;
             }
             const int tw = tw_base + (q / SEG) * LPW;
-            dst[(q % SEG) * T + tw] = (float)ipv;
+            const float ipf = (float)ipv;
+            dst[(q % SEG) * T + tw] = ipf;
+            // product of the segment's chain multipliers gw*ip, as the pass forms them
+            seg_prod *= gwf32 * ipf;
+            if (q % SEG == SEG - 1) {
+                prod[tw] = seg_prod;
+                seg_prod = 1.f;
+            }
         }
     }
 }
@@ -283,6 +325,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
     float *D = U + LD * LD;
     float *vin_s = D + LD * LD;
     float *red = vin_s + LD;  // [2][2][NW]
+    __shared__ int nonfinite_flag;
 
     const int tid = threadIdx.x;
     const int n = a.n, m = a.m;
@@ -290,11 +333,13 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
     const TIO *inp = static_cast<const TIO *>(a.input);
     const TIO *Gg = static_cast<const TIO *>(a.G);
     TIO *out = static_cast<TIO *>(a.out);
-    float *piv = a.scratch + (size_t)blockIdx.x * (2 * SEG * T);
+    float *piv = a.scratch + (size_t)blockIdx.x * (2 * SEG * T + 2 * T);
     const float gw = a.gw;
     const float tol = a.ctl.tol_v;
     const int kres = a.ctl.residual_period;
     const int maxit = a.ctl.max_iters;
+    const bool ff = a.ctl.residual_ff != 0;  // precise residual in float-float instead of FP64
+    const bool precise_first = kres == 1;    // every iteration precise
     long long cached_tile = -1;
 
     for (long long item = blockIdx.x; item < a.nitems; item += gridDim.x) {
@@ -325,15 +370,17 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             float omega = a.ctl.omega > 0.f ? a.ctl.omega : 1.f;
             const bool adapt = !(a.ctl.omega > 0.f);
             float prev_delta = 0.f;
-            bool res64 = false;
+            bool res64 = precise_first;
             int status = 0, it = 0, par = 0;
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
-                if (res64) line_pass<LD, true, true>(U, D, Gs, vin_s, piv, m, n, gw, omega, dmax, vmax);
-                else line_pass<LD, true, false>(U, D, Gs, vin_s, piv, m, n, gw, omega, dmax, vmax);
+                if (!res64) line_pass<LD, true, 0>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax);
+                else if (ff) line_pass<LD, true, 2>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax);
+                else line_pass<LD, true, 1>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax);
                 __syncthreads();
-                if (res64) line_pass<LD, false, true>(D, U, Gs, vin_s, piv + SEG * T, n, m, gw, omega, dmax, vmax);
-                else line_pass<LD, false, false>(D, U, Gs, vin_s, piv + SEG * T, n, m, gw, omega, dmax, vmax);
+                if (!res64) line_pass<LD, false, 0>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax);
+                else if (ff) line_pass<LD, false, 2>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax);
+                else line_pass<LD, false, 1>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax);
                 dmax = warp_max(dmax);
                 vmax = warp_max(vmax);
                 if ((tid & 31) == 0) {
@@ -390,12 +437,15 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 prev_delta = delta;
             }
             // ---- outputs ------------------------------------------------------
+            if (tid == 0) nonfinite_flag = 0;
+            __syncthreads();
             if (a.ret_V) {
                 for (int e = tid; e < n * m; e += T) {
                     const int i = e / m, j = e - i * m;
                     const int q = swz<LD>(i, j);
                     const TIO uu = (TIO)U[q] + (TIO)vin_s[i];
                     const size_t sol = ((size_t)b * a.numX + x) * a.numY + y;
+                    if (!isfinite((float)uu) || !isfinite(D[q])) nonfinite_flag = 1;
                     if (a.ret_V == 2) {
                         out[(sol * 2 + 0) * n * m + (size_t)i * m + j] = uu;
                         out[(sol * 2 + 1) * n * m + (size_t)i * m + j] = (TIO)D[q];
@@ -423,7 +473,10 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
 #pragma unroll
                 for (int off = LPW; off < 32; off <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
                 if (s == 0 && j < m) out[((size_t)b * a.numX + x) * ldG + (size_t)y * m + j] = acc;
+                if (s == 0 && j < m && !isfinite((float)acc)) nonfinite_flag = 1;
             }
+            __syncthreads();
+            if (nonfinite_flag) status |= FADESIM_ST_NONFINITE;
             if (tid == 0) {
                 record_solve(a.stats, a.iters_out, ((long long)b * a.numX + x) * a.numY + y, it, status);
             }
@@ -442,8 +495,8 @@ int line_relax_ld(int n, int m) {
 static int nwarps(int ld) { return ld == 128 ? LineCfg<128>::NW : (ld == 64 ? LineCfg<64>::NW : LineCfg<32>::NW); }
 int line_relax_threads(int ld) { return nwarps(ld) * 32; }
 size_t line_relax_smem(int ld) { return (size_t)(3 * ld * ld + ld + 4 * nwarps(ld)) * sizeof(float); }
-// pivots of both passes: 2 x SEG x T = 2 x LD x LD floats
-size_t line_relax_scratch_floats_per_cta(int ld) { return (size_t)2 * ld * ld; }
+// pivots of both passes (2 x SEG x T = 2 x LD x LD floats) and segment products (2 x T)
+size_t line_relax_scratch_floats_per_cta(int ld) { return (size_t)2 * ld * ld + 2 * (size_t)nwarps(ld) * 32; }
 
 template <int LD, typename TIO>
 static cudaError_t prep_one() {

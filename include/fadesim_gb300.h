@@ -48,10 +48,12 @@ typedef struct fadesim_solve_opts {
     int method;            /* FADESIM_METHOD_* */
     double tol_v;          /* target max node error in volts (converging methods); <=0: 1e-8 */
     int max_iters;         /* cap on line iterations / point sweeps; <=0: method default */
-    int residual_period;   /* FP64 residual every k line iterations and for the final test; 0: 4;
-                              <0: FP32 residuals only (the final test is FP32 too) */
+    int residual_period;   /* precise residual every k line iterations, and always for the final
+                              convergence test; 0: 1 (every iteration); <0: FP32 residuals only */
     double omega;          /* relaxation factor; <=0: adaptive (line) or autotuned table (rbsor) */
     int vectors_per_cta;   /* input vectors one CTA solves per work item; <=0: automatic */
+    int residual_kind;     /* precise residual arithmetic: 0 = float-float (default: error-free FP32
+                              transforms, FP64-class accuracy on the FP32 pipe), 1 = native FP64 */
 } fadesim_solve_opts;
 
 typedef struct fadesim_solve_stats {
