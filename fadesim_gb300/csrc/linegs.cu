@@ -65,6 +65,10 @@ __device__ __forceinline__ int swz(int r, int c) {
     return r * LD + (c ^ x);
 }
 
+// Input voltages in shared memory, one pad word per 16 rows: the bitline pass
+// reads rows 16s + k for NSEG segments s at once, which would otherwise share banks.
+__device__ __forceinline__ int vpad(int p) { return p + (p >> 4); }
+
 // Knuth's error-free sum: s + e == a + b exactly (round-to-nearest).
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = __fadd_rn(a, b);
@@ -102,6 +106,16 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     const bool line_ok = line < NL;
     const int p0 = s * SEG;
     auto at = [&](int p) { return WORD ? swz<LD>(line, p) : swz<LD>(p, line); };
+    // Addresses of this segment's nodes.  The swizzle term is constant along a
+    // wordline segment, so node k sits at Bw ^ k; along a bitline segment it
+    // depends on k only through k % V, so node k sits at Rb[k % V] + k * LD
+    // (an immediate offset from one of V registers).
+    constexpr int V = (LD == 128) ? 4 : 8;
+    const int Bw = swz<LD>(line & (LD - 1), p0);
+    int Rb[V];
+#pragma unroll
+    for (int t = 0; t < V; ++t) Rb[t] = swz<LD>(p0 + t, line & (LD - 1)) - t * LD;
+    auto qk = [&](int k) { return WORD ? (Bw ^ k) : (Rb[k % V] + k * LD); };
 
     float x[SEG];
     // ---- residual of the line equations at the current iterate -------------
@@ -110,7 +124,7 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     // BIT:  upper link absent at the open top, lower link always present
     //       (ground below the last node, deviation 0).
     {
-        const float vl = (WORD && line_ok) ? vin_s[line] : 0.f;
+        const float vl = (WORD && line_ok) ? vin_s[vpad(line)] : 0.f;
         const float prev0 = (line_ok && p0 > 0 && p0 - 1 < L) ? own[at(p0 - 1)] : 0.f;
         const float cur0 = (line_ok && p0 < L) ? own[at(p0)] : 0.f;
         if (RES == 1) {
@@ -123,13 +137,13 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
             for (int k = 0; k < SEG; ++k) {
                 const int p = p0 + k;
                 const bool valid = line_ok && p < L;
-                const double dn = widen_f64((line_ok && p + 1 < L) ? own[at(p + 1)] : 0.f);
+                const double dn = widen_f64((line_ok && p + 1 < L) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f);
                 float r = 0.f;
                 if (valid) {
-                    const int q = at(p);
+                    const int q = qk(k);
                     const double g = widen_f64(Gs[q]);
                     const double o = widen_f64(oth[q]);
-                    const double src = WORD ? (o - vld) - dc : (o + widen_f64(vin_s[p])) - dc;
+                    const double src = WORD ? (o - vld) - dc : (o + widen_f64(vin_s[vpad(p)])) - dc;
                     const bool has_l = WORD || p > 0, has_r = !WORD || p + 1 < L;
                     // second difference along the line (exact: widened FP32 inputs)
                     const double lap = (has_l && has_r) ? fma(-2.0, dc, dp + dn) : (has_l ? dp - dc : dn - dc);
@@ -149,15 +163,15 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
             for (int k = 0; k < SEG; ++k) {
                 const int p = p0 + k;
                 const bool valid = line_ok && p < L;
-                const float dn = (line_ok && p + 1 < L) ? own[at(p + 1)] : 0.f;
+                const float dn = (line_ok && p + 1 < L) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
                 float r = 0.f;
                 if (valid) {
-                    const int q = at(p);
+                    const int q = qk(k);
                     const float g = Gs[q];
                     const float o = oth[q];
                     const bool has_l = WORD || p > 0, has_r = !WORD || p + 1 < L;
                     float sh, sl, th, tl, a1h, a1l, a2h, a2l, lh, ll;
-                    two_sum(o, WORD ? -vl : vin_s[p], sh, sl);       // o -/+ vin
+                    two_sum(o, WORD ? -vl : vin_s[vpad(p)], sh, sl);       // o -/+ vin
                     two_sum(sh, -dc, th, tl);                         // ... - own
                     two_sum(has_l ? dp : dc, -dc, a1h, a1l);          // left difference (0 if absent)
                     two_sum(has_r ? dn : dc, -dc, a2h, a2l);          // right difference (0 if absent)
@@ -182,15 +196,15 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
             for (int k = 0; k < SEG; ++k) {
                 const int p = p0 + k;
                 const bool valid = line_ok && p < L;
-                const float nxt = (line_ok && p + 1 < L) ? own[at(p + 1)] : 0.f;
+                const float nxt = (line_ok && p + 1 < L) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
                 float r = 0.f;
                 if (valid) {
-                    const int q = at(p);
+                    const int q = qk(k);
                     const float g = Gs[q];
                     const float o = oth[q];
                     const float gl = WORD ? gw : (p > 0 ? gw : 0.f);
                     const float gr = WORD ? (p + 1 < L ? gw : 0.f) : gw;
-                    const float src = WORD ? (o - vl) - cur : (o + vin_s[p]) - cur;
+                    const float src = WORD ? (o - vl) - cur : (o + vin_s[vpad(p)]) - cur;
                     r = gl * (prev - cur) + gr * (nxt - cur) + g * src;
                 }
                 x[k] = r;
@@ -257,7 +271,7 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     for (int k = 0; k < SEG; ++k) {
         const int p = p0 + k;
         if (line_ok && p < L) {
-            const int q = at(p);
+            const int q = qk(k);
             const float nv = fmaf(omega, x[k], own[q]);
             own[q] = nv;
             dm = fmaxf(dm, fabsf(x[k]));
@@ -324,7 +338,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
     float *U = Gs + LD * LD;
     float *D = U + LD * LD;
     float *vin_s = D + LD * LD;
-    float *red = vin_s + LD;  // [2][2][NW]
+    float *red = vin_s + LD + LD / 16;  // [2][2][NW]
     __shared__ int nonfinite_flag;
 
     const int tid = threadIdx.x;
@@ -341,6 +355,14 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
     const bool ff = a.ctl.residual_ff != 0;  // precise residual in float-float instead of FP64
     const bool precise_first = kres == 1;    // every iteration precise
     long long cached_tile = -1;
+    __shared__ unsigned long long st_solves, st_iters;  // this CTA's counters (thread 0)
+    __shared__ int st_max, st_or;
+    if (tid == 0) {
+        st_solves = 0;
+        st_iters = 0;
+        st_max = 0;
+        st_or = 0;
+    }
 
     for (long long item = blockIdx.x; item < a.nitems; item += gridDim.x) {
         const long long tile = item / a.nchunks;
@@ -365,7 +387,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 U[e] = 0.f;
                 D[e] = 0.f;
             }
-            if (tid < LD) vin_s[tid] = (tid < n) ? (float)inp[((size_t)b * a.numX + x) * n + tid] : 0.f;
+            if (tid < LD) vin_s[vpad(tid)] = (tid < n) ? (float)inp[((size_t)b * a.numX + x) * n + tid] : 0.f;
             __syncthreads();
             float omega = a.ctl.omega > 0.f ? a.ctl.omega : 1.f;
             const bool adapt = !(a.ctl.omega > 0.f);
@@ -388,12 +410,10 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     red[(par * 2 + 1) * NW + (tid >> 5)] = vmax;
                 }
                 __syncthreads();
-                float delta = 0.f, vm = 0.f;
-#pragma unroll
-                for (int w = 0; w < NW; ++w) {
-                    delta = fmaxf(delta, red[(par * 2 + 0) * NW + w]);
-                    vm = fmaxf(vm, red[(par * 2 + 1) * NW + w]);
-                }
+                // every warp reduces the NW partial maxima itself (no second barrier)
+                const int ln = tid & 31;
+                float delta = warp_max(ln < NW ? red[(par * 2 + 0) * NW + ln] : 0.f);
+                float vm = warp_max(ln < NW ? red[(par * 2 + 1) * NW + ln] : 0.f);
                 par ^= 1;
                 ++it;
                 if (!isfinite(delta) || !isfinite(vm)) {
@@ -443,7 +463,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 for (int e = tid; e < n * m; e += T) {
                     const int i = e / m, j = e - i * m;
                     const int q = swz<LD>(i, j);
-                    const TIO uu = (TIO)U[q] + (TIO)vin_s[i];
+                    const TIO uu = (TIO)U[q] + (TIO)vin_s[vpad(i)];
                     const size_t sol = ((size_t)b * a.numX + x) * a.numY + y;
                     if (!isfinite((float)uu) || !isfinite(D[q])) nonfinite_flag = 1;
                     if (a.ret_V == 2) {
@@ -466,7 +486,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                         const int i = s * SEG + k;
                         if (i < n) {
                             const int q = swz<LD>(i, j);
-                            acc += (TIO)Gs[q] * (((TIO)U[q] + (TIO)vin_s[i]) - (TIO)D[q]);
+                            acc += (TIO)Gs[q] * (((TIO)U[q] + (TIO)vin_s[vpad(i)]) - (TIO)D[q]);
                         }
                     }
                 }
@@ -478,9 +498,20 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             __syncthreads();
             if (nonfinite_flag) status |= FADESIM_ST_NONFINITE;
             if (tid == 0) {
-                record_solve(a.stats, a.iters_out, ((long long)b * a.numX + x) * a.numY + y, it, status);
+                if (a.iters_out) a.iters_out[((long long)b * a.numX + x) * a.numY + y] = it;
+                st_solves += 1;
+                st_iters += it;
+                st_max = max(st_max, it);
+                st_or |= status;
             }
         }
+    }
+    __syncthreads();
+    if (tid == 0 && a.stats && st_solves) {
+        atomicAdd(&a.stats->solves, st_solves);
+        atomicAdd(&a.stats->iters_sum, st_iters);
+        atomicMax(&a.stats->iters_max, st_max);
+        atomicOr(&a.stats->status_or, st_or);
     }
 }
 
@@ -494,7 +525,7 @@ int line_relax_ld(int n, int m) {
 
 static int nwarps(int ld) { return ld == 128 ? LineCfg<128>::NW : (ld == 64 ? LineCfg<64>::NW : LineCfg<32>::NW); }
 int line_relax_threads(int ld) { return nwarps(ld) * 32; }
-size_t line_relax_smem(int ld) { return (size_t)(3 * ld * ld + ld + 4 * nwarps(ld)) * sizeof(float); }
+size_t line_relax_smem(int ld) { return (size_t)(3 * ld * ld + ld + ld / 16 + 4 * nwarps(ld)) * sizeof(float); }
 // pivots of both passes (2 x SEG x T = 2 x LD x LD floats) and segment products (2 x T)
 size_t line_relax_scratch_floats_per_cta(int ld) { return (size_t)2 * ld * ld + 2 * (size_t)nwarps(ld) * 32; }
 
