@@ -40,6 +40,11 @@ EXPORTS = {
     "fadesim_last_error": [],
     "fadesim_version": [],
     "fadesim_ir_drop_gs_noalloc_f32": [_vp, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp],
+    "fadesim_quantize_f32": [_vp, ctypes.c_longlong, _i, _vp, _vp],
+    "fadesim_slice_inputs_f32": [_vp, _i, _i, _i, _i, _i, _i, ctypes.c_float, _vp, _vp],
+    "fadesim_map_conductance_f32": [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _i, ctypes.c_float, ctypes.c_float, _vp, _vp],
+    "fadesim_adc_shift_add_f32": [_vp, _i, _i, _i, _i, _i, _i, ctypes.c_float, ctypes.c_float, ctypes.c_float, _i, _i,
+                                  _i, _i, _i, _vp, _vp],
     "fadesim_noalloc_scratch_bytes": [],
     "fadesim_noalloc_last_error": [],
 }

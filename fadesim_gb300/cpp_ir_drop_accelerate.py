@@ -17,6 +17,7 @@ match the reference's converged solver.  ``options.method = "sweeps"`` (or
 sweep order for exactly ``iter_times`` sweeps instead.
 """
 import ctypes
+import math
 import os
 from dataclasses import dataclass
 
@@ -60,7 +61,7 @@ def _check_input(t, name):
 
 
 def _solve(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, beta, enable_break,
-           break_threshould, nonlinear_cell_enable, nonlinear_params, ret_V, opts, want_stats, want_iters):
+           break_threshould, nonlinear_cell_enable, nonlinear_params, ret_V, opts, want_stats, want_iters, out=None):
     _check_input(input, "input")
     _check_input(G, "G")
     if row_size < 2:
@@ -78,11 +79,17 @@ def _solve(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_w
     lib = _lib.load()
     dtype = _lib.F64 if input.dtype == torch.float64 else _lib.F32
     if ret_V == 2:
-        out = torch.empty((batch_size, numX, numY, 2, row_size, col_size), dtype=input.dtype, device=input.device)
+        shape = (batch_size, numX, numY, 2, row_size, col_size)
     elif ret_V:
-        out = torch.empty((batch_size, numX, numY, row_size, col_size), dtype=input.dtype, device=input.device)
+        shape = (batch_size, numX, numY, row_size, col_size)
     else:
-        out = torch.empty((batch_size, numX, numY * col_size), dtype=input.dtype, device=input.device)
+        shape = (batch_size, numX, numY * col_size)
+    if out is None:
+        out = torch.empty(shape, dtype=input.dtype, device=input.device)
+    elif (not out.is_contiguous() or out.dtype != input.dtype or out.device != input.device
+          or out.numel() != math.prod(shape)):
+        raise RuntimeError("out must be a contiguous %s tensor of %d elements on %s" % (input.dtype, math.prod(shape),
+                                                                                      input.device))
     iters = None
     if want_iters:
         iters = torch.empty((batch_size, numX, numY), dtype=torch.int32, device=input.device)
@@ -119,11 +126,12 @@ def ir_drop_gs(input, G, batch_size, row_size, col_size, numX, numY, iter_times,
 def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_times=600, g_wire=1 / 2.93, beta=1.9,
                   enable_break=False, break_threshould=1e-7, nonlinear_cell_enable=False, nonlinear_params=(),
                   ret_V=False, method=None, tol_v=None, max_iters=None, residual_period=None, omega=None,
-                  vectors_per_cta=None, residual=None, return_stats=True, return_iters=False):
+                  vectors_per_cta=None, residual=None, return_stats=True, return_iters=False, out=None):
     """``ir_drop_gs`` with explicit solver options (``ret_V=2`` returns both node
     planes, [batch, numX, numY, 2, rows, cols]).  Returns (out, stats, iters):
     stats is a dict (solves, iters_sum, iters_max, status_or) and iters an int32
-    [batch, numX, numY] tensor of per-solve iterations (None unless asked)."""
+    [batch, numX, numY] tensor of per-solve iterations (None unless asked).  ``out``
+    may be a preallocated contiguous tensor of the output's size."""
     o = SolverOptions(**{k: v for k, v in vars(options).items()})
     for k, v in dict(tol_v=tol_v, max_iters=max_iters, residual_period=residual_period, omega=omega,
                      vectors_per_cta=vectors_per_cta, residual=residual).items():
@@ -131,7 +139,7 @@ def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_tim
             setattr(o, k, v)
     out, st, it = _solve(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, beta,
                          enable_break, break_threshould, nonlinear_cell_enable, nonlinear_params, ret_V,
-                         o.to_c(method), return_stats, return_iters)
+                         o.to_c(method), return_stats, return_iters, out=out)
     stats = None
     if st is not None:
         stats = dict(solves=int(st.solves), iters_sum=int(st.iters_sum), iters_max=int(st.iters_max),

@@ -95,6 +95,33 @@ int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G, int batch
                           int n_nonlinear_params, int ret_V, void *out, const fadesim_solve_opts *opts,
                           fadesim_solve_stats *stats, int *per_solve_iters, void *stream);
 
+/* ---- integer stages around the solve (bit-exact with the reference's float32
+ * arithmetic given the same currents).  Device pointers, async on stream. ---- */
+
+/* q = round-half-even(x / 2^s) as int32; s from the host as the reference computes it
+ * (fixedPoint/nn/fixedPointArithmetic.py:76-96, quantization_tensor). */
+int fadesim_quantize_f32(const float *x, long long n, int s, int32_t *q, void *stream);
+
+/* Input voltages for nbits input-bit cycles, stacked on the batch:
+ * v[bit*B + b, x, r] = ((xq[b, x*rows + r] >> bit*dac_bits) & (2^dac_bits - 1)) * inputV, zero-padded
+ * to numX*rows (splitArrayArithmetic.py:1199-1201 bit slicing, :714-749 padding and voltage). */
+int fadesim_slice_inputs_f32(const int32_t *xq, int B, int insize, int rows, int numX, int nbits, int dac_bits,
+                             float inputV, float *v, void *stream);
+
+/* Conductance map of one weight slice of one PN array: G[x, r, y*cols + c] = slice * dG + Gmin, slice =
+ * ((negative ? max(-w, 0) : max(w, 0)) >> shift) & (2^cell_bits - 1), padded cells at state 0
+ * (splitArrayArithmetic.py:1191-1195,1212-1215 PN split and slicing, :753-757 mapping). */
+int fadesim_map_conductance_f32(const int32_t *wq, int insize, int outsize, int rows, int cols, int numX, int numY,
+                                int shift, int cell_bits, int negative, float dG, float Gmin, float *G, void *stream);
+
+/* ADC codes round(I / adcUseI * levels) summed over row tiles, cropped, scaled, pos - neg, and
+ * shift-added over input bits i and slices j in the reference's order, the top input bit subtracted
+ * when complement != 0 (splitArrayArithmetic.py:835-836, 961-978, 1224-1227).  I is
+ * [nslices][2][nbits][B][numX][ldI]; out is [B, outsize]; s12 = s1 + s2. */
+int fadesim_adc_shift_add_f32(const float *I, int nbits, int nslices, int B, int numX, int ldI, int outsize,
+                              float adcUseI, float levels, float scale, int s12, int dac_bits, int cell_bits,
+                              int input_bits, int complement, float *out, void *stream);
+
 /* Allocation-free variant of the line solve (FP32, bitline currents only).
  * No counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc -- code running inside someone else's stream capture, host
