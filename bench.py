@@ -259,6 +259,18 @@ def run_ours(args):
     e2e_ms = e0.elapsed_time(e1)
     e2e_value = solves_per_step * args.steps * world / (e2e_ms / 1e3)
 
+    # the same step under the other residual precisions (one timed step each)
+    variants = {}
+    for vname, kw in [("fp32_residual_only", dict(residual_period=-1)), ("native_fp64_residual", dict(residual="fp64"))]:
+        acc.ir_drop_gs_ex(ti, tg, B, ROWS, COLS, X, Y, g_wire=gw, method="line", return_stats=False, **kw)
+        v0 = torch.cuda.Event(enable_timing=True)
+        v1 = torch.cuda.Event(enable_timing=True)
+        v0.record(stream)
+        acc.ir_drop_gs_ex(ti, tg, B, ROWS, COLS, X, Y, g_wire=gw, method="line", return_stats=False, **kw)
+        v1.record(stream)
+        torch.cuda.synchronize()
+        variants[vname + "_solves_per_s"] = solves_per_step / (v0.elapsed_time(v1) / 1e3)
+
     # the plain red-black SOR kernel on a bounded sample of the same workload
     nps = 256
     tgs = tg[:nps // 16].contiguous()
@@ -284,13 +296,14 @@ def run_ours(args):
         "config": {"workload": "%d tiles x %d vectors of 128x128 per rank (ir_drop_gs layout B=%d, numX=%d, "
                                "numY=1), 4-state cells, 2.93 ohm wires, Bernoulli 0.2 V inputs"
                                % (N_TILES, N_VEC, B, X),
-                   "solver": "block line relaxation (residual form, FP32 + FP64 final residual), tol 1e-8 V",
+                   "solver": "block line relaxation: FP32 tridiagonal line solves, residual recomputed every "
+                             "iteration in float-float (FP64-class) arithmetic, tol 1e-8 V",
                    "l2": "inputs %.0f MB vs 129 MB L2, no flush" % ((G.nbytes + vin.nbytes) / 1e6),
                    "max_node_err_v_sample": err, "line_iters_mean": stats["iters_sum"] / max(1, stats["solves"]),
                    "line_iters_max": stats["iters_max"],
                    "plain_rbsor_solves_per_s": rb_value,
                    "plain_rbsor_sweeps_mean": rb_stats["iters_sum"] / max(1, rb_stats["solves"]),
-                   "speedup_vs_plain_rbsor": value / world / rb_value},
+                   "speedup_vs_plain_rbsor": value / world / rb_value, **variants},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "traffic": traffic * solves_per_step if traffic else None,
