@@ -86,19 +86,33 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
     const int sms = device_sms();
     int grid = 0, ld = 0;
     size_t scratch_floats = 0;
+    int cld = 0;
     if (method == FADESIM_METHOD_LINE) {
         ld = line_relax_ld(a.n, a.m);
-        if (!ld) return fail(FADESIM_E_UNSUPPORTED, "line relaxation in this build handles rows, cols <= 128");
+        cld = ld ? 0 : cluster_relax_ld(a.n, a.m);
+        if (!ld && !cld) return fail(FADESIM_E_UNSUPPORTED, "line relaxation in this build handles rows, cols <= 512");
         a.ctl.max_iters = (opts && opts->max_iters > 0) ? opts->max_iters : 400;
         a.ctl.omega = (opts && opts->omega > 0) ? (float)opts->omega : 0.f;
-        CUDA_TRY(line_relax_prepare(ld, dtype));
-        int per_sm = 0;
-        CUDA_TRY(line_relax_occupancy(ld, dtype, &per_sm));
-        if (per_sm < 1) return fail(FADESIM_E_CUDA, "line relaxation kernel does not fit on this device");
-        grid = per_sm * sms;
-        plan_items(a, grid, opts ? opts->vectors_per_cta : 0);
-        if ((long long)grid > a.nitems) grid = (int)a.nitems;
-        scratch_floats = line_relax_scratch_floats_per_cta(ld) * grid;
+        if (ld) {
+            CUDA_TRY(line_relax_prepare(ld, dtype));
+            int per_sm = 0;
+            CUDA_TRY(line_relax_occupancy(ld, dtype, &per_sm));
+            if (per_sm < 1) return fail(FADESIM_E_CUDA, "line relaxation kernel does not fit on this device");
+            grid = per_sm * sms;
+            plan_items(a, grid, opts ? opts->vectors_per_cta : 0);
+            if ((long long)grid > a.nitems) grid = (int)a.nitems;
+            scratch_floats = line_relax_scratch_floats_per_cta(ld) * grid;
+        } else {
+            const int csize = cluster_relax_size(cld);
+            int clusters = 0;
+            CUDA_TRY(cluster_relax_occupancy(cld, dtype, &clusters));
+            if (clusters < 1)
+                return fail(FADESIM_E_UNSUPPORTED, "this device cannot co-schedule the cluster the tile size needs");
+            plan_items(a, clusters, opts ? opts->vectors_per_cta : 0);
+            if ((long long)clusters > a.nitems) clusters = (int)a.nitems;
+            grid = clusters * csize;
+            scratch_floats = cluster_relax_scratch_floats_per_cta(cld) * grid;
+        }
     } else {
         if (L > 128) return fail(FADESIM_E_UNSUPPORTED, "red-black SOR in this build handles rows, cols <= 128");
         a.ctl.max_iters = (opts && opts->max_iters > 0) ? opts->max_iters : 20000;
@@ -117,8 +131,10 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
     a.stats = dst;
     a.scratch = reinterpret_cast<float *>(reinterpret_cast<char *>(scr.p) + 256);
     CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(DevStats), st));
-    if (method == FADESIM_METHOD_LINE) {
+    if (method == FADESIM_METHOD_LINE && ld) {
         CUDA_TRY(launch_line_relax(a, ld, dtype, grid, st));
+    } else if (method == FADESIM_METHOD_LINE) {
+        CUDA_TRY(launch_cluster_relax(a, cld, dtype, grid, st));
     } else {
         CUDA_TRY(launch_rbsor(a, dtype, grid, st));
     }
@@ -209,7 +225,9 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
     a.ret_V = ret_V == 2 ? 2 : (ret_V ? 1 : 0);
     a.iters_out = per_solve_iters;
     int method = opts ? opts->method : FADESIM_METHOD_AUTO;
-    if (method == FADESIM_METHOD_AUTO) method = line_relax_ld(row_size, col_size) ? FADESIM_METHOD_LINE : FADESIM_METHOD_SWEEPS;
+    if (method == FADESIM_METHOD_AUTO)
+        method = (line_relax_ld(row_size, col_size) || cluster_relax_ld(row_size, col_size)) ? FADESIM_METHOD_LINE
+                                                                                           : FADESIM_METHOD_SWEEPS;
     switch (method) {
         case FADESIM_METHOD_LINE:
         case FADESIM_METHOD_RBSOR:

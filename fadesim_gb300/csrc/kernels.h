@@ -34,6 +34,15 @@ cudaError_t line_relax_prepare(int ld, int dtype);
 cudaError_t line_relax_occupancy(int ld, int dtype, int *ctas_per_sm);
 cudaError_t launch_line_relax(const SolveArgs &a, int ld, int dtype, int grid, cudaStream_t st);
 
+// Block line relaxation for 128 < rows, cols <= 512 on thread-block clusters
+// (4 CTAs up to 256, 16 CTAs up to 512).  Returns 256/512, or 0 if the shape
+// is not handled.
+int cluster_relax_ld(int n, int m);
+int cluster_relax_size(int ld);
+size_t cluster_relax_scratch_floats_per_cta(int ld);
+cudaError_t cluster_relax_occupancy(int ld, int dtype, int *clusters);
+cudaError_t launch_cluster_relax(const SolveArgs &a, int ld, int dtype, int grid, cudaStream_t st);
+
 // Plain red-black point SOR, planes resident in shared memory (n, m <= 128).
 size_t rbsor_smem(int n, int m);
 cudaError_t rbsor_prepare(int dtype);

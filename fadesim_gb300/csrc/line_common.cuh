@@ -1,0 +1,121 @@
+// Device helpers shared by the line-relaxation kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fadesim {
+
+// Knuth's error-free sum: s + e == a + b exactly (round-to-nearest).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// float -> double on the integer pipe (exact for normal numbers, zero, inf and
+// NaN; FP32 subnormals, which the solve never produces, widen to ~2^-127).
+__device__ __forceinline__ double widen_f64(float f) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int mag = b & 0x7fffffffu;
+    unsigned int hi;
+    if (mag == 0u) hi = b;                                                // signed zero
+    else if (mag >= 0x7f800000u) hi = (b & 0x80000000u) | 0x7ff00000u | (mag & 0x007fffffu) >> 3 | (mag > 0x7f800000u ? 0x00080000u : 0u);
+    else hi = (b & 0x80000000u) | ((mag >> 3) + (896u << 20));
+    return __hiloint2double((int)hi, (int)((b & 7u) << 29));
+}
+
+// Residual of one node's line equation at the current iterate (amperes):
+//   r = gl (prev - cur) + gr (nxt - cur) + g src,
+//   src = (o - vin) - cur on a wordline (o = bitline node, cur = u - vin),
+//   src = (o + vin) - cur on a bitline (o = wordline deviation, cur = d),
+// gl = gw if has_l else 0, gr = gw if has_r else 0.  Unknowns are deviations
+// from the ideal state, so every difference is between nearby values.
+// RES 0: FP32.  RES 1: FP64 (widened on the integer pipe).  RES 2: float-float,
+// error-free FP32 transforms carrying every difference and product exactly.
+template <bool WORD, int RES>
+__device__ __forceinline__ float line_residual(float prev, float cur, float nxt, float g, float o, float vin,
+                                               bool has_l, bool has_r, float gw) {
+    if (RES == 1) {
+        const double dp = widen_f64(prev), dc = widen_f64(cur), dn = widen_f64(nxt);
+        const double src = WORD ? (widen_f64(o) - widen_f64(vin)) - dc : (widen_f64(o) + widen_f64(vin)) - dc;
+        // second difference along the line (exact: widened FP32 inputs)
+        const double lap = (has_l && has_r) ? fma(-2.0, dc, dp + dn) : (has_l ? dp - dc : (has_r ? dn - dc : 0.0));
+        return __double2float_rn(fma((double)gw, lap, widen_f64(g) * src));
+    } else if (RES == 2) {
+        float sh, sl, th, tl, a1h, a1l, a2h, a2l, lh, ll;
+        two_sum(o, WORD ? -vin : vin, sh, sl);           // o -/+ vin
+        two_sum(sh, -cur, th, tl);                        // ... - own
+        two_sum(has_l ? prev : cur, -cur, a1h, a1l);      // left difference (0 if absent)
+        two_sum(has_r ? nxt : cur, -cur, a2h, a2l);       // right difference (0 if absent)
+        two_sum(a1h, a2h, lh, ll);
+        const float lap_lo = __fadd_rn(ll, __fadd_rn(a1l, a2l));
+        const float src_lo = __fadd_rn(tl, sl);
+        const float p1h = __fmul_rn(gw, lh), p1l = __fmaf_rn(gw, lh, -p1h);
+        const float p2h = __fmul_rn(g, th), p2l = __fmaf_rn(g, th, -p2h);
+        float rh, rl;
+        two_sum(p1h, p2h, rh, rl);
+        const float lo = __fadd_rn(__fadd_rn(rl, __fadd_rn(p1l, p2l)), __fmaf_rn(gw, lap_lo, __fmul_rn(g, src_lo)));
+        return __fadd_rn(rh, lo);
+    } else {
+        const float gl = has_l ? gw : 0.f, gr = has_r ? gw : 0.f;
+        const float src = WORD ? (o - vin) - cur : (o + vin) - cur;
+        return gl * (prev - cur) + gr * (nxt - cur) + g * src;
+    }
+}
+
+}  // namespace fadesim
+
+namespace fadesim {
+
+// Stop test and relaxation factor of the line iteration, evaluated identically
+// by every thread (and every CTA of a cluster) from the same per-iteration
+// maxima.  delta = largest correction of the iteration, vm = largest deviation.
+//   error estimate  delta * rho / (1 - rho), rho the larger of the last ratio,
+//                   the 3-iteration geometric rate and omega - 1;
+//   floor           4 ulps of the largest deviation (FP32 resolution);
+//   relaxation      block Gauss-Seidel for 3 iterations, then
+//                   omega = 2 / (1 + sqrt(1 - rho_GS)) (Young, 2-block
+//                   partition), refined at iteration 12 from the observed SOR
+//                   rate lambda via mu^2 = (lambda + omega - 1)^2 / (lambda omega^2).
+struct LineStop {
+    float omega;
+    bool adapt;
+    int it;
+    float h0, h1, h2, h3;  // delta of this and the 3 previous iterations
+
+    __device__ __forceinline__ void init(float omega_fixed) {
+        adapt = !(omega_fixed > 0.f);
+        omega = adapt ? 1.f : omega_fixed;
+        it = 0;
+        h0 = h1 = h2 = h3 = 0.f;
+    }
+
+    __device__ __forceinline__ bool update(float delta, float vm, float tol) {
+        ++it;
+        const float prev = h0;
+        h3 = h2;
+        h2 = h1;
+        h1 = h0;
+        h0 = delta;
+        if (it == 1) return delta <= 0.f;
+        const float floor_v = 4.f * 1.1920929e-07f * vm;
+        const float ratio = prev > 0.f ? delta / prev : 0.f;
+        const float rate3 = (it >= 4 && h3 > 0.f) ? cbrtf(delta / h3) : 0.f;
+        const float rho = fmaxf(fmaxf(ratio, rate3), omega - 1.f);
+        const float est = rho < 0.999f ? delta * rho / (1.f - rho) : INFINITY;
+        const bool stalled = delta <= floor_v && ratio >= 0.9f;
+        if (adapt) {
+            if (it == 3 && ratio > 0.05f && ratio < 1.f) {
+                omega = fminf(1.95f, 2.f / (1.f + sqrtf(1.f - ratio)));
+            } else if (it == 12 && omega > 1.f && rate3 > omega - 1.f + 0.02f && rate3 < 1.f) {
+                const float mu2 = (rate3 + omega - 1.f) * (rate3 + omega - 1.f) / (rate3 * omega * omega);
+                if (mu2 < 1.f) {
+                    const float w2 = 2.f / (1.f + sqrtf(1.f - mu2));
+                    if (w2 > omega + 0.01f) omega = fminf(1.95f, w2);
+                }
+            }
+        }
+        return est <= fmaxf(tol, floor_v) || stalled;
+    }
+};
+
+}  // namespace fadesim

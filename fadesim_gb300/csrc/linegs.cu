@@ -30,6 +30,7 @@
 #include <math.h>
 
 #include "kernels.h"
+#include "line_common.cuh"
 
 namespace fadesim {
 
@@ -69,25 +70,6 @@ __device__ __forceinline__ int swz(int r, int c) {
 // reads rows 16s + k for NSEG segments s at once, which would otherwise share banks.
 __device__ __forceinline__ int vpad(int p) { return p + (p >> 4); }
 
-// Knuth's error-free sum: s + e == a + b exactly (round-to-nearest).
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// float -> double on the integer pipe (exact for normal numbers, zero, inf and
-// NaN; FP32 subnormals, which the solve never produces, widen to ~2^-127).
-__device__ __forceinline__ double widen_f64(float f) {
-    const unsigned int b = __float_as_uint(f);
-    const unsigned int mag = b & 0x7fffffffu;
-    unsigned int hi;
-    if (mag == 0u) hi = b;                                                // signed zero
-    else if (mag >= 0x7f800000u) hi = (b & 0x80000000u) | 0x7ff00000u | (mag & 0x007fffffu) >> 3 | (mag > 0x7f800000u ? 0x00080000u : 0u);
-    else hi = (b & 0x80000000u) | ((mag >> 3) + (896u << 20));
-    return __hiloint2double((int)hi, (int)((b & 7u) << 29));
-}
-
 // One pass over all lines of one plane.  WORD: wordline rows (own plane = U
 // deviations, other = D); else bitline columns (own = D, other = U).
 template <int LD, bool WORD, int RES>
@@ -125,92 +107,22 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     //       (ground below the last node, deviation 0).
     {
         const float vl = (WORD && line_ok) ? vin_s[vpad(line)] : 0.f;
-        const float prev0 = (line_ok && p0 > 0 && p0 - 1 < L) ? own[at(p0 - 1)] : 0.f;
-        const float cur0 = (line_ok && p0 < L) ? own[at(p0)] : 0.f;
-        if (RES == 1) {
-            // FP64 residual.  FP32 values are widened on the integer pipe
-            // (widen_f64) and each node costs 6 FP64 operations: GB300's FP64
-            // rate is a small fraction of its FP32 rate.
-            const double gwd = (double)gw, vld = widen_f64(vl);
-            double dp = widen_f64(prev0), dc = widen_f64(cur0);
+        float prev = (line_ok && p0 > 0 && p0 - 1 < L) ? own[at(p0 - 1)] : 0.f;
+        float cur = (line_ok && p0 < L) ? own[at(p0)] : 0.f;
 #pragma unroll
-            for (int k = 0; k < SEG; ++k) {
-                const int p = p0 + k;
-                const bool valid = line_ok && p < L;
-                const double dn = widen_f64((line_ok && p + 1 < L) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f);
-                float r = 0.f;
-                if (valid) {
-                    const int q = qk(k);
-                    const double g = widen_f64(Gs[q]);
-                    const double o = widen_f64(oth[q]);
-                    const double src = WORD ? (o - vld) - dc : (o + widen_f64(vin_s[vpad(p)])) - dc;
-                    const bool has_l = WORD || p > 0, has_r = !WORD || p + 1 < L;
-                    // second difference along the line (exact: widened FP32 inputs)
-                    const double lap = (has_l && has_r) ? fma(-2.0, dc, dp + dn) : (has_l ? dp - dc : dn - dc);
-                    r = __double2float_rn(fma(gwd, lap, g * src));
-                }
-                x[k] = r;
-                dp = dc;
-                dc = dn;
+        for (int k = 0; k < SEG; ++k) {
+            const int p = p0 + k;
+            const bool valid = line_ok && p < L;
+            const float nxt = (line_ok && p + 1 < L) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
+            float r = 0.f;
+            if (valid) {
+                const int q = qk(k);
+                r = line_residual<WORD, RES>(prev, cur, nxt, Gs[q], oth[q], WORD ? vl : vin_s[vpad(p)],
+                                             WORD || p > 0, !WORD || p + 1 < L, gw);
             }
-        } else if (RES == 2) {
-            // float-float residual: error-free FP32 transforms (two_sum,
-            // two_prod) carry every difference and product exactly; only the
-            // final collection of the small error terms rounds.  Accuracy is
-            // that of the FP64 form at FP32-pipe cost.
-            float dp = prev0, dc = cur0;
-#pragma unroll
-            for (int k = 0; k < SEG; ++k) {
-                const int p = p0 + k;
-                const bool valid = line_ok && p < L;
-                const float dn = (line_ok && p + 1 < L) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
-                float r = 0.f;
-                if (valid) {
-                    const int q = qk(k);
-                    const float g = Gs[q];
-                    const float o = oth[q];
-                    const bool has_l = WORD || p > 0, has_r = !WORD || p + 1 < L;
-                    float sh, sl, th, tl, a1h, a1l, a2h, a2l, lh, ll;
-                    two_sum(o, WORD ? -vl : vin_s[vpad(p)], sh, sl);       // o -/+ vin
-                    two_sum(sh, -dc, th, tl);                         // ... - own
-                    two_sum(has_l ? dp : dc, -dc, a1h, a1l);          // left difference (0 if absent)
-                    two_sum(has_r ? dn : dc, -dc, a2h, a2l);          // right difference (0 if absent)
-                    two_sum(a1h, a2h, lh, ll);
-                    const float lap_lo = __fadd_rn(ll, __fadd_rn(a1l, a2l));
-                    const float src_lo = __fadd_rn(tl, sl);
-                    const float p1h = __fmul_rn(gw, lh), p1l = __fmaf_rn(gw, lh, -p1h);
-                    const float p2h = __fmul_rn(g, th), p2l = __fmaf_rn(g, th, -p2h);
-                    float rh, rl;
-                    two_sum(p1h, p2h, rh, rl);
-                    const float lo = __fadd_rn(__fadd_rn(rl, __fadd_rn(p1l, p2l)),
-                                               __fmaf_rn(gw, lap_lo, __fmul_rn(g, src_lo)));
-                    r = __fadd_rn(rh, lo);
-                }
-                x[k] = r;
-                dp = dc;
-                dc = dn;
-            }
-        } else {
-            float prev = prev0, cur = cur0;
-#pragma unroll
-            for (int k = 0; k < SEG; ++k) {
-                const int p = p0 + k;
-                const bool valid = line_ok && p < L;
-                const float nxt = (line_ok && p + 1 < L) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
-                float r = 0.f;
-                if (valid) {
-                    const int q = qk(k);
-                    const float g = Gs[q];
-                    const float o = oth[q];
-                    const float gl = WORD ? gw : (p > 0 ? gw : 0.f);
-                    const float gr = WORD ? (p + 1 < L ? gw : 0.f) : gw;
-                    const float src = WORD ? (o - vl) - cur : (o + vin_s[vpad(p)]) - cur;
-                    r = gl * (prev - cur) + gr * (nxt - cur) + g * src;
-                }
-                x[k] = r;
-                prev = cur;
-                cur = nxt;
-            }
+            x[k] = r;
+            prev = cur;
+            cur = nxt;
         }
     }
     // ---- T^-1 r by Thomas, segmented over NSEG lanes ------------------------
@@ -389,9 +301,9 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             }
             if (tid < LD) vin_s[vpad(tid)] = (tid < n) ? (float)inp[((size_t)b * a.numX + x) * n + tid] : 0.f;
             __syncthreads();
-            float omega = a.ctl.omega > 0.f ? a.ctl.omega : 1.f;
-            const bool adapt = !(a.ctl.omega > 0.f);
-            float prev_delta = 0.f;
+            LineStop stop;
+            stop.init(a.ctl.omega);
+            float omega = stop.omega;
             bool res64 = precise_first;
             int status = 0, it = 0, par = 0;
             while (true) {
@@ -420,25 +332,8 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     status = FADESIM_ST_NONFINITE;
                     break;
                 }
-                // stop test: delta * rho / (1 - rho) below the target, rho the
-                // observed contraction (bounded below by omega-1, the SOR rate)
-                // FP32 resolution of the deviation planes: changes below a few
-                // ulps of the largest deviation are rounding, not progress
-                const float floor_v = 4.f * 1.1920929e-07f * vm;
-                bool small;
-                if (it == 1) {
-                    small = delta <= 0.f;
-                } else {
-                    const float ratio = prev_delta > 0.f ? delta / prev_delta : 0.f;
-                    const float rho = fmaxf(ratio, omega - 1.f);
-                    const float est = rho < 0.999f ? delta * rho / (1.f - rho) : INFINITY;
-                    // stalled: the change no longer shrinks and is at rounding level
-                    const bool stalled = delta <= floor_v && ratio >= 0.9f;
-                    small = est <= fmaxf(tol, floor_v) || stalled;
-                    if (adapt && it == 3 && ratio > 0.05f && ratio < 1.f) {
-                        omega = fminf(1.9f, 2.f / (1.f + sqrtf(1.f - ratio)));
-                    }
-                }
+                const bool small = stop.update(delta, vm, tol);
+                omega = stop.omega;
                 if (small) {
                     // the final test must pass on an iteration whose residual was
                     // FP64 (kres < 0: FP32 only, the FP32 test is final)
@@ -454,7 +349,6 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     status = FADESIM_ST_MAXITER;
                     break;
                 }
-                prev_delta = delta;
             }
             // ---- outputs ------------------------------------------------------
             if (tid == 0) nonfinite_flag = 0;

@@ -34,8 +34,9 @@ extern "C" {
 #define FADESIM_F64 1
 
 /* solver methods */
-#define FADESIM_METHOD_AUTO 0      /* line relaxation where it fits, else sweep order */
-#define FADESIM_METHOD_LINE 1      /* block line relaxation, residual form, to tolerance */
+#define FADESIM_METHOD_AUTO 0      /* line relaxation up to 512 x 512, else the sweep order */
+#define FADESIM_METHOD_LINE 1      /* block line relaxation, residual form, to tolerance (<= 512 x 512;
+                                      > 128 on 4- or 16-CTA clusters) */
 #define FADESIM_METHOD_RBSOR 2     /* plain red-black point SOR, residual form, to tolerance */
 #define FADESIM_METHOD_SWEEPS 3    /* the reference's sweep order for exactly iter_times sweeps */
 
