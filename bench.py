@@ -160,6 +160,40 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def mixed_batch(torch, n_tiles=4096, n_vec=64, seed=2, steps=3):
+    """4096 tiles with sizes drawn uniformly from {64, 128, 256}^2 (square), 64
+    Bernoulli 0.2 V vectors each, one CUDA-graph replay per step."""
+    from fadesim_gb300.batched import TileBatch, TileGroup
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice([64, 128, 256], size=n_tiles)
+    groups = []
+    for n in (64, 128, 256):
+        T = int((sizes == n).sum())
+        states = rng.integers(0, 4, (T, n, n), dtype=np.int8)
+        G = torch.from_numpy((1.0 / R_STATES)[states].astype(np.float32)).cuda()
+        v = torch.from_numpy((rng.integers(0, 2, (n_vec, T, n)) * V_READ).astype(np.float32)).cuda()
+        groups.append(TileGroup(G, v))
+    batch = TileBatch(groups, g_wire=1 / R_WIRE, tuned=False)
+    st = batch.run(stats=True)
+    batch.capture()
+    batch.replay()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        batch.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"workload": "4096 tiles, sizes uniform in {64,128,256}^2, 64 vectors each, one CUDA graph",
+            "tiles_by_size": {str(g.n): g.T for g in groups}, "solves_per_step": batch.solves,
+            "ms_per_step": ms, "solves_per_s": batch.solves / (ms / 1e3),
+            "nodes_per_s": sum(g.solves * 2 * g.n * g.n for g in groups) / (ms / 1e3),
+            "iters_max_by_size": {str(g.n): s["iters_max"] for g, s in zip(groups, st)},
+            "status_or": int(np.bitwise_or.reduce([s["status_or"] for s in st]))}
+
+
 def check_accuracy(acc, G, vin, torch):
     """A seeded sample of solves against the FP64 oracle (both planes)."""
     from oracle import nodal
@@ -271,6 +305,9 @@ def run_ours(args):
         torch.cuda.synchronize()
         variants[vname + "_solves_per_s"] = solves_per_step / (v0.elapsed_time(v1) / 1e3)
 
+    # the mixed-size batch (tiles of 64, 128 and 256)
+    mixed = mixed_batch(torch) if not args.no_mixed else None
+
     # the plain red-black SOR kernel on a bounded sample of the same workload
     nps = 256
     tgs = tg[:nps // 16].contiguous()
@@ -303,7 +340,8 @@ def run_ours(args):
                    "line_iters_max": stats["iters_max"],
                    "plain_rbsor_solves_per_s": rb_value,
                    "plain_rbsor_sweeps_mean": rb_stats["iters_sum"] / max(1, rb_stats["solves"]),
-                   "speedup_vs_plain_rbsor": value / world / rb_value, **variants},
+                   "speedup_vs_plain_rbsor": value / world / rb_value, **variants,
+                   "mixed_sizes": mixed},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "traffic": traffic * solves_per_step if traffic else None,
@@ -328,6 +366,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tiles", type=int, default=N_TILES, help="128x128 tiles per rank (64 vectors each)")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-size (64/128/256) batch figure")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident solve only (no e2e, comparator or CPU baseline); for profiling")
     args = ap.parse_args()

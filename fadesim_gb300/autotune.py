@@ -1,0 +1,84 @@
+"""Project autotuner for the solver's launch parameters.
+
+For a tile shape it times a small set of candidate settings on a seeded sample
+of the caller's own tiles -- work split (vectors per CTA), precise-residual
+period, and for the point-SOR comparator the relaxation factor -- keeps the
+fastest that converges, and caches the winner in a JSON file keyed by GPU name,
+shape and method.  ``lookup`` returns the cached keyword arguments for
+``cpp_ir_drop_accelerate.ir_drop_gs_ex`` (empty when nothing is cached).
+"""
+import json
+import os
+import threading
+import time
+
+import torch
+
+from . import cpp_ir_drop_accelerate as _acc
+
+CACHE = os.environ.get("FADESIM_TUNE_CACHE",
+                       os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json"))
+_lock = threading.Lock()
+_mem = None
+
+
+def _key(n, m, method):
+    name = torch.cuda.get_device_name() if torch.cuda.is_available() else "cpu"
+    return "%s|%dx%d|%s" % (name, n, m, method)
+
+
+def _load():
+    global _mem
+    if _mem is None:
+        try:
+            with open(CACHE) as f:
+                _mem = json.load(f)
+        except (OSError, ValueError):
+            _mem = {}
+    return _mem
+
+
+def lookup(n, m, method="line"):
+    with _lock:
+        return dict(_load().get(_key(n, m, method), {}).get("kw", {}))
+
+
+def _store(n, m, method, kw, ms):
+    with _lock:
+        d = _load()
+        d[_key(n, m, method)] = {"kw": kw, "ms": ms}
+        os.makedirs(os.path.dirname(CACHE), exist_ok=True)
+        tmp = CACHE + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, CACHE)
+
+
+def candidates(method):
+    if method == "rbsor":
+        return [dict(omega=w) for w in (1.96, 1.97, 1.975, 1.98, 1.985)]
+    return [dict(vectors_per_cta=v, residual_period=k) for v in (0, 8, 32) for k in (1, 4)]
+
+
+def tune(G, vin, g_wire=1 / 2.93, method="line", reps=3):
+    """Time each candidate on (G [T, n, m], vin [B, T, n]) and cache the fastest
+    setting whose solves all converged.  Returns (kwargs, ms per call)."""
+    T, n, m = G.shape
+    B = vin.shape[0]
+    best = None
+    for kw in candidates(method):
+        _, st, _ = _acc.ir_drop_gs_ex(vin, G, B, n, m, T, 1, g_wire=g_wire, method=method, **kw)
+        if st["status_or"] != 1:
+            continue
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            _acc.ir_drop_gs_ex(vin, G, B, n, m, T, 1, g_wire=g_wire, method=method, return_stats=False, **kw)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) * 1e3 / reps
+        if best is None or ms < best[1]:
+            best = (kw, ms)
+    if best is None:
+        raise RuntimeError("no candidate setting converged for %dx%d" % (n, m))
+    _store(n, m, method, best[0], best[1])
+    return best

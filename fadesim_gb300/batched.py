@@ -1,0 +1,87 @@
+"""Batches of crossbar tiles of uneven size, solved as one GPU job.
+
+A layer (or any workload) can hold tiles of several sizes, each with its own
+input vectors.  Tiles are grouped by shape; every group is one launch of the
+solver that fits it (shared-memory tile-per-CTA kernel up to 128 x 128,
+cluster-per-tile kernel up to 512 x 512), and the groups run concurrently on
+forked streams.  ``TileBatch.capture()`` records the whole job as one CUDA graph
+for replay (inputs updated in place between replays).  Per-shape launch
+parameters come from ``fadesim_gb300.autotune`` when a tuned entry exists.
+"""
+import torch
+
+from . import autotune
+from . import cpp_ir_drop_accelerate as _acc
+
+
+class TileGroup:
+    """Tiles of one shape: G [T, n, m] and inputs vin [B, T, n] (contiguous, CUDA)."""
+
+    def __init__(self, G, vin):
+        if G.dim() != 3 or vin.dim() != 3 or vin.shape[1] != G.shape[0] or vin.shape[2] != G.shape[1]:
+            raise ValueError("TileGroup wants G [T, n, m] and vin [B, T, n]")
+        self.G = G.contiguous()
+        self.vin = vin.contiguous()
+        self.T, self.n, self.m = G.shape
+        self.B = vin.shape[0]
+        self.out = torch.empty((self.B, self.T, self.m), dtype=G.dtype, device=G.device)
+
+    @property
+    def solves(self):
+        return self.B * self.T
+
+
+class TileBatch:
+    """Several TileGroups solved together (one group per shape)."""
+
+    def __init__(self, groups, g_wire=1 / 2.93, method="line", tol_v=1e-8, residual="ff", tuned=True):
+        self.groups = list(groups)
+        self.g_wire = g_wire
+        self.method = method
+        self.tol_v = tol_v
+        self.residual = residual
+        self.tuned = tuned
+        self.streams = [torch.cuda.Stream() for _ in self.groups]
+        self.graph = None
+
+    @property
+    def solves(self):
+        return sum(g.solves for g in self.groups)
+
+    def _launch(self, g, stream, stats):
+        kw = autotune.lookup(g.n, g.m, self.method) if self.tuned else {}
+        with torch.cuda.stream(stream):
+            _, st, _ = _acc.ir_drop_gs_ex(g.vin, g.G, g.B, g.n, g.m, g.T, 1, g_wire=self.g_wire, method=self.method,
+                                          tol_v=self.tol_v, residual=self.residual, return_stats=stats,
+                                          out=g.out, **kw)
+        return st
+
+    def run(self, stats=False):
+        """Solve every group; returns the per-group stats when ``stats``."""
+        main = torch.cuda.current_stream()
+        ev = torch.cuda.Event()
+        ev.record(main)
+        out = []
+        for g, s in zip(self.groups, self.streams):
+            s.wait_event(ev)
+            out.append(self._launch(g, s, stats))
+        for s in self.streams:
+            main.wait_stream(s)
+        return out if stats else None
+
+    def capture(self):
+        """Record run() as a CUDA graph (warm-up launch first, as graph capture needs)."""
+        self.run()
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.run()
+        return self.graph
+
+    def replay(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()
+
+    def outputs(self):
+        return [g.out for g in self.groups]
