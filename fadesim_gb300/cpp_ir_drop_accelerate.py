@@ -39,6 +39,8 @@ class SolverOptions:
     omega: float = 0.0           # 0: adaptive (line) / size formula (rbsor)
     vectors_per_cta: int = 0     # 0: automatic
     residual: str = "ff"         # precise residual: "ff" (float-float on the FP32 pipe) or "fp64"
+    read_noise_sigma: float = 0.0  # > 0: Gaussian read noise, sigma relative to each cell current
+    noise_seed: int = 0
 
     def to_c(self, method=None):
         m = method if method is not None else self.method
@@ -47,7 +49,8 @@ class SolverOptions:
         if self.residual not in ("fp64", "ff"):
             raise ValueError("residual must be 'fp64' or 'ff'")
         return _lib.SolveOpts(_METHODS[m], float(self.tol_v), int(self.max_iters), int(self.residual_period),
-                              float(self.omega), int(self.vectors_per_cta), 1 if self.residual == "fp64" else 0)
+                              float(self.omega), int(self.vectors_per_cta), 1 if self.residual == "fp64" else 0,
+                              float(self.read_noise_sigma), int(self.noise_seed) & (2 ** 64 - 1))
 
 
 options = SolverOptions()
@@ -126,7 +129,8 @@ def ir_drop_gs(input, G, batch_size, row_size, col_size, numX, numY, iter_times,
 def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_times=600, g_wire=1 / 2.93, beta=1.9,
                   enable_break=False, break_threshould=1e-7, nonlinear_cell_enable=False, nonlinear_params=(),
                   ret_V=False, method=None, tol_v=None, max_iters=None, residual_period=None, omega=None,
-                  vectors_per_cta=None, residual=None, return_stats=True, return_iters=False, out=None):
+                  vectors_per_cta=None, residual=None, read_noise_sigma=None, noise_seed=None, return_stats=True,
+                  return_iters=False, out=None):
     """``ir_drop_gs`` with explicit solver options (``ret_V=2`` returns both node
     planes, [batch, numX, numY, 2, rows, cols]).  Returns (out, stats, iters):
     stats is a dict (solves, iters_sum, iters_max, status_or) and iters an int32
@@ -134,7 +138,8 @@ def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_tim
     may be a preallocated contiguous tensor of the output's size."""
     o = SolverOptions(**{k: v for k, v in vars(options).items()})
     for k, v in dict(tol_v=tol_v, max_iters=max_iters, residual_period=residual_period, omega=omega,
-                     vectors_per_cta=vectors_per_cta, residual=residual).items():
+                     vectors_per_cta=vectors_per_cta, residual=residual, read_noise_sigma=read_noise_sigma,
+                     noise_seed=noise_seed).items():
         if v is not None:
             setattr(o, k, v)
     out, st, it = _solve(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, beta,

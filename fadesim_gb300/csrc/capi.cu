@@ -205,9 +205,11 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
     if (batch_size < 0 || numX < 1 || numY < 1) return fail(FADESIM_E_ARG, "batch_size >= 0, numX >= 1, numY >= 1");
     if (!(g_wire > 0) || !isfinite(g_wire)) return fail(FADESIM_E_ARG, "g_wire must be positive and finite");
     if (nonlinear_cell_enable) {
-        (void)nonlinear_params;
-        (void)n_nonlinear_params;
-        return fail(FADESIM_E_UNSUPPORTED, "nonlinear cells are not implemented in this build");
+        if (!nonlinear_params || n_nonlinear_params < 6)
+            return fail(FADESIM_E_ARG, "nonlinear_params must hold [R_on, R_off, a_on, b_on, a_off, b_off]");
+        const double *q = nonlinear_params;
+        if (!(q[1] > q[0]) || !(q[2] > 0) || !(q[3] > 0) || !(q[4] > 0) || !(q[5] > 0))
+            return fail(FADESIM_E_ARG, "nonlinear_params need R_off > R_on and positive a, b");
     }
     if (stats) *stats = fadesim_solve_stats{0, 0, 0, 0};
     if (batch_size == 0) return FADESIM_OK;
@@ -224,10 +226,28 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
     a.gw = (float)g_wire;
     a.ret_V = ret_V == 2 ? 2 : (ret_V ? 1 : 0);
     a.iters_out = per_solve_iters;
+    if (nonlinear_cell_enable) {
+        const double *q = nonlinear_params;
+        a.ctl.nl = 1;
+        a.ctl.nl_R_on = (float)q[0];
+        a.ctl.nl_inv_dR = (float)(1.0 / (q[1] - q[0]));
+        a.ctl.nl_a_on = (float)q[2];
+        a.ctl.nl_a_off = (float)q[4];
+        a.ctl.nl_r0_on = (float)(1.0 / (q[2] * q[3]));
+        a.ctl.nl_r0_off = (float)(1.0 / (q[4] * q[5]));
+    }
+    if (opts && opts->read_noise_sigma > 0) {
+        a.ctl.noise_sigma = (float)opts->read_noise_sigma;
+        a.ctl.noise_seed = opts->noise_seed;
+    }
     int method = opts ? opts->method : FADESIM_METHOD_AUTO;
     if (method == FADESIM_METHOD_AUTO)
         method = (line_relax_ld(row_size, col_size) || cluster_relax_ld(row_size, col_size)) ? FADESIM_METHOD_LINE
                                                                                            : FADESIM_METHOD_SWEEPS;
+    if (nonlinear_cell_enable && method != FADESIM_METHOD_LINE)
+        return fail(FADESIM_E_UNSUPPORTED, "nonlinear cells are solved by the line method (rows, cols <= 512)");
+    if (a.ctl.noise_sigma > 0 && (method != FADESIM_METHOD_LINE || ret_V))
+        return fail(FADESIM_E_UNSUPPORTED, "read noise applies to the line method's currents");
     switch (method) {
         case FADESIM_METHOD_LINE:
         case FADESIM_METHOD_RBSOR:

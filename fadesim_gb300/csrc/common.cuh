@@ -22,7 +22,43 @@ struct SolveCtl {
     int residual_period;  // precise residual every k iterations (<0: never)
     float omega;          // <= 0: adaptive
     int residual_ff;      // precise residual in float-float (FP32 pipe) instead of FP64
+    // sinh cells (nonlinear_params = [R_on, R_off, a_on, b_on, a_off, b_off])
+    int nl;
+    float nl_R_on, nl_inv_dR;        // z = (1/g_lin - R_on) / (R_off - R_on), clamped at 0
+    float nl_a_on, nl_a_off;         // a of I = b sinh(a V)
+    float nl_r0_on, nl_r0_off;       // 1 / (a b): the state's resistance at V -> 0
+    // additive read noise on every cell current: N(0, (sigma I_cell)^2)
+    float noise_sigma;
+    unsigned long long noise_seed;
 };
+
+// sinh(t)/t, t >= 0 (series below 1e-2: truncation < 1e-10)
+__device__ __forceinline__ float sinhc(float t) { return t < 1e-2f ? fmaf(t * t, 1.f / 6.f, 1.f) : sinhf(t) / t; }
+
+// Chord conductance I(V)/V of the reference's sinh cell at cell voltage V for
+// a cell at position z between the on and off states:
+// 1/R(V), R(V) = (1-z) |V| / (b_on sinh(a_on |V|)) + z |V| / (b_off sinh(a_off |V|)).
+__device__ __forceinline__ float nl_geff(float z, float V, const SolveCtl &c) {
+    const float x = fabsf(V);
+    const float R = (1.f - z) * c.nl_r0_on / sinhc(c.nl_a_on * x) + z * c.nl_r0_off / sinhc(c.nl_a_off * x);
+    return 1.f / R;
+}
+
+__device__ __forceinline__ float nl_z(float g, const SolveCtl &c) {
+    return g > 0.f ? fmaxf(0.f, (1.f / g - c.nl_R_on) * c.nl_inv_dR) : 0.f;
+}
+
+// Standard normal from a counter (splitmix64 hash, Box-Muller): the same value
+// for the same (seed, a, b) on every run and every device.
+__device__ __forceinline__ float normal_from(unsigned long long seed, unsigned long long a, unsigned long long b) {
+    unsigned long long zz = seed + 0x9E3779B97F4A7C15ull * (a * 0x100000001B3ull + b + 1ull);
+    zz = (zz ^ (zz >> 30)) * 0xBF58476D1CE4E5B9ull;
+    zz = (zz ^ (zz >> 27)) * 0x94D049BB133111EBull;
+    zz ^= zz >> 31;
+    const float u1 = ((float)(unsigned int)(zz >> 40) + 0.5f) * (1.f / 16777216.f);   // (0, 1)
+    const float u2 = (float)(unsigned int)(zz & 0xffffffu) * (1.f / 16777216.f);      // [0, 1)
+    return sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
+}
 
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll

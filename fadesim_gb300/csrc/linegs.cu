@@ -72,11 +72,12 @@ __device__ __forceinline__ int vpad(int p) { return p + (p >> 4); }
 
 // One pass over all lines of one plane.  WORD: wordline rows (own plane = U
 // deviations, other = D); else bitline columns (own = D, other = U).
-template <int LD, bool WORD, int RES>
+template <int LD, bool WORD, int RES, bool NL>
 __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *__restrict__ oth,
                                           const float *__restrict__ Gs, const float *__restrict__ vin_s,
                                           const float *__restrict__ piv, const float *__restrict__ segprod, int L,
-                                          int NL, float gw, float omega, float &dmax, float &vmax) {
+                                          int NLINES, float gw, float omega, float &dmax, float &vmax,
+                                          const SolveCtl &ctl) {
     constexpr int SEG = LineCfg<LD>::SEG;
     constexpr int T = LineCfg<LD>::T;
     constexpr int LPW = LineCfg<LD>::LPW;
@@ -85,7 +86,7 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     const int lane = tid & 31;
     const int s = lane / LPW;
     const int line = (tid >> 5) * LPW + (lane % LPW);
-    const bool line_ok = line < NL;
+    const bool line_ok = line < NLINES;
     const int p0 = s * SEG;
     auto at = [&](int p) { return WORD ? swz<LD>(line, p) : swz<LD>(p, line); };
     // Addresses of this segment's nodes.  The swizzle term is constant along a
@@ -117,8 +118,10 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
             float r = 0.f;
             if (valid) {
                 const int q = qk(k);
-                r = line_residual<WORD, RES>(prev, cur, nxt, Gs[q], oth[q], WORD ? vl : vin_s[vpad(p)],
-                                             WORD || p > 0, !WORD || p + 1 < L, gw);
+                const float o = oth[q], vv = WORD ? vl : vin_s[vpad(p)];
+                // cell conductance: stored, or the sinh cell's at the present cell voltage
+                const float g = NL ? nl_geff(Gs[q], WORD ? (cur + vv) - o : (o + vv) - cur, ctl) : Gs[q];
+                r = line_residual<WORD, RES>(prev, cur, nxt, g, o, vv, WORD || p > 0, !WORD || p + 1 < L, gw);
             }
             x[k] = r;
             prev = cur;
@@ -240,7 +243,7 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
     }
 }
 
-template <int LD, typename TIO>
+template <int LD, typename TIO, bool NL>
 __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_kernel(SolveArgs a) {
     constexpr int T = LineCfg<LD>::T;
     constexpr int NW = LineCfg<LD>::NW;
@@ -291,6 +294,14 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             __syncthreads();
             line_pivots<LD>(Gs, piv, n, m, gw);
             __syncthreads();
+            if (NL) {
+                // the sinh cells keep their on/off position; the linear values served the pivots
+                for (int e = tid; e < n * m; e += T) {
+                    const int i = e / m, j = e - i * m;
+                    Gs[swz<LD>(i, j)] = nl_z(Gs[swz<LD>(i, j)], a.ctl);
+                }
+                __syncthreads();
+            }
             cached_tile = tile;
         }
         for (int b = b0; b < b1; ++b) {
@@ -308,13 +319,13 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             int status = 0, it = 0, par = 0;
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
-                if (!res64) line_pass<LD, true, 0>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax);
-                else if (ff) line_pass<LD, true, 2>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax);
-                else line_pass<LD, true, 1>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax);
+                if (!res64) line_pass<LD, true, 0, NL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax, a.ctl);
+                else if (ff) line_pass<LD, true, 2, NL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax, a.ctl);
+                else line_pass<LD, true, 1, NL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax, a.ctl);
                 __syncthreads();
-                if (!res64) line_pass<LD, false, 0>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax);
-                else if (ff) line_pass<LD, false, 2>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax);
-                else line_pass<LD, false, 1>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax);
+                if (!res64) line_pass<LD, false, 0, NL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax, a.ctl);
+                else if (ff) line_pass<LD, false, 2, NL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax, a.ctl);
+                else line_pass<LD, false, 1, NL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax, a.ctl);
                 dmax = warp_max(dmax);
                 vmax = warp_max(vmax);
                 if ((tid & 31) == 0) {
@@ -380,7 +391,14 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                         const int i = s * SEG + k;
                         if (i < n) {
                             const int q = swz<LD>(i, j);
-                            acc += (TIO)Gs[q] * (((TIO)U[q] + (TIO)vin_s[vpad(i)]) - (TIO)D[q]);
+                            const TIO V = ((TIO)U[q] + (TIO)vin_s[vpad(i)]) - (TIO)D[q];
+                            TIO Ic = (TIO)(NL ? nl_geff(Gs[q], (float)V, a.ctl) : Gs[q]) * V;
+                            if (a.ctl.noise_sigma > 0.f)
+                                Ic *= (TIO)1 + (TIO)(a.ctl.noise_sigma *
+                                                     normal_from(a.ctl.noise_seed,
+                                                                 ((unsigned long long)b * a.numX + x) * a.numY + y,
+                                                                 (unsigned long long)i * m + j));
+                            acc += Ic;
                         }
                     }
                 }
@@ -425,7 +443,10 @@ size_t line_relax_scratch_floats_per_cta(int ld) { return (size_t)2 * ld * ld + 
 
 template <int LD, typename TIO>
 static cudaError_t prep_one() {
-    return cudaFuncSetAttribute(line_relax_kernel<LD, TIO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(line_relax_kernel<LD, TIO, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)line_relax_smem(LD));
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(line_relax_kernel<LD, TIO, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)line_relax_smem(LD));
 }
 
@@ -443,7 +464,7 @@ cudaError_t line_relax_prepare(int ld, int dtype) {
 
 template <int LD, typename TIO>
 static cudaError_t occ_one(int *n) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, line_relax_kernel<LD, TIO>, LineCfg<LD>::T,
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, line_relax_kernel<LD, TIO, false>, LineCfg<LD>::T,
                                                          line_relax_smem(LD));
 }
 
@@ -461,7 +482,8 @@ cudaError_t line_relax_occupancy(int ld, int dtype, int *ctas) {
 
 template <int LD, typename TIO>
 static cudaError_t launch_one(const SolveArgs &a, int grid, cudaStream_t st) {
-    line_relax_kernel<LD, TIO><<<grid, LineCfg<LD>::T, line_relax_smem(LD), st>>>(a);
+    if (a.ctl.nl) line_relax_kernel<LD, TIO, true><<<grid, LineCfg<LD>::T, line_relax_smem(LD), st>>>(a);
+    else line_relax_kernel<LD, TIO, false><<<grid, LineCfg<LD>::T, line_relax_smem(LD), st>>>(a);
     return cudaGetLastError();
 }
 

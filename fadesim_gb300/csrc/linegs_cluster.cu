@@ -103,11 +103,12 @@ __device__ __forceinline__ void scan_down(float C, float X, int s, float &Cinc, 
 }
 
 // Wordline pass over the CTA's rows (lines local to the CTA).
-template <int LDM, int RES>
+template <int LDM, int RES, bool NL>
 __device__ __forceinline__ void cl_word_pass(float *__restrict__ U, const float *__restrict__ D,
                                              const float *__restrict__ Gs, const float *__restrict__ vin,
                                              const float *__restrict__ piv, const float *__restrict__ segprod,
-                                             int nloc, int m, float gw, float omega, float &dmax, float &vmax) {
+                                             int nloc, int m, float gw, float omega, float &dmax, float &vmax,
+                                             const SolveCtl &ctl) {
     constexpr int NSEG = CCfg<LDM>::NSEG_W, LPW = CCfg<LDM>::LPW_W, SEG = CL_SEG, S = CCfg<LDM>::S;
     const int tid = threadIdx.x, lane = tid & 31, s = lane / LPW;
     const int line = (tid >> 5) * LPW + (lane % LPW);
@@ -124,7 +125,11 @@ __device__ __forceinline__ void cl_word_pass(float *__restrict__ U, const float 
             const int p = p0 + k;
             const float nxt = (ok && p + 1 < m) ? U[k + 1 < SEG ? base + k + 1 : base + SEG + 1] : 0.f;
             float r = 0.f;
-            if (ok && p < m) r = line_residual<true, RES>(prev, cur, nxt, Gs[base + k], D[base + k], vl, true, p + 1 < m, gw);
+            if (ok && p < m) {
+                const float o = D[base + k];
+                const float g = NL ? nl_geff(Gs[base + k], (cur + vl) - o, ctl) : Gs[base + k];
+                r = line_residual<true, RES>(prev, cur, nxt, g, o, vl, true, p + 1 < m, gw);
+            }
             x[k] = r;
             prev = cur;
             cur = nxt;
@@ -170,14 +175,14 @@ __device__ __forceinline__ void cl_word_pass(float *__restrict__ U, const float 
 }
 
 // Bitline pass: columns cross the cluster.  Contains two cluster barriers.
-template <int LDM, int RES>
+template <int LDM, int RES, bool NL>
 __device__ __forceinline__ void cl_bit_pass(cg::cluster_group &cluster, int rank, float *__restrict__ D,
                                             const float *__restrict__ U, const float *__restrict__ Gs,
                                             const float *__restrict__ vin, const float *__restrict__ piv,
                                             const float *__restrict__ segprod, const float *__restrict__ hup,
                                             const float *__restrict__ hdn, float *__restrict__ aggF,
                                             float *__restrict__ aggB, int row0, int nloc, int m, float gw,
-                                            float omega, float &dmax, float &vmax) {
+                                            float omega, float &dmax, float &vmax, const SolveCtl &ctl) {
     constexpr int C = CCfg<LDM>::C, NSEG = CCfg<LDM>::NSEG_B, LPW = CCfg<LDM>::LPW_B, SEG = CL_SEG;
     constexpr int S = CCfg<LDM>::S;
     const int tid = threadIdx.x, lane = tid & 31, s = lane / LPW;
@@ -195,9 +200,11 @@ __device__ __forceinline__ void cl_bit_pass(cg::cluster_group &cluster, int rank
             float nxt = 0.f;
             if (ok) nxt = (lr + 1 < nloc) ? D[(lr + 1) * S + cb] : hdn[col];
             float r = 0.f;
-            if (ok && lr < nloc)
-                r = line_residual<false, RES>(prev, cur, nxt, Gs[lr * S + cb], U[lr * S + cb], vin[lr], row0 + lr > 0,
-                                              true, gw);
+            if (ok && lr < nloc) {
+                const float o = U[lr * S + cb];
+                const float g = NL ? nl_geff(Gs[lr * S + cb], (o + vin[lr]) - cur, ctl) : Gs[lr * S + cb];
+                r = line_residual<false, RES>(prev, cur, nxt, g, o, vin[lr], row0 + lr > 0, true, gw);
+            }
             x[k] = r;
             prev = cur;
             cur = nxt;
@@ -366,7 +373,7 @@ __device__ void cl_pivots(cg::cluster_group &cluster, int rank, const float *__r
     cluster.sync();  // the band products are read remotely until here
 }
 
-template <int LDM, typename TIO>
+template <int LDM, typename TIO, bool NL>
 __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a) {
     constexpr int C = CCfg<LDM>::C, RPC = CCfg<LDM>::RPC, S = CCfg<LDM>::S, SEG = CL_SEG;
     constexpr int LPW_B = CCfg<LDM>::LPW_B, NSEG_B = CCfg<LDM>::NSEG_B;
@@ -420,6 +427,13 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             __syncthreads();
             cl_pivots<LDM>(cluster, rank, Gs, piv, reinterpret_cast<double *>(aux), row0, nloc, n, m, gw);
             __syncthreads();
+            if (NL) {
+                for (int e = tid; e < RPC * LDM; e += CL_T) {
+                    const int lr = e / LDM, c = e - lr * LDM;
+                    Gs[cidx<LDM>(lr, c)] = nl_z(Gs[cidx<LDM>(lr, c)], a.ctl);
+                }
+                __syncthreads();
+            }
             cached_tile = tile;
         }
         for (int b = b0; b < b1; ++b) {
@@ -438,9 +452,9 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             int status = 0, it = 0, par = 0;
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
-                if (!res64) cl_word_pass<LDM, 0>(U, D, Gs, vin, piv, piv + 2 * SEG * CL_T, nloc, m, gw, omega, dmax, vmax);
-                else if (ff) cl_word_pass<LDM, 2>(U, D, Gs, vin, piv, piv + 2 * SEG * CL_T, nloc, m, gw, omega, dmax, vmax);
-                else cl_word_pass<LDM, 1>(U, D, Gs, vin, piv, piv + 2 * SEG * CL_T, nloc, m, gw, omega, dmax, vmax);
+                if (!res64) cl_word_pass<LDM, 0, NL>(U, D, Gs, vin, piv, piv + 2 * SEG * CL_T, nloc, m, gw, omega, dmax, vmax, a.ctl);
+                else if (ff) cl_word_pass<LDM, 2, NL>(U, D, Gs, vin, piv, piv + 2 * SEG * CL_T, nloc, m, gw, omega, dmax, vmax, a.ctl);
+                else cl_word_pass<LDM, 1, NL>(U, D, Gs, vin, piv, piv + 2 * SEG * CL_T, nloc, m, gw, omega, dmax, vmax, a.ctl);
                 __syncthreads();
                 if (tid < LDM) {
                     // halo rows: the row above the band and the row below it (0 V ground below the last row)
@@ -453,14 +467,14 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 __syncthreads();
                 float *pB = piv + SEG * CL_T, *sB = piv + 2 * SEG * CL_T + CL_T;
                 if (!res64)
-                    cl_bit_pass<LDM, 0>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, gw,
-                                        omega, dmax, vmax);
+                    cl_bit_pass<LDM, 0, NL>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, gw,
+                                        omega, dmax, vmax, a.ctl);
                 else if (ff)
-                    cl_bit_pass<LDM, 2>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, gw,
-                                        omega, dmax, vmax);
+                    cl_bit_pass<LDM, 2, NL>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, gw,
+                                        omega, dmax, vmax, a.ctl);
                 else
-                    cl_bit_pass<LDM, 1>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, gw,
-                                        omega, dmax, vmax);
+                    cl_bit_pass<LDM, 1, NL>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, gw,
+                                        omega, dmax, vmax, a.ctl);
                 dmax = warp_max(dmax);
                 vmax = warp_max(vmax);
                 if ((tid & 31) == 0) {
@@ -531,7 +545,14 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                         const int lr = s * SEG + k;
                         if (lr < nloc) {
                             const int q = cidx<LDM>(lr, j);
-                            acc += Gs[q] * ((U[q] + vin[lr]) - D[q]);
+                            const float V = (U[q] + vin[lr]) - D[q];
+                            float Ic = (NL ? nl_geff(Gs[q], V, a.ctl) : Gs[q]) * V;
+                            if (a.ctl.noise_sigma > 0.f)
+                                Ic *= 1.f + a.ctl.noise_sigma *
+                                                normal_from(a.ctl.noise_seed,
+                                                            ((unsigned long long)b * a.numX + x) * a.numY + y,
+                                                            (unsigned long long)(row0 + lr) * m + j);
+                            acc += Ic;
                         }
                     }
                 }
@@ -586,7 +607,7 @@ size_t cluster_relax_scratch_floats_per_cta(int) { return (size_t)2 * CL_SEG * C
 
 template <int LDM, typename TIO>
 static cudaError_t cl_launch_cfg(int *clusters, const SolveArgs *a, int grid, cudaStream_t st) {
-    auto kern = line_relax_cluster_kernel<LDM, TIO>;
+    auto kern = (a && a->ctl.nl) ? line_relax_cluster_kernel<LDM, TIO, true> : line_relax_cluster_kernel<LDM, TIO, false>;
     const size_t smem = cl_smem_floats<LDM>() * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

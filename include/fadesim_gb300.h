@@ -55,6 +55,9 @@ typedef struct fadesim_solve_opts {
     int vectors_per_cta;   /* input vectors one CTA solves per work item; <=0: automatic */
     int residual_kind;     /* precise residual arithmetic: 0 = float-float (default: error-free FP32
                               transforms, FP64-class accuracy on the FP32 pipe), 1 = native FP64 */
+    double read_noise_sigma;        /* > 0: each cell current gets N(0, (sigma * I_cell)^2) in the returned
+                                       bitline currents (line method); not a reference feature */
+    unsigned long long noise_seed;  /* counter-based: same seed, same noise */
 } fadesim_solve_opts;
 
 typedef struct fadesim_solve_stats {

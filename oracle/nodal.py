@@ -138,3 +138,58 @@ def min_eigen_bound(n, m, g_wire):
     """
     L = max(n, m)
     return float(g_wire) * 4.0 * np.sin(np.pi / (2.0 * (2 * L + 1))) ** 2
+
+
+def nonlinear_z(g_lin, R_on, R_off):
+    """Cell position between the on and off states from its linear conductance,
+    z = (1/g - R_on) / (R_off - R_on), negative z set to 0
+    (split_arr_matmul.cu:176-182 get_nonlinear_ratio_z, called at :244)."""
+    z = (1.0 / np.asarray(g_lin, np.float64) - R_on) / (R_off - R_on)
+    return np.where(z < 0, 0.0, z)
+
+
+def nonlinear_conductance(V, z, params):
+    """Chord conductance I(V)/V of the sinh cell: 1/R(V) with
+    R(V) = (1-z) |V| / (b_on sinh(a_on |V|)) + z |V| / (b_off sinh(a_off |V|))
+    (split_arr_matmul.cu:184-196 nonlinear_R_tensor), evaluated without the
+    reference's |V| < 1e-5 clamp (deal_v, :142-166) by the limit sinh(x)/x -> 1."""
+    R_on, R_off, a_on, b_on, a_off, b_off = [float(p) for p in params]
+    x = np.abs(np.asarray(V, np.float64))
+
+    def r(a, b):
+        ax = a * x
+        f = np.where(ax < 1e-4, 1.0 + ax * ax / 6.0, np.sinh(np.maximum(ax, 1e-300)) / np.maximum(ax, 1e-300))
+        return 1.0 / (a * b * f)
+
+    return 1.0 / ((1.0 - z) * r(a_on, b_on) + z * r(a_off, b_off))
+
+
+def solve_nonlinear(g_lin, g_wire, vin, params, tol=1e-14, max_iter=200):
+    """FP64 fixed point of the nonlinear nodal system by Picard iteration: the
+    cell conductances are re-evaluated at the current cell voltages and the
+    linear system is solved exactly (sparse LU) until the node voltages move
+    less than ``tol``.  Returns (u, d, iterations)."""
+    z = nonlinear_z(g_lin, params[0], params[1])
+    g = np.asarray(g_lin, np.float64).copy()
+    u, d = solve(g, g_wire, vin)
+    for it in range(1, max_iter + 1):
+        g = nonlinear_conductance(u - d, z, params)
+        u2, d2 = solve(g, g_wire, vin)
+        delta = max(np.abs(u2 - u).max(), np.abs(d2 - d).max())
+        u, d = u2, d2
+        if delta < tol:
+            return u, d, it
+    raise RuntimeError("nonlinear oracle did not converge")
+
+
+def nonlinear_currents(g_lin, u, d, params):
+    z = nonlinear_z(g_lin, params[0], params[1])
+    V = u - d
+    return (nonlinear_conductance(V, z, params) * V).sum(axis=-2)
+
+
+def sinh_params(R_on, R_off, a=2.0):
+    """[R_on, R_off, a_on, b_on, a_off, b_off] for I = (V/R) sinh(aV)/(aV), i.e.
+    b = 1/(a R): the cell law of the large-tile non-ideal configuration written
+    in the reference's parameterisation (commonConst.py:200-207)."""
+    return [R_on, R_off, a, 1.0 / (a * R_on), a, 1.0 / (a * R_off)]

@@ -82,3 +82,59 @@ def ir_drop_gs(input_v, G, batch_size, row_size, col_size, numX, numY, iter_time
     if return_iters:
         return res, iters
     return res
+
+
+def ir_drop_gs_nonlinear(input_v, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, beta, params):
+    """The reference's nonlinear sweeps (split_arr_matmul.cu:241-262), FP64.
+
+    Before every sweep the cell conductances are recomputed from the cell
+    voltages held in the buffers the sweep is about to overwrite -- after the
+    ping-pong swap those hold the state from two sweeps back -- with |V| < 1e-5
+    clamped to +-1e-5 (deal_v) and z from the linear conductances.  Returns the
+    currents computed with the last conductances, as get_current does.
+    """
+    import numpy as _np
+    R_on, R_off, a_on, b_on, a_off, b_off = [float(p) for p in params]
+    B, X, Y, n, m = batch_size, numX, numY, row_size, col_size
+    gw = float(g_wire)
+    w = float(beta)
+    inp = _np.asarray(input_v, _np.float64).reshape(B, X, n)
+    glin = _np.asarray(G, _np.float64).reshape(X, n, Y, m).transpose(0, 2, 1, 3)[None]
+    z = (1.0 / glin - R_on) / (R_off - R_on)
+    z = _np.where(z < 0, 0.0, z)
+    cur_u = _np.broadcast_to(inp[:, :, None, :, None], (B, X, Y, n, m)).copy()   # "voltage_up"
+    cur_d = _np.zeros((B, X, Y, n, m))
+    prev_u, prev_d = cur_u.copy(), cur_d.copy()                                  # "..._prev" (newest)
+    g = _np.broadcast_to(glin, (B, X, Y, n, m))
+    for _ in range(iter_times):
+        V = cur_u - cur_d
+        small = (V < 1e-5) & (V > -1e-5)
+        V = _np.where(small, _np.where(V > 0, 1e-5, -1e-5), V)
+        Va = _np.abs(V)
+        g = 1.0 / ((1 - z) * Va / (b_on * _np.sinh(a_on * Va)) + z * Va / (b_off * _np.sinh(a_off * Va)))
+        # one sweep in the reference order, writing cur_* from prev_*
+        left = inp[:, :, None, :]
+        for j in range(m):
+            gj = g[..., j]
+            if j == m - 1:
+                num = gw * left + gj * prev_d[..., j]
+                sumg = gw + gj
+            else:
+                num = gw * left + gw * prev_u[..., j + 1] + gj * prev_d[..., j]
+                sumg = 2 * gw + gj
+            cur_u[..., j] = w * num / sumg + (1 - w) * prev_u[..., j]
+            left = cur_u[..., j]
+        below = _np.zeros((B, X, Y, m))
+        for i in range(n - 1, -1, -1):
+            gi = g[..., i, :]
+            if i == 0:
+                num = gw * below + gi * cur_u[..., i, :]
+                sumg = gw + gi
+            else:
+                num = gw * prev_d[..., i - 1, :] + gw * below + gi * cur_u[..., i, :]
+                sumg = 2 * gw + gi
+            cur_d[..., i, :] = w * num / sumg + (1 - w) * prev_d[..., i, :]
+            below = cur_d[..., i, :]
+        cur_u, prev_u = prev_u, cur_u
+        cur_d, prev_d = prev_d, cur_d
+    return ((prev_u - prev_d) * g).sum(axis=3).reshape(B, X, Y * m)
