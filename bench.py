@@ -194,6 +194,35 @@ def mixed_batch(torch, n_tiles=4096, n_vec=64, seed=2, steps=3):
             "status_or": int(np.bitwise_or.reduce([s["status_or"] for s in st]))}
 
 
+def large_nonideal(torch, acc, n_tiles=64, n_vec=32, seed=5):
+    """512x512 tiles on 16-CTA clusters with sinh cells I = (V/R) sinh(2V)/(2V),
+    lognormal R variation (sigma 0.1), 1% Gaussian read noise, 32 inputs per tile
+    uniform in [0, 0.2] V: a bounded sample of the 1024-tile configuration."""
+    from fadesim_gb300.variation import add_variation_device
+    rng = np.random.default_rng(seed)
+    n = 512
+    states = rng.integers(0, 4, (n_tiles, n, n), dtype=np.int8)
+    G = torch.from_numpy((1.0 / R_STATES)[states].astype(np.float32)).cuda()
+    G = add_variation_device(G, 0.1, seed=seed)
+    v = torch.from_numpy((rng.random((n_vec, n_tiles, n)) * V_READ).astype(np.float32)).cuda()
+    params = [1e6, 2e6, 2.0, 1.0 / (2.0 * 1e6), 2.0, 1.0 / (2.0 * 2e6)]
+    kw = dict(g_wire=1 / R_WIRE, nonlinear_cell_enable=True, nonlinear_params=params, method="line",
+              read_noise_sigma=0.01, noise_seed=seed)
+    _, st, _ = acc.ir_drop_gs_ex(v, G, n_vec, n, n, n_tiles, 1, **kw)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    acc.ir_drop_gs_ex(v, G, n_vec, n, n, n_tiles, 1, return_stats=False, **kw)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"workload": "%d tiles 512x512 (16-CTA clusters) x %d vectors U[0,0.2] V, sinh cells a=2, "
+                        "lognormal sigma 0.1, 1%% read noise" % (n_tiles, n_vec),
+            "solves": n_tiles * n_vec, "ms": ms, "solves_per_s": n_tiles * n_vec / (ms / 1e3),
+            "node_updates_per_s": n_tiles * n_vec * 2 * n * n * st["iters_sum"] / st["solves"] / (ms / 1e3),
+            "line_iters_mean": st["iters_sum"] / st["solves"], "status_or": st["status_or"]}
+
+
 def check_accuracy(acc, G, vin, torch):
     """A seeded sample of solves against the FP64 oracle (both planes)."""
     from oracle import nodal
@@ -307,6 +336,11 @@ def run_ours(args):
 
     # the mixed-size batch (tiles of 64, 128 and 256)
     mixed = mixed_batch(torch) if not args.no_mixed else None
+    large = large_nonideal(torch, acc) if not args.no_mixed else None
+    warm = None
+    if not args.no_warm:
+        from fadesim_gb300.warmstart_eval import train_and_evaluate
+        warm = train_and_evaluate(size=ROWS, steps=600, batch=32, infer=8192)
 
     # the plain red-black SOR kernel on a bounded sample of the same workload
     nps = 256
@@ -341,7 +375,7 @@ def run_ours(args):
                    "plain_rbsor_solves_per_s": rb_value,
                    "plain_rbsor_sweeps_mean": rb_stats["iters_sum"] / max(1, rb_stats["solves"]),
                    "speedup_vs_plain_rbsor": value / world / rb_value, **variants,
-                   "mixed_sizes": mixed},
+                   "mixed_sizes": mixed, "large_nonideal": large, "learned_warm_start": warm},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "traffic": traffic * solves_per_step if traffic else None,
@@ -366,7 +400,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tiles", type=int, default=N_TILES, help="128x128 tiles per rank (64 vectors each)")
-    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-size (64/128/256) batch figure")
+    ap.add_argument("--no-mixed", action="store_true",
+                    help="skip the mixed-size (64/128/256) and large non-ideal (512) figures")
+    ap.add_argument("--no-warm", action="store_true", help="skip training/evaluating the learned warm start")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident solve only (no e2e, comparator or CPU baseline); for profiling")
     args = ap.parse_args()

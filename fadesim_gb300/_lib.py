@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libfadesim_gb300.so")
 F32 = 0
 F64 = 1
 METHOD_AUTO, METHOD_LINE, METHOD_RBSOR, METHOD_SWEEPS = 0, 1, 2, 3
-ST_CONVERGED, ST_MAXITER, ST_NONFINITE = 1, 2, 4
+ST_CONVERGED, ST_MAXITER, ST_NONFINITE, ST_WARM_REJECTED = 1, 2, 4, 8
 
 
 class SolveOpts(ctypes.Structure):
@@ -38,6 +38,8 @@ EXPORTS = {
     "fadesim_ir_drop_gs_f64": [_vp, _vp, _i, _i, _i, _i, _i, _i, _d, _d, _i, _d, _i, _vp, _i, _i, _vp, _vp],
     "fadesim_ir_drop_gs_ex": [_i, _vp, _vp, _i, _i, _i, _i, _i, _i, _d, _d, _i, _d, _i, _vp, _i, _i, _vp,
                               ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _vp, _vp],
+    "fadesim_ir_drop_gs_warm": [_i, _vp, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp, ctypes.POINTER(SolveOpts),
+                                ctypes.POINTER(SolveStats), _vp, _vp],
     "fadesim_last_error": [],
     "fadesim_version": [],
     "fadesim_ir_drop_gs_noalloc_f32": [_vp, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp],

@@ -166,3 +166,35 @@ ir2s_ou_local = _not_here("ir2s_ou_local", "split_arr_matmul.cu:565")
 ir2s_ou = _not_here("ir2s_ou", "split_arr_matmul.cu:953")
 ir_gs_ou_local = _not_here("ir_gs_ou_local", "split_arr_matmul.cu:690")
 ir_gs_ou = _not_here("ir_gs_ou", "split_arr_matmul.cu:1197")
+
+
+def ir_drop_gs_warm(input, G, batch_size, row_size, col_size, numX, numY, init, g_wire=1 / 2.93, tol_v=None,
+                    residual=None, return_iters=False, method="line", omega=None):
+    """Line solve from given initial planes ``init`` [batch, numX, numY, 2, rows, cols]
+    (FP32 wordline deviations u - vin and bitline voltages d, e.g. a learned
+    prediction).  Returns (currents, stats, iters)."""
+    _check_input(input, "input")
+    _check_input(G, "G")
+    _check_input(init, "init")
+    if init.dtype != torch.float32 or init.numel() != batch_size * numX * numY * 2 * row_size * col_size:
+        raise RuntimeError("init must be float32 [batch, numX, numY, 2, rows, cols]")
+    o = SolverOptions(**{k: v for k, v in vars(options).items()})
+    if tol_v is not None:
+        o.tol_v = tol_v
+    if residual is not None:
+        o.residual = residual
+    if omega is not None:
+        o.omega = omega
+    out = torch.empty((batch_size, numX, numY * col_size), dtype=input.dtype, device=input.device)
+    iters = torch.empty((batch_size, numX, numY), dtype=torch.int32, device=input.device) if return_iters else None
+    st = _lib.SolveStats()
+    lib = _lib.load()
+    with torch.cuda.device(input.device):
+        rc = lib.fadesim_ir_drop_gs_warm(_lib.F64 if input.dtype == torch.float64 else _lib.F32, input.data_ptr(),
+                                         G.data_ptr(), batch_size, row_size, col_size, numX, numY, float(g_wire),
+                                         init.data_ptr(), out.data_ptr(), ctypes.byref(o.to_c(method)),
+                                         ctypes.byref(st), iters.data_ptr() if return_iters else None,
+                                         torch.cuda.current_stream(input.device).cuda_stream)
+    _lib.check(rc)
+    return out, dict(solves=int(st.solves), iters_sum=int(st.iters_sum), iters_max=int(st.iters_max),
+                     status_or=int(st.status_or)), iters

@@ -187,6 +187,8 @@ int run_sweeps(int dtype, SolveArgs a, int iter_times, double gw, double beta, i
 
 }  // namespace
 
+static thread_local const float *g_warm_init = nullptr;
+
 extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G, int batch_size, int row_size,
                                      int col_size, int numX, int numY, int iter_times, double g_wire, double beta,
                                      int enable_break, double break_threshould, int nonlinear_cell_enable,
@@ -226,6 +228,9 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
     a.gw = (float)g_wire;
     a.ret_V = ret_V == 2 ? 2 : (ret_V ? 1 : 0);
     a.iters_out = per_solve_iters;
+    a.init = g_warm_init;
+    if (a.init && (ret_V == 1 || !line_relax_ld(row_size, col_size)))
+        return fail(FADESIM_E_UNSUPPORTED, "warm starts apply to tiles up to 128 x 128");
     if (nonlinear_cell_enable) {
         const double *q = nonlinear_params;
         a.ctl.nl = 1;
@@ -278,4 +283,20 @@ extern "C" int fadesim_ir_drop_gs_f64(const double *input, const double *G, int 
     return fadesim_ir_drop_gs_ex(FADESIM_F64, input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire,
                                  beta, enable_break, break_threshould, nonlinear_cell_enable, nonlinear_params,
                                  n_nonlinear_params, ret_V, out, nullptr, nullptr, nullptr, stream);
+}
+
+extern "C" int fadesim_ir_drop_gs_warm(int dtype, const void *input, const void *G, int batch_size, int row_size,
+                                       int col_size, int numX, int numY, double g_wire, const float *init, void *out,
+                                       const fadesim_solve_opts *opts, fadesim_solve_stats *stats,
+                                       int *per_solve_iters, void *stream) {
+    if (!init) return fail(FADESIM_E_ARG, "init planes required");
+    fadesim_solve_opts o = opts ? *opts : fadesim_solve_opts{};
+    if (o.method == FADESIM_METHOD_AUTO) o.method = FADESIM_METHOD_LINE;
+    if (o.method != FADESIM_METHOD_LINE && o.method != FADESIM_METHOD_RBSOR)
+        return fail(FADESIM_E_UNSUPPORTED, "warm starts apply to the line and red-black SOR methods");
+    g_warm_init = init;
+    const int rc = fadesim_ir_drop_gs_ex(dtype, input, G, batch_size, row_size, col_size, numX, numY, 0, g_wire, 1.0,
+                                         0, 0.0, 0, nullptr, 0, 0, out, &o, stats, per_solve_iters, stream);
+    g_warm_init = nullptr;
+    return rc;
 }

@@ -22,6 +22,7 @@ struct SolveArgs {
     float *scratch;     // per-CTA scratch (kernel specific)
     int *iters_out;     // optional [B, numX, numY]
     DevStats *stats;    // optional
+    const float *init;  // optional warm start: deviation planes [B, numX, numY, 2, n, m] (u - vin, d)
 };
 
 // Block line relaxation, planes resident in shared memory (n, m <= 128).

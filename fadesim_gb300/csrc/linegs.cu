@@ -312,6 +312,17 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             }
             if (tid < LD) vin_s[vpad(tid)] = (tid < n) ? (float)inp[((size_t)b * a.numX + x) * n + tid] : 0.f;
             __syncthreads();
+            // warm start: initial deviation planes [2][n][m] of this solve
+            bool warm = a.init != nullptr;
+            if (warm) {
+                const float *w0 = a.init + (((size_t)b * a.numX + x) * a.numY + y) * 2 * n * m;
+                for (int e = tid; e < n * m; e += T) {
+                    const int i = e / m, j = e - i * m;
+                    U[swz<LD>(i, j)] = w0[e];
+                    D[swz<LD>(i, j)] = w0[(size_t)n * m + e];
+                }
+                __syncthreads();
+            }
             LineStop stop;
             stop.init(a.ctl.omega);
             float omega = stop.omega;
@@ -340,8 +351,24 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 par ^= 1;
                 ++it;
                 if (!isfinite(delta) || !isfinite(vm)) {
-                    status = FADESIM_ST_NONFINITE;
+                    status |= FADESIM_ST_NONFINITE;
                     break;
+                }
+                if (warm && it == 1 && !(delta < vm)) {
+                    // the prediction moved as much as the solution is large: discard
+                    // it and start again from the ideal state
+                    __syncthreads();
+                    for (int e = tid; e < LD * LD; e += T) {
+                        U[e] = 0.f;
+                        D[e] = 0.f;
+                    }
+                    __syncthreads();
+                    warm = false;
+                    status |= FADESIM_ST_WARM_REJECTED;
+                    stop.init(a.ctl.omega);
+                    omega = stop.omega;
+                    res64 = precise_first;
+                    continue;
                 }
                 const bool small = stop.update(delta, vm, tol);
                 omega = stop.omega;
@@ -349,7 +376,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     // the final test must pass on an iteration whose residual was
                     // FP64 (kres < 0: FP32 only, the FP32 test is final)
                     if (res64 || kres < 0) {
-                        status = FADESIM_ST_CONVERGED;
+                        status |= FADESIM_ST_CONVERGED;
                         break;
                     }
                     res64 = true;
@@ -357,7 +384,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     res64 = (kres > 0) && (it % kres == 0);
                 }
                 if (it >= maxit) {
-                    status = FADESIM_ST_MAXITER;
+                    status |= FADESIM_ST_MAXITER;
                     break;
                 }
             }

@@ -67,6 +67,15 @@ __global__ void __launch_bounds__(RB_THREADS, 1) rbsor_kernel(SolveArgs a) {
                 D[e] = 0.f;
             }
             if (tid < n) vin_s[tid] = (float)inp[((size_t)b * a.numX + x) * n + tid];
+            if (a.init) {
+                // warm start: initial deviation planes [2][n][m] of this solve
+                const float *w0 = a.init + (((size_t)b * a.numX + x) * a.numY + y) * 2 * n * m;
+                for (int e = tid; e < n * m; e += RB_THREADS) {
+                    const int i = e / m, j = e - i * m;
+                    U[i * LDP + j] = w0[e];
+                    D[i * LDP + j] = w0[(size_t)n * m + e];
+                }
+            }
             __syncthreads();
             float prev_check = 0.f;
             int sweeps = 0, status = 0, par = 0;

@@ -44,6 +44,7 @@ extern "C" {
 #define FADESIM_ST_CONVERGED 1
 #define FADESIM_ST_MAXITER 2
 #define FADESIM_ST_NONFINITE 4
+#define FADESIM_ST_WARM_REJECTED 8  /* the warm start was discarded and the solve restarted from zero */
 
 typedef struct fadesim_solve_opts {
     int method;            /* FADESIM_METHOD_* */
@@ -142,6 +143,17 @@ int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G, int batch
                                    int numX, int numY, double g_wire, float *out, void *stream);
 size_t fadesim_noalloc_scratch_bytes(void);
 const char *fadesim_noalloc_last_error(void);
+
+/* fadesim_ir_drop_gs_ex started from given node planes (a learned warm start): init is a DEVICE
+ * FP32 array [batch, numX, numY, 2, rows, cols] of wordline deviations u - vin and bitline voltages
+ * d.  The line method (rows, cols <= 128) iterates from them to the same tolerance; a prediction
+ * whose first correction is as large as the solution is discarded (FADESIM_ST_WARM_REJECTED) and
+ * the solve restarts from the ideal state.  opts->method FADESIM_METHOD_RBSOR starts the plain
+ * red-black SOR from the planes instead (the comparator the learned start is measured against). */
+int fadesim_ir_drop_gs_warm(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
+                            int numX, int numY, double g_wire, const float *init, void *out,
+                            const fadesim_solve_opts *opts, fadesim_solve_stats *stats, int *per_solve_iters,
+                            void *stream);
 
 /* Message for the last failing call on this thread. */
 const char *fadesim_last_error(void);
