@@ -155,6 +155,41 @@ int fadesim_ir_drop_gs_warm(int dtype, const void *input, const void *G, int bat
                             const fadesim_solve_opts *opts, fadesim_solve_stats *stats, int *per_solve_iters,
                             void *stream);
 
+/* ---- kernels of the learned warm-start network (no reference counterpart; the
+ * reference's learned-solver precedent is its SCN/fcm training path, which
+ * this path does not drop in for).  Device pointers, async on stream, return
+ * FADESIM_OK, FADESIM_E_ARG or FADESIM_E_CUDA.  Activations are NHWC bf16 with
+ * channels a multiple of 16; weights [Cout][3][3][Cin] bf16 with Cout a
+ * multiple of 8 and at most 128; "same" zero padding. ---- */
+
+/* Y = act(conv3x3(X, W) + bias) (+ skip): flags 1 = ReLU, 2 = add skip after
+ * the activation, 4 = store FP32 instead of bf16. */
+int fadesim_conv3x3_fwd_bf16(const void *X, const void *W, const float *bias, const void *skip, void *Y, int N,
+                             int H, int Wd, int Cin, int Cout, int flags, void *stream);
+/* dW[Cout][3][3][Cin] += sum over pixels of dY x X (FP32 accumulation with atomics: zero dW first). */
+int fadesim_conv3x3_wgrad_bf16(const void *dY, const void *X, float *dW, int N, int H, int Wd, int Cin, int Cout,
+                               void *stream);
+/* Wf[ci][8 - tap][co] = W[co][tap][ci], ci padded to Cin_pad8: the weights of the input-gradient convolution. */
+int fadesim_weight_flip_bf16(const void *W, void *Wf, int Cin, int Cout, int Cin_pad8, void *stream);
+/* db[c] += sum over P pixels of dY[p, c]. */
+int fadesim_bias_grad_bf16(const void *dY, float *db, long long P, int C, void *stream);
+/* 2x2 average pool (upsample = 0) or nearest 2x upsample (upsample = 1), or their gradients
+ * (backward = 1).  H, W are the full-resolution side's size for the pool and the low-resolution
+ * side's for the upsample, in both directions. */
+int fadesim_pool_bf16(const void *X, void *Y, int N, int H, int W, int C, int backward, int upsample, void *stream);
+/* dZ = dY where Yact > 0, else 0. */
+int fadesim_relu_bwd_bf16(const void *dY, const void *Yact, void *dZ, long long n, void *stream);
+/* C = A + B (bf16). */
+int fadesim_add_bf16(const void *A, const void *B, void *C, long long n, void *stream);
+/* Mean squared error of the first Cv of Cp FP32 prediction channels [P, Cp] against target [P, Cv]:
+ * loss (FP32, accumulated: zero it first) and the bf16 gradient dpred [P, Cp] (0 past Cv). */
+int fadesim_mse_f32(const float *pred, const float *target, void *dpred, float *loss, long long P, int Cp, int Cv,
+                    void *stream);
+/* One Adam step (bias-corrected, step >= 1) on FP32 master weights w with moments m, v; refreshes the
+ * bf16 copy wb. */
+int fadesim_adam_f32(float *w, void *wb, const float *g, float *m, float *v, long long n, float lr, float b1,
+                     float b2, float eps, int step, void *stream);
+
 /* Message for the last failing call on this thread. */
 const char *fadesim_last_error(void);
 
