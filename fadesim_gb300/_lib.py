@@ -48,6 +48,10 @@ EXPORTS = {
     "fadesim_map_conductance_f32": [_vp, _i, _i, _i, _i, _i, _i, _i, _i, _i, ctypes.c_float, ctypes.c_float, _vp, _vp],
     "fadesim_adc_shift_add_f32": [_vp, _i, _i, _i, _i, _i, _i, ctypes.c_float, ctypes.c_float, ctypes.c_float, _i, _i,
                                   _i, _i, _i, _vp, _vp],
+    "fadesim_slice_inputs_im2col_f32": [_vp] + [_i] * 19 + [ctypes.c_float, _vp, _vp],
+    "fadesim_map_conductance_ref_f32": [_vp] + [_i] * 10 + [ctypes.c_float, ctypes.c_float, _vp, _vp],
+    "fadesim_adc_shift_add_ex_f32": [_vp] + [_i] * 7 + [ctypes.c_float] * 3 + [_i] * 5 + [ctypes.c_float, _vp, _i,
+                                                                                         _vp, _vp],
     "fadesim_noalloc_scratch_bytes": [],
     "fadesim_noalloc_last_error": [],
 }

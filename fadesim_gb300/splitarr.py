@@ -1,16 +1,20 @@
-"""PimTorch's bit-sliced crossbar matmul and ``Linear_sp`` layer on the GPU.
+"""PimTorch's bit-sliced crossbar matmul and its ``Linear_sp`` / ``Conv2d_sp``
+layers on the GPU.
 
 Mirrors ``splitArr_matmul_nn`` (pimtorch/pimfixedpoint/fixedPoint/nn/
-splitArrayArithmetic.py:1161-1228) and the PN, whole-array branch of ``matmul``
-(:442-1018) for the default PimTorch settings -- PN weight arrays, complement-
-code inputs, 1-bit DAC, no OU, no BNN, no compensation -- and
-``Linear_sp.forward`` (fixedPoint/nn/modules/linear_split.py:53-78).  The
-integer stages (quantisation, PN split, bit slicing, conductance mapping, ADC,
-shift-add) run in the CUDA kernels of ``libfadesim_gb300.so`` and are bit-exact
-with the reference's float32 arithmetic given the same currents; the currents
-come from the IR-drop solve (``cpp_ir_drop_accelerate.ir_drop_gs`` unless a
-``solver`` is passed).  The solves of one (weight slice, array) pair cover all
-input-bit cycles at once: the input bits are stacked on the batch.
+splitArrayArithmetic.py:1161-1260) and the whole-array branch of ``matmul``
+(:442-1018) -- PN or Ref-column weight arrays, complement-code or
+negative-pulse inputs, no OU, no BNN, no compensation -- with
+``Linear_sp.forward`` (fixedPoint/nn/modules/linear_split.py:53-78) and
+``Conv2d_sp.forward`` (fixedPoint/nn/modules/conv_split.py:89-136) on top.  The
+integer stages (quantisation, PN split or Ref offset, bit slicing with the
+convolution's unfold done by addressing, conductance mapping, ADC,
+reference-column subtraction, shift-add, bias, fold) run in the CUDA kernels
+of ``libfadesim_gb300.so`` and are bit-exact with the reference's float32
+arithmetic given the same currents; the currents come from the IR-drop solve
+(``cpp_ir_drop_accelerate.ir_drop_gs`` unless a ``solver`` is passed).  The
+solves of one (weight slice, array) pair cover all input-bit cycles at once:
+the input bits are stacked on the batch.
 
 Array and device parameters come from an object with ``phyArrParams``'s
 attribute names, so the reference's own ``commonConst.phyArrParams`` can be
@@ -19,6 +23,7 @@ passed unchanged; ``ArrayConfig`` holds the same defaults.
 import math
 from dataclasses import dataclass, field
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -43,6 +48,7 @@ class ArrayConfig:
     ir_drop_less_than_threshold: float = 1e-7
     nonlinear_cell_enable: bool = False
     nonlinear_params: list = field(default_factory=list)
+    inputVmode: str = "complement_code"   # or "neg_pulse" (commonConst.py:170-172,224)
 
     @property
     def cellMaxConduct(self):
@@ -95,60 +101,164 @@ def default_solver(cfg):
     return solve
 
 
-def splitArr_matmul_nn(input, w, inputBits, dacBits, adcBits, outputBits, weightBits, arrType="PN",
-                       float_type=torch.float32, cfg=None, solver=None):
-    """Same arguments as the reference; ``arrType`` is "PN" or an enum whose name is
-    "PN"; ``cfg`` is a phyArrParams-like object (default ``ArrayConfig()``);
-    ``solver(v, G, B, rows, cols, numX, numY, out)`` may replace the IR-drop solve."""
-    cfg = cfg if cfg is not None else ArrayConfig()
-    name = getattr(arrType, "name", arrType)
-    if name != "PN":
-        raise NotImplementedError("only the PN array mode is implemented (Ref mode is not)")
-    if float_type != torch.float32:
-        raise NotImplementedError("the integer-stage kernels are float32, as Linear_sp's default fp_type")
-    if dacBits != 1:
+def _mode_name(v, default):
+    v = default if v is None else v
+    return getattr(v, "name", v)
+
+
+def _check_modes(arr, in_mode, dacBits, cfg):
+    if arr not in ("PN", "Ref"):
+        raise NotImplementedError("array mode %r (PN and Ref are implemented)" % (arr,))
+    if in_mode not in ("complement_code", "neg_pulse"):
+        raise NotImplementedError("input mode %r" % (in_mode,))
+    if in_mode == "complement_code" and dacBits != 1:
         raise Exception("[Error] Complement code input mode, but dac is not 1 bit. dacbits = {}".format(dacBits))
     if getattr(cfg, "useOUSize", False) or getattr(cfg, "useBNN", False):
         raise NotImplementedError("OU and BNN modes are not implemented")
     if getattr(cfg, "sigma", 0) != 0:
         raise NotImplementedError("conductance variation: use fadesim_gb300.variation on the maps")
+
+
+def _split_matmul_core(xq, geom, M, insize, has_ones, ones_q, s1, w, inputBits, dacBits, adcBits, weightBits, arr,
+                       neg_pulse, cfg, solver, bias=None, L=0):
+    """The bit-serial, bit-sliced product of splitArr_matmul_nn from quantised
+    inputs: xq is an int32 NCHW image (geom = N, C, H, W, kh, kw, sh, sw, ph,
+    pw, dh, dw; a linear layer is the 1x1 case) whose unfold has M rows and
+    insize columns (plus a ones column if has_ones); w [insize(+1), outsize]
+    float weights.  Returns float32 [M, outsize], or [M/L, outsize, L] if L."""
+    lib = _lib.load()
     if weightBits % cfg.cellBits != 0:
         raise Exception("[Error] cellbit is not factor of weight_bit")
-    lib = _lib.load()
     solver = solver or default_solver(cfg)
+    dev = xq.device
+    K = insize + (1 if has_ones else 0)
+    outsize = w.shape[1]
+    rows, cols = cfg.arrRowSize, cfg.arrColSize
+    numX = -(-K // rows)
+    numY = -(-outsize // cols)
+    nbits = len(range(0, inputBits, dacBits))
+    nslices = len(range(0, weightBits, cfg.cellBits))
+    inputV = cfg.inputMaxVoltage / (2 ** dacBits - 1)
+    st = _stream()
+    v = torch.empty((nbits * M, numX, rows), dtype=torch.float32, device=dev)
+    _lib.check(lib.fadesim_slice_inputs_im2col_f32(xq.data_ptr(), *geom, int(bool(has_ones)), int(ones_q), rows, numX,
+                                                   nbits, dacBits, int(bool(neg_pulse)), inputV, v.data_ptr(), st))
+    ref = arr == "Ref"
+    wq, s2 = quantize(w, weightBits, pn=not ref)
+    cb = cols + 2 if ref else cols
+    narr = 1 if ref else 2
+    I = torch.empty((nslices, narr, nbits * M, numX, numY * cb), dtype=torch.float32, device=dev)
+    G = torch.empty((numX, rows, numY * cb), dtype=torch.float32, device=dev)
+    plus = 2 ** (weightBits - 1)
+    for j in range(nslices):
+        for a in range(narr):
+            if ref:
+                _lib.check(lib.fadesim_map_conductance_ref_f32(wq.data_ptr(), K, outsize, rows, cols, numX, numY,
+                                                               j * cfg.cellBits, cfg.cellBits, plus,
+                                                               2 ** weightBits - 1, cfg.cellDeltaConduct,
+                                                               cfg.cellMinConduct, G.data_ptr(), st))
+            else:
+                _lib.check(lib.fadesim_map_conductance_f32(wq.data_ptr(), K, outsize, rows, cols, numX, numY,
+                                                           j * cfg.cellBits, cfg.cellBits, a, cfg.cellDeltaConduct,
+                                                           cfg.cellMinConduct, G.data_ptr(), st))
+            r = solver(v, G, nbits * M, rows, cb, numX, numY, I[j, a])
+            if r is not None and r.data_ptr() != I[j, a].data_ptr():
+                I[j, a].copy_(r.reshape(I[j, a].shape))
+    shape = (M // L, outsize, L) if L else (M, outsize)
+    out = torch.empty(shape, dtype=torch.float32, device=dev)
+    scale = rows * (2 ** dacBits - 1) * (2 ** cfg.cellBits - 1) / (2 ** adcBits - 1)
+    b = None
+    if bias is not None:
+        b = bias.detach().to(device=dev, dtype=torch.float32).contiguous()
+    _lib.check(lib.fadesim_adc_shift_add_ex_f32(I.data_ptr(), cols if ref else 0, nbits, nslices, M, numX, numY * cb,
+                                                outsize, cfg.adcUseI, float(2 ** adcBits - 1), scale, s1 + s2,
+                                                dacBits, cfg.cellBits, inputBits, 0 if neg_pulse else 1,
+                                                float(plus), b.data_ptr() if b is not None else None, int(L),
+                                                out.data_ptr(), st))
+    return out
+
+
+def splitArr_matmul_nn(input, w, inputBits, dacBits, adcBits, outputBits, weightBits, arrType="PN",
+                       float_type=torch.float32, cfg=None, solver=None):
+    """Same arguments as the reference; ``arrType`` is "PN" / "Ref" or an enum
+    with that name; ``cfg`` is a phyArrParams-like object (default
+    ``ArrayConfig()``; its ``inputVmode`` selects complement-code or
+    negative-pulse inputs); ``solver(v, G, B, rows, cols, numX, numY, out)`` may
+    replace the IR-drop solve."""
+    cfg = cfg if cfg is not None else ArrayConfig()
+    arr = _mode_name(arrType, "PN")
+    in_mode = _mode_name(getattr(cfg, "inputVmode", None), "complement_code")
+    _check_modes(arr, in_mode, dacBits, cfg)
+    if float_type != torch.float32:
+        raise NotImplementedError("the integer-stage kernels are float32, as Linear_sp's default fp_type")
     with torch.no_grad():
         x = input.to(device="cuda", dtype=torch.float32).contiguous()
         w = w.to(device=x.device, dtype=torch.float32).contiguous()
         B, insize = x.shape
-        outsize = w.shape[1]
         xq, s1 = quantize(x, inputBits, pn=False)
-        wq, s2 = quantize(w, weightBits, pn=True)
-        rows, cols = cfg.arrRowSize, cfg.arrColSize
-        numX = -(-insize // rows)
-        numY = -(-outsize // cols)
-        nbits = len(range(0, inputBits, dacBits))
-        nslices = len(range(0, weightBits, cfg.cellBits))
-        inputV = cfg.inputMaxVoltage / (2 ** dacBits - 1)
-        st = _stream()
-        v = torch.empty((nbits * B, numX, rows), dtype=torch.float32, device=x.device)
-        _lib.check(lib.fadesim_slice_inputs_f32(xq.data_ptr(), B, insize, rows, numX, nbits, dacBits, inputV,
-                                                v.data_ptr(), st))
-        I = torch.empty((nslices, 2, nbits * B, numX, numY * cols), dtype=torch.float32, device=x.device)
-        G = torch.empty((numX, rows, numY * cols), dtype=torch.float32, device=x.device)
-        for j in range(nslices):
-            for pn in (0, 1):
-                _lib.check(lib.fadesim_map_conductance_f32(wq.data_ptr(), insize, outsize, rows, cols, numX, numY,
-                                                           j * cfg.cellBits, cfg.cellBits, pn, cfg.cellDeltaConduct,
-                                                           cfg.cellMinConduct, G.data_ptr(), st))
-                r = solver(v, G, nbits * B, rows, cols, numX, numY, I[j, pn])
-                if r is not None and r.data_ptr() != I[j, pn].data_ptr():
-                    I[j, pn].copy_(r.reshape(I[j, pn].shape))
-        out = torch.empty((B, outsize), dtype=torch.float32, device=x.device)
-        scale = rows * (2 ** dacBits - 1) * (2 ** cfg.cellBits - 1) / (2 ** adcBits - 1)
-        _lib.check(lib.fadesim_adc_shift_add_f32(I.data_ptr(), nbits, nslices, B, numX, numY * cols, outsize,
-                                                 cfg.adcUseI, float(2 ** adcBits - 1), scale, s1 + s2, dacBits,
-                                                 cfg.cellBits, inputBits, 1, out.data_ptr(), st))
-        return out
+        geom = (B, insize, 1, 1, 1, 1, 1, 1, 0, 0, 1, 1)
+        return _split_matmul_core(xq, geom, B, insize, False, 0, s1, w, inputBits, dacBits, adcBits, weightBits, arr,
+                                  in_mode == "neg_pulse", cfg, solver)
+
+
+def _covered(n, k, s, p, d, on):
+    """Which of n input positions an unfold with kernel k, stride s, padding p,
+    dilation d and on outputs reads."""
+    cov = np.zeros(n, dtype=bool)
+    for o in range(on):
+        for t in range(k):
+            h = o * s - p + t * d
+            if 0 <= h < n:
+                cov[h] = True
+    return cov
+
+
+def conv2d_split(input, weight, bias, stride=1, padding=0, dilation=1, inputBits=8, dacBits=1, adcBits=10,
+                 outputBits=10, weightBits=8, arrType="PN", use_fp_bias=True, cfg=None, solver=None):
+    """Conv2d_sp's evaluation (fixedPoint/nn/modules/conv_split.py:89-136):
+    unfold, splitArr_matmul_nn against the weights reshaped [Cout, C*kh*kw] and
+    transposed, float32 bias (or a bias row in the array driven by ones when
+    ``use_fp_bias`` is False), fold to [N, Cout, OH, OW].  The unfold is done by
+    addressing inside the slicing kernel and the fold by the output layout of
+    the shift-add kernel; results equal the reference's bit for bit given the
+    same currents.  Zero padding only, groups 1."""
+    cfg = cfg if cfg is not None else ArrayConfig()
+    arr = _mode_name(arrType, "PN")
+    in_mode = _mode_name(getattr(cfg, "inputVmode", None), "complement_code")
+    _check_modes(arr, in_mode, dacBits, cfg)
+    pair = lambda t: tuple(t) if isinstance(t, (tuple, list)) else (t, t)
+    (sh, sw), (ph, pw), (dh, dw) = pair(stride), pair(padding), pair(dilation)
+    with torch.no_grad():
+        x = input.to(device="cuda", dtype=torch.float32).contiguous()
+        wt = weight.to(device=x.device, dtype=torch.float32)
+        N, C, H, W = x.shape
+        Cout, Cw, kh, kw = wt.shape
+        if Cw != C:
+            raise NotImplementedError("grouped convolutions are not supported by Conv2d_sp's evaluation path")
+        OH = (H + 2 * ph - dh * (kh - 1) - 1) // sh + 1
+        OW = (W + 2 * pw - dw * (kw - 1) - 1) // sw + 1
+        if OH < 1 or OW < 1:
+            raise RuntimeError("input too small for the kernel")
+        ones = bias is not None and not use_fp_bias
+        rmask = torch.from_numpy(_covered(H, kh, sh, ph, dh, OH)).to(x.device)
+        cmask = torch.from_numpy(_covered(W, kw, sw, pw, dw, OW)).to(x.device)
+        max_abs = float(x[:, :, rmask][:, :, :, cmask].abs().max().item()) if N else 0.0
+        if ones:
+            max_abs = max(max_abs, 1.0)
+        s1 = _fixed_point_position(max_abs, inputBits, False)
+        xq = torch.empty(x.shape, dtype=torch.int32, device=x.device)
+        lib = _lib.load()
+        _lib.check(lib.fadesim_quantize_f32(x.data_ptr(), x.numel(), s1, xq.data_ptr(), _stream()))
+        ones_q = int(np.rint(np.float32(1.0) / np.float32(2.0 ** s1))) if ones else 0
+        wm = wt.reshape(Cout, -1).t()
+        if ones:
+            wm = torch.cat((wm, bias.detach().to(wm).reshape(1, -1)), 0)
+        geom = (N, C, H, W, kh, kw, sh, sw, ph, pw, dh, dw)
+        L = OH * OW
+        out = _split_matmul_core(xq, geom, N * L, C * kh * kw, ones, ones_q, s1, wm.contiguous(), inputBits, dacBits,
+                                 adcBits, weightBits, arr, in_mode == "neg_pulse", cfg, solver,
+                                 bias=bias if (bias is not None and use_fp_bias) else None, L=L)
+        return out.reshape(N, Cout, OH, OW)
 
 
 class Linear_sp(torch.nn.Module):
@@ -182,3 +292,53 @@ class Linear_sp(torch.nn.Module):
         if self.hasBias and self.useFpBias:
             out = out + self.fp_bias.to(out.device)
         return out
+
+
+class Conv2d_sp(torch.nn.Module):
+    """Conv2d_sp (fixedPoint/nn/modules/conv_split.py:29-136): float training,
+    crossbar-simulated evaluation through ``conv2d_split``.  Zero padding and
+    groups = 1 in evaluation, as the reference's unfold path supports."""
+
+    def __init__(self, in_channels, out_channels, kernel_size, stride=1, padding=0, dilation=1, groups=1, bias=True,
+                 padding_mode="zeros", input_bit_width=8, output_bit_width=10, weight_bit_width=8, dac_bit_width=1,
+                 adc_bit_width=10, phy_arr_mode="PN", fp_type=torch.float32, use_fp_bias=True, cfg=None, solver=None):
+        super().__init__()
+        if groups <= 0:
+            raise ValueError("groups must be a positive integer")
+        if in_channels % groups != 0:
+            raise ValueError("in_channels must be divisible by groups")
+        if out_channels % groups != 0:
+            raise ValueError("out_channels must be divisible by groups")
+        pair = lambda t: tuple(t) if isinstance(t, (tuple, list)) else (t, t)
+        self.in_channels, self.out_channels = in_channels, out_channels
+        self.kernel_size, self.stride = pair(kernel_size), pair(stride)
+        self.padding, self.dilation = pair(padding), pair(dilation)
+        self.groups, self.padding_mode = groups, padding_mode
+        self.hasBias, self.useFpBias = bias, use_fp_bias
+        self.inputBits, self.outputBits, self.weightBits = input_bit_width, output_bit_width, weight_bit_width
+        self.adcBits, self.dacBits = adc_bit_width, dac_bit_width
+        self.phyArrMode, self.fp_type = phy_arr_mode, fp_type
+        self.cfg, self.solver = cfg, solver
+        self.fp_weight = torch.nn.Parameter(torch.empty((out_channels, in_channels // groups, *self.kernel_size),
+                                                        dtype=fp_type))
+        self.fp_bias = torch.nn.Parameter(torch.empty(out_channels, dtype=fp_type)) if bias else None
+        torch.nn.init.kaiming_uniform_(self.fp_weight, a=math.sqrt(5))
+        if self.fp_bias is not None:
+            fan_in = self.fp_weight[0].numel()
+            bound = 1 / math.sqrt(fan_in) if fan_in else 0
+            torch.nn.init.uniform_(self.fp_bias, -bound, bound)
+
+    def forward(self, input):
+        if self.training:
+            if self.padding_mode != "zeros":
+                pad = (self.padding[1], self.padding[1], self.padding[0], self.padding[0])
+                return torch.nn.functional.conv2d(torch.nn.functional.pad(input, pad, mode=self.padding_mode),
+                                                  self.fp_weight, self.fp_bias, self.stride, 0, self.dilation,
+                                                  self.groups)
+            return torch.nn.functional.conv2d(input, self.fp_weight, self.fp_bias, self.stride, self.padding,
+                                              self.dilation, self.groups)
+        if self.groups != 1 or self.padding_mode != "zeros":
+            raise NotImplementedError("crossbar evaluation supports groups=1 and zero padding")
+        return conv2d_split(input, self.fp_weight, self.fp_bias if self.hasBias else None, self.stride, self.padding,
+                            self.dilation, self.inputBits, self.dacBits, self.adcBits, self.outputBits,
+                            self.weightBits, self.phyArrMode, self.useFpBias, cfg=self.cfg, solver=self.solver)

@@ -127,6 +127,37 @@ int fadesim_adc_shift_add_f32(const float *I, int nbits, int nslices, int B, int
                               float adcUseI, float levels, float scale, int s12, int dac_bits, int cell_bits,
                               int input_bits, int complement, float *out, void *stream);
 
+/* Input voltages of a convolution (or, as the 1x1 case N = batch, C = in_features, H = W = 1, of a
+ * linear layer) straight from the NCHW int32 quantised image, the unfold done by addressing
+ * (torch.nn.functional.unfold as Conv2d_sp calls it, fixedPoint/nn/modules/conv_split.py:106-107):
+ * matrix row p = (n, oh, ow), column k = (ch, ki, kj), then a column of ones_q when has_ones (a
+ * bias mapped into the array, conv_split.py:113-115), then zeros to numX*rows.
+ * v[bit*M + p, x, r] = level * inputV with M = N*OH*OW and level = (q >> bit*dac_bits) & mask, or
+ * -((|q| >> bit*dac_bits) & mask) for a negative q when neg_pulse != 0 (negative-pulse input mode,
+ * splitArrayArithmetic.py:1183-1187,1202-1203). */
+int fadesim_slice_inputs_im2col_f32(const int32_t *xq, int N, int C, int H, int W, int kh, int kw, int sh, int sw,
+                                    int ph, int pw, int dh, int dw, int has_ones, int ones_q, int rows, int numX,
+                                    int nbits, int dac_bits, int neg_pulse, float inputV, float *v, void *stream);
+
+/* Conductance map of one weight slice of a Ref-column array (phyArrMode.Ref): G [numX, rows,
+ * numY*(cols+2)]; data cells hold ((min(w + plus, maximum)) >> shift) & (2^cell_bits - 1), padded cells
+ * state 0, and each column block ends with a state-0 and a state-1 reference column on every row
+ * (splitArrayArithmetic.py:758-771, 1229-1242). */
+int fadesim_map_conductance_ref_f32(const int32_t *wq, int insize, int outsize, int rows, int cols, int numX,
+                                    int numY, int shift, int cell_bits, int plus, int maximum, float dG, float Gmin,
+                                    float *G, void *stream);
+
+/* fadesim_adc_shift_add_f32 for both array modes, with the float32 bias and the output layout of
+ * the layer.  ref_cols == 0: PN, I as above.  ref_cols == cols: Ref, I [nslices][nbits][B][numX][ldI]
+ * with ldI = numY*(cols+2); per row tile the state-0 column's code is subtracted from each column's
+ * and, for slice 0, rint(plus * (code_one - code_zero)) too (splitArrayArithmetic.py:980-996).
+ * bias (may be NULL) is added after the shift-add (linear_split.py:73-76, conv_split.py:123-126);
+ * L > 0 writes [B/L, outsize, L] (a convolution's NCHW output, L = OH*OW), else [B, outsize]. */
+int fadesim_adc_shift_add_ex_f32(const float *I, int ref_cols, int nbits, int nslices, int B, int numX, int ldI,
+                                 int outsize, float adcUseI, float levels, float scale, int s12, int dac_bits,
+                                 int cell_bits, int input_bits, int complement, float plus, const float *bias, int L,
+                                 float *out, void *stream);
+
 /* Allocation-free variant of the line solve (FP32, bitline currents only).
  * No counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc -- code running inside someone else's stream capture, host

@@ -2,8 +2,9 @@
 
 Test infrastructure only: see ``oracle/__init__.py``.
 
-Covers the PN-array, whole-array (no OU), complement-code-input, 1-bit-DAC path
-of ``splitArr_matmul_nn`` / ``matmul``:
+Covers the whole-array (no OU) path of ``splitArr_matmul_nn`` / ``matmul`` for
+PN and Ref-column arrays, complement-code and negative-pulse inputs, and the
+``Conv2d_sp`` evaluation path around it:
 
 * fixed-point quantisation, s = ceil(log2(max|x| / (2^(b-1)-1))) for Normal and
   ceil(log2(max|x| / (2^b-1))) for PN, x_int = round-half-even(x / 2^s)
@@ -17,7 +18,14 @@ of ``splitArr_matmul_nn`` / ``matmul``:
 * sum over row tiles, crop, * rows*(2^dac-1)*(2^cell-1)/(2^adc-1), pos - neg
   (splitArrayArithmetic.py:961-978);
 * shift-add: output +/- out * 2^(i+j+s1+s2), the top input bit subtracted
-  (complement code) (splitArrayArithmetic.py:1224-1227).
+  (complement code) (splitArrayArithmetic.py:1224-1227);
+* negative-pulse inputs: bit i of a negative input is -((|x| >> i) & mask),
+  every bit added (splitArrayArithmetic.py:1183-1187,1202-1203);
+* Ref-column arrays: weights quantised as Normal, offset by 2^(b-1) and
+  clamped to 2^b-1 (:1229-1242), two reference columns per column block (state 0
+  and state 1, :758-771), the state-0 column's code subtracted from every
+  column and, for slice 0, 2^(b-1) times the state-1 column's (:980-996);
+* Conv2d_sp: unfold, matmul, fold (fixedPoint/nn/modules/conv_split.py:106-134).
 
 Every float step is float32 with the reference's operation order; scalar
 operands are rounded to float32 first, which is what torch does for a float32
@@ -145,3 +153,120 @@ def droop_solver(in_v, G, B, rows, cols, numX, numY):
     ideal = ideal_solver(in_v, G, B, rows, cols, numX, numY).astype(np.float64)
     j = np.arange(numY * cols) % cols
     return (ideal * (1.0 - 0.0031 * (j % 11) - 0.0007 * (j // 11))).astype(f32)
+
+
+def slice_matmul_ref(in_v, g, j, p, solver):
+    """One input-bit x weight-slice product on a Ref-column array
+    (matmul, splitArrayArithmetic.py:758-771 map, :818 solve, :835-836 ADC,
+    :980-996 reference-column subtraction).
+
+    in_v [B, insize] input levels (signed for negative pulses); g [insize,
+    outsize] cell states of slice j.  Returns float32 [B, outsize].
+    """
+    B, insize = in_v.shape
+    outsize = g.shape[1]
+    rows, cols = p.arrRowSize, p.arrColSize
+    inputV = p.inputMaxVoltage / (2 ** p.dac_bits - 1)
+    pad_in = (-insize) % rows
+    pad_out = (-outsize) % cols
+    in_v = np.pad(in_v, ((0, 0), (0, pad_in)))
+    g = np.pad(g, ((0, pad_in), (0, pad_out)))
+    true_in, true_out = insize + pad_in, outsize + pad_out
+    numX, numY = true_in // rows, true_out // cols
+    extra = np.zeros((true_in, numY, 2), g.dtype)
+    extra[..., 1] = 1
+    g = np.concatenate([g.reshape(true_in, numY, cols), extra], axis=2)
+    G = (g.astype(f32) * f32(p.cellDeltaConduct) + f32(p.cellMinConduct)).reshape(numX, rows, numY * (cols + 2))
+    in_f = (in_v.astype(f32) * f32(inputV)).reshape(B, numX, rows)
+    I = np.asarray(solver(in_f, G, B, rows, cols + 2, numX, numY), f32)
+    code = np.round((I / f32(p.adcUseI)) * f32(2 ** p.adc_bits - 1)).reshape(B, numX, numY, cols + 2)
+    code = code - code[..., cols:cols + 1]
+    if j == 0:
+        plus = 2 ** (p.weight_bits - 1)
+        code = code - np.round(code[..., cols + 1:cols + 2] * f32(plus))
+    scale = f32(rows * (2 ** p.dac_bits - 1) * (2 ** p.cellBits - 1) / (2 ** p.adc_bits - 1))
+    return (code[..., :cols].sum(axis=1, dtype=f32).reshape(B, -1)[:, :outsize] * scale).astype(f32)
+
+
+def split_matmul_ex(x, w, p, arr="PN", neg_pulse=False, solver=ideal_solver):
+    """splitArr_matmul_nn (splitArrayArithmetic.py:1161-1260) for PN or Ref
+    arrays and complement-code or negative-pulse inputs."""
+    x = np.asarray(x, f32)
+    w = np.asarray(w, f32)
+    B = x.shape[0]
+    xi, s1 = quantize(x, p.input_bits, pn=False)
+    if not neg_pulse and p.dac_bits != 1:
+        raise ValueError("complement-code inputs need a 1-bit DAC")
+    mask_cell = (1 << p.cellBits) - 1
+    mask_in = (1 << p.dac_bits) - 1
+
+    def in_bits(i):
+        b = (xi >> i) & mask_in
+        if neg_pulse:
+            b = np.where(xi < 0, -((np.abs(xi) >> i) & mask_in), b)
+        return b
+
+    def sign(i):
+        return -1 if (i == p.input_bits - 1 and not neg_pulse) else 1
+
+    out = np.zeros((B, w.shape[1]), f32)
+    if arr == "PN":
+        wi, s2 = quantize(w, p.weight_bits, pn=True)
+        wpos = np.where(wi < 0, 0, wi).astype(np.int32)
+        wneg = np.abs(np.where(wi > 0, 0, wi)).astype(np.int32)
+        for i in range(0, p.input_bits, p.dac_bits):
+            ib = in_bits(i)
+            for j in range(0, p.weight_bits, p.cellBits):
+                o = slice_matmul(ib, (wpos >> j) & mask_cell, (wneg >> j) & mask_cell, p, solver)
+                t = o * f32(2.0 ** (i + j + s1 + s2))
+                out = (out + t if sign(i) > 0 else out - t).astype(f32)
+        return out
+    wi, s2 = quantize(w, p.weight_bits, pn=False)
+    plus = 2 ** (p.weight_bits - 1)
+    wi = np.minimum(wi + plus, 2 ** p.weight_bits - 1).astype(np.int32)
+    for i in range(0, p.input_bits, p.dac_bits):
+        ib = in_bits(i)
+        for j in range(0, p.weight_bits, p.cellBits):
+            o = slice_matmul_ref(ib, (wi >> j) & mask_cell, j, p, solver)
+            t = o * f32(2.0 ** (i + j + s1 + s2))
+            out = (out + t if sign(i) > 0 else out - t).astype(f32)
+    return out
+
+
+def unfold(x, kh, kw, stride=(1, 1), padding=(0, 0), dilation=(1, 1)):
+    """torch.nn.functional.unfold as a [N*L, C*kh*kw] matrix (rows = output
+    positions, columns ordered channel, kernel row, kernel column)."""
+    x = np.asarray(x)
+    N, C, H, W = x.shape
+    sh, sw = stride
+    ph, pw = padding
+    dh, dw = dilation
+    OH = (H + 2 * ph - dh * (kh - 1) - 1) // sh + 1
+    OW = (W + 2 * pw - dw * (kw - 1) - 1) // sw + 1
+    xp = np.pad(x, ((0, 0), (0, 0), (ph, ph), (pw, pw)))
+    cols = np.empty((N, OH, OW, C, kh, kw), x.dtype)
+    for ki in range(kh):
+        for kj in range(kw):
+            cols[:, :, :, :, ki, kj] = xp[:, :, ki * dh:ki * dh + sh * (OH - 1) + 1:sh,
+                                          kj * dw:kj * dw + sw * (OW - 1) + 1:sw].transpose(0, 2, 3, 1)
+    return cols.reshape(N * OH * OW, C * kh * kw), OH, OW
+
+
+def conv2d_sp(x, weight, bias, p, stride=(1, 1), padding=(0, 0), dilation=(1, 1), arr="PN", neg_pulse=False,
+              use_fp_bias=True, solver=ideal_solver):
+    """Conv2d_sp evaluation (conv_split.py:106-134): unfold, the split matmul
+    against W reshaped [Cout, C*kh*kw] and transposed, bias in float32 (or
+    mapped to an extra array row driven by ones), fold back to NCHW."""
+    x = np.asarray(x, f32)
+    weight = np.asarray(weight, f32)
+    N = x.shape[0]
+    Cout, _, kh, kw = weight.shape
+    cols, OH, OW = unfold(x, kh, kw, stride, padding, dilation)
+    wm = weight.reshape(Cout, -1).T
+    if bias is not None and not use_fp_bias:
+        cols = np.concatenate([cols, np.ones((cols.shape[0], 1), f32)], axis=1)
+        wm = np.concatenate([wm, np.asarray(bias, f32)[None]], axis=0)
+    y = split_matmul_ex(cols, wm, p, arr=arr, neg_pulse=neg_pulse, solver=solver)
+    if bias is not None and use_fp_bias:
+        y = (y + np.asarray(bias, f32)).astype(f32)
+    return np.ascontiguousarray(y.reshape(N, OH * OW, Cout).transpose(0, 2, 1)).reshape(N, Cout, OH, OW)

@@ -7,13 +7,14 @@ Runs only where the reference tree is present (it reads it from
    ``make -C oracle ref`` into ``oracle/_ref/sim``, run on seeded configs written
    as explicit per-cell ``setCellR`` lines (its ``randSetR`` is unseeded).
 2. The reference's PimTorch modules, imported through a throw-away package in a
-   temporary directory: the six ``fixedPoint/nn`` files are copied there
-   unchanged except that the import-time JIT build and ``chdir`` in
-   ``commonConst.py`` are removed (the CUDA source does not compile against this
+   temporary directory: the six ``fixedPoint/nn`` files and
+   ``fixedPoint/nn/modules/conv_split.py`` are copied there unchanged except
+   that the import-time JIT build and ``chdir`` in ``commonConst.py`` are
+   removed (the CUDA source does not compile against this
    torch and there is no GPU here).  Nothing from that copy is kept.
 3. Their outputs, saved as small .npz files next to this script.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [sim] [pimtorch] [layers]
 """
 import os
 import re
@@ -97,6 +98,9 @@ def import_pimtorch():
     for f in ["conductance_variation.py", "fixedPointArithmetic.py", "ir_drop_solve.py",
               "splitArrayArithmetic.py", "ir_drop_compensate.py"]:
         shutil.copy(os.path.join(NN, f), os.path.join(pkg, "nn", f))
+    os.makedirs(os.path.join(pkg, "nn", "modules"))
+    open(os.path.join(pkg, "nn", "modules", "__init__.py"), "w").close()
+    shutil.copy(os.path.join(NN, "modules", "conv_split.py"), os.path.join(pkg, "nn", "modules", "conv_split.py"))
     with open(os.path.join(NN, "commonConst.py")) as f:
         src = f.read()
     # drop the import-time chdir and JIT build of the CUDA extension
@@ -186,7 +190,91 @@ def pimtorch_fixtures():
         shutil.rmtree(td, ignore_errors=True)
 
 
+def pimtorch_layer_fixtures():
+    """Ref-column arrays, negative-pulse inputs and Conv2d_sp evaluation, through
+    the reference's own splitArr_matmul_nn and Conv2d_sp with the droop solve."""
+    import torch
+    td, cc, ids, sa = import_pimtorch()
+    try:
+        import fixedPoint.nn.modules.conv_split as cs
+        P = cc.phyArrParams
+        P.cpp_ir_drop_accelerate_flag = True
+        P.cpp_ir_drop_accelerate = _DroopSolve()
+        P.IRdropMode = cc.ir_drop_mode.accurate_GS_math
+        P.useOUSize = False
+        P.useBNN = False
+        P.sigma = 0
+        # linear layers: (name, params, input mode, array mode, dac bits, x, w)
+        lin = [
+            ("ref_c2", dict(Ron=1e3, Roff=1e6, cellBits=2, rows=32, cols=24, inputMaxVoltage=0.2, adc_bits=8),
+             "complement_code", "Ref", 1,
+             lambda r: r.integers(0, 256, (6, 90)).astype(np.float32),
+             lambda r: (r.standard_normal((90, 50)) * 0.05).astype(np.float32)),
+            ("ref_signed", dict(Ron=1e3, Roff=1e6, cellBits=1, rows=64, cols=64, inputMaxVoltage=1.0, adc_bits=10),
+             "complement_code", "Ref", 1,
+             lambda r: r.standard_normal((4, 130)).astype(np.float32),
+             lambda r: (r.standard_normal((130, 70)) * 0.1).astype(np.float32)),
+            ("negpulse_pn_dac2", dict(Ron=1e3, Roff=1e6, cellBits=2, rows=32, cols=32, inputMaxVoltage=0.3,
+                                      adc_bits=9, dac_bits=2),
+             "neg_pulse", "PN", 2,
+             lambda r: r.standard_normal((5, 75)).astype(np.float32),
+             lambda r: (r.standard_normal((75, 40)) * 0.08).astype(np.float32)),
+            ("negpulse_ref", dict(Ron=1e3, Roff=1e6, cellBits=1, rows=32, cols=16, inputMaxVoltage=1.0, adc_bits=10),
+             "neg_pulse", "Ref", 1,
+             lambda r: r.standard_normal((3, 40)).astype(np.float32),
+             lambda r: (r.standard_normal((40, 33)) * 0.1).astype(np.float32)),
+        ]
+        for name, kw, imode, amode, dac, mkx, mkw in lin:
+            p = intstages.ArrayParams(**kw)
+            set_params(cc, p)
+            P.inputVmode = getattr(cc.input_v_mode, imode)
+            r = np.random.default_rng(100 + len(name))
+            x, w = mkx(r), mkw(r)
+            y = sa.splitArr_matmul_nn(torch.from_numpy(x), torch.from_numpy(w), 8, dac, p.adc_bits, 10, 8,
+                                      getattr(cc.phyArrMode, amode), torch.float32)
+            np.savez_compressed(os.path.join(HERE, "pimtorch_layer_%s.npz" % name), x=x, w=w, y=y.numpy(),
+                                input_mode=imode, arr_mode=amode, **dict(kw, dac_bits=dac))
+        # Conv2d_sp: (name, params, array mode, use_fp_bias, conv args, input shape, big value at an
+        # input row the unfold never reads)
+        conv = [
+            ("conv_pn", dict(Ron=1e3, Roff=1e6, cellBits=2, rows=32, cols=32, inputMaxVoltage=0.2, adc_bits=8),
+             "PN", True, dict(in_channels=3, out_channels=10, kernel_size=(3, 3), stride=1, padding=1),
+             (2, 3, 9, 9), None),
+            ("conv_ref_stride", dict(Ron=1e3, Roff=1e6, cellBits=1, rows=16, cols=16, inputMaxVoltage=1.0,
+                                     adc_bits=10),
+             "Ref", False, dict(in_channels=4, out_channels=20, kernel_size=(2, 3), stride=(3, 1), padding=(0, 1),
+                                dilation=(1, 2)),
+             (2, 4, 11, 7), 5),
+        ]
+        for name, kw, amode, fpb, cargs, shape, hole in conv:
+            p = intstages.ArrayParams(**kw)
+            set_params(cc, p)
+            P.inputVmode = cc.input_v_mode.complement_code
+            r = np.random.default_rng(200 + len(name))
+            torch.manual_seed(7)
+            layer = cs.Conv2d_sp(**cargs, bias=True, input_bit_width=8, output_bit_width=10, weight_bit_width=8,
+                                 dac_bit_width=1, adc_bit_width=p.adc_bits,
+                                 phy_arr_mode=getattr(cc.phyArrMode, amode), use_fp_bias=fpb)
+            x = r.standard_normal(shape).astype(np.float32)
+            if hole is not None:
+                x[:, :, hole, :] = 40.0
+            layer.eval()
+            with torch.no_grad():
+                y = layer(torch.from_numpy(x))
+            np.savez_compressed(os.path.join(HERE, "pimtorch_layer_%s.npz" % name), x=x,
+                                weight=layer.fp_weight.detach().numpy(), bias=layer.fp_bias.detach().numpy(),
+                                y=y.numpy(), arr_mode=amode, use_fp_bias=fpb,
+                                **{"conv_" + k: np.array(v) for k, v in cargs.items()}, **kw)
+    finally:
+        shutil.rmtree(td, ignore_errors=True)
+
+
 if __name__ == "__main__":
-    sim_fixtures()
-    pimtorch_fixtures()
+    which = sys.argv[1:] or ["sim", "pimtorch", "layers"]
+    if "sim" in which:
+        sim_fixtures()
+    if "pimtorch" in which:
+        pimtorch_fixtures()
+    if "layers" in which:
+        pimtorch_layer_fixtures()
     print("fixtures written to", HERE)

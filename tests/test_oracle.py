@@ -107,6 +107,40 @@ def test_integer_stages_bit_exact(gold, name):
     assert np.array_equal(y, z["y"])
 
 
+LAYER_LINEAR = ["ref_c2", "ref_signed", "negpulse_pn_dac2", "negpulse_ref"]
+LAYER_CONV = ["conv_pn", "conv_ref_stride"]
+
+
+def layer_params(z):
+    kw = {k: z[k].item() for k in ["Ron", "Roff", "cellBits", "rows", "cols", "inputMaxVoltage", "adc_bits"]}
+    if "dac_bits" in z:
+        kw["dac_bits"] = int(z["dac_bits"])
+    return intstages.ArrayParams(**kw)
+
+
+@pytest.mark.parametrize("name", LAYER_LINEAR)
+def test_ref_and_negpulse_stages_bit_exact(gold, name):
+    """Ref-column arrays and negative-pulse inputs against the reference's own
+    splitArr_matmul_nn (same droop solve)."""
+    z = gold("pimtorch_layer_%s.npz" % name)
+    y = intstages.split_matmul_ex(z["x"], z["w"], layer_params(z), arr=str(z["arr_mode"]),
+                                  neg_pulse=str(z["input_mode"]) == "neg_pulse", solver=intstages.droop_solver)
+    assert y.dtype == np.float32
+    assert np.array_equal(y, z["y"])
+
+
+@pytest.mark.parametrize("name", LAYER_CONV)
+def test_conv2d_sp_bit_exact(gold, name):
+    """Conv2d_sp evaluation (unfold, split matmul, bias, fold) against the reference module."""
+    z = gold("pimtorch_layer_%s.npz" % name)
+    pair = lambda k, d: tuple(np.broadcast_to(z[k], 2)) if k in z else d
+    y = intstages.conv2d_sp(z["x"], z["weight"], z["bias"], layer_params(z), stride=pair("conv_stride", (1, 1)),
+                            padding=pair("conv_padding", (0, 0)), dilation=pair("conv_dilation", (1, 1)),
+                            arr=str(z["arr_mode"]), use_fp_bias=bool(z["use_fp_bias"]), solver=intstages.droop_solver)
+    assert y.shape == z["y"].shape
+    assert np.array_equal(y, z["y"])
+
+
 def test_converged_sweeps_reach_direct_solution():
     """The sweep-order restatement converges to the direct solve (same system)."""
     rng = np.random.default_rng(5)
