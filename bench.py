@@ -4,8 +4,10 @@ Workload (one step): 4096 independent 128x128 crossbar tiles, 64 input vectors
 each (262,144 tile x vector solves), four-state cells R in {2e6, 1.6e6, 1.3e6,
 1e6} ohm drawn uniformly, 2.93 ohm wire segments, wordline inputs
 Bernoulli(0.5) in {0, 0.2} V, bitlines grounded, FP32.  Every solve is driven
-to 1e-8 V (estimated) of the nodal solution; a seeded sample is checked against
-the FP64 oracle before timing.  Data are synthetic (seeded numpy generators).
+to an estimated 5e-7 V of the nodal solution (the metric's 1e-6 V bound with a
+2x margin on the estimate; --tol changes it); a seeded sample of 512 solves,
+run exactly as the timed ones, is checked against the FP64 oracle before
+timing.  Data are synthetic (seeded numpy generators).
 
 Metric: 128x128 crossbar solves per second, whole job.  ``value`` is measured
 with inputs resident in HBM; ``e2e`` through the public drop-in call with
@@ -37,6 +39,7 @@ R_STATES = np.array([2e6, 1.6e6, 1.3e6, 1e6])
 R_WIRE = 2.93
 V_READ = 0.2
 METRIC = "128x128 crossbar solves/s (<=1e-6 V node error)"
+TOL_V = 5e-7  # stop when the estimated max node error is below this (volts)
 UNIT = "solves/s"
 # algorithmic HBM bytes per solve: G amortised over the tile's vectors, the
 # input vector and the output currents, FP32
@@ -223,17 +226,21 @@ def large_nonideal(torch, acc, n_tiles=64, n_vec=32, seed=5):
             "line_iters_mean": st["iters_sum"] / st["solves"], "status_or": st["status_or"]}
 
 
-def check_accuracy(acc, G, vin, torch):
-    """A seeded sample of solves against the FP64 oracle (both planes)."""
+def check_accuracy(acc, G, vin, torch, k=8):
+    """Max node error over both planes of k tiles x all their vectors, solved as
+    the timed run solves them (same options, one work item per tile), against
+    the FP64 oracle.  Float64 inputs give float64 planes, so the comparison is
+    not limited by FP32 rounding of the output (the solve itself is FP32)."""
     from oracle import nodal
-    k = 4
-    tg = torch.from_numpy(G[:k]).cuda()
-    ti = torch.from_numpy(np.ascontiguousarray(vin[:16, :k])).cuda()
-    planes, _, _ = acc.ir_drop_gs_ex(ti, tg, 16, ROWS, COLS, k, 1, g_wire=1 / R_WIRE, ret_V=2, method="line")
-    planes = planes.double().cpu().numpy()
+    nv = vin.shape[0]
+    tg = torch.from_numpy(G[:k].astype(np.float64)).cuda()
+    ti = torch.from_numpy(np.ascontiguousarray(vin[:, :k]).astype(np.float64)).cuda()
+    planes, _, _ = acc.ir_drop_gs_ex(ti, tg, nv, ROWS, COLS, k, 1, g_wire=1 / R_WIRE, ret_V=2, method="line",
+                                     vectors_per_cta=nv)
+    planes = planes.cpu().numpy()
     err = 0.0
     for x in range(k):
-        u, d = nodal.solve(G[x].astype(np.float64), 1 / R_WIRE, vin[:16, x].astype(np.float64))
+        u, d = nodal.solve(G[x].astype(np.float64), 1 / R_WIRE, vin[:, x].astype(np.float64))
         err = max(err, np.abs(planes[:, x, 0, 0] - u).max(), np.abs(planes[:, x, 0, 1] - d).max())
     return err
 
@@ -251,6 +258,7 @@ def run_ours(args):
     from fadesim_gb300 import cpp_ir_drop_accelerate as acc
     from fadesim_gb300.build import build
     build()
+    acc.options.tol_v = args.tol  # every call below, the drop-in included
 
     G, vin = make_workload(1000 + rank, n_tiles=args.tiles)
     tg = torch.from_numpy(G).cuda()
@@ -324,7 +332,8 @@ def run_ours(args):
 
     # the same step under the other residual precisions (one timed step each)
     variants = {}
-    for vname, kw in [("fp32_residual_only", dict(residual_period=-1)), ("native_fp64_residual", dict(residual="fp64"))]:
+    for vname, kw in [("fp32_residual_only", dict(residual_period=-1)), ("native_fp64_residual", dict(residual="fp64")),
+                      ("float_float_every_iteration", dict(residual_period=1)), ("tol_1e-8", dict(tol_v=1e-8))]:
         acc.ir_drop_gs_ex(ti, tg, B, ROWS, COLS, X, Y, g_wire=gw, method="line", return_stats=False, **kw)
         v0 = torch.cuda.Event(enable_timing=True)
         v1 = torch.cuda.Event(enable_timing=True)
@@ -367,8 +376,11 @@ def run_ours(args):
         "config": {"workload": "%d tiles x %d vectors of 128x128 per rank (ir_drop_gs layout B=%d, numX=%d, "
                                "numY=1), 4-state cells, 2.93 ohm wires, Bernoulli 0.2 V inputs"
                                % (N_TILES, N_VEC, B, X),
-                   "solver": "block line relaxation: FP32 tridiagonal line solves, residual recomputed every "
-                             "iteration in float-float (FP64-class) arithmetic, tol 1e-8 V",
+                   "solver": "block line relaxation: FP32 tridiagonal line solves; residual in FP32, and in "
+                             "float-float (FP64-class) arithmetic on the iteration expected to be the last, which "
+                             "must pass the stop test; tol %.0e V (estimated max node error)" % args.tol,
+                   "accuracy_sample": "%d tiles x %d vectors solved as timed, FP64 oracle, both planes"
+                                      % (8, N_VEC),
                    "l2": "inputs %.0f MB vs 129 MB L2, no flush" % ((G.nbytes + vin.nbytes) / 1e6),
                    "max_node_err_v_sample": err, "line_iters_mean": stats["iters_sum"] / max(1, stats["solves"]),
                    "line_iters_max": stats["iters_max"],
@@ -400,6 +412,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--tiles", type=int, default=N_TILES, help="128x128 tiles per rank (64 vectors each)")
+    ap.add_argument("--tol", type=float, default=TOL_V, help="stop tolerance, estimated max node error (V)")
     ap.add_argument("--no-mixed", action="store_true",
                     help="skip the mixed-size (64/128/256) and large non-ideal (512) figures")
     ap.add_argument("--no-warm", action="store_true", help="skip training/evaluating the learned warm start")

@@ -57,7 +57,7 @@ def _store(n, m, method, kw, ms):
 def candidates(method):
     if method == "rbsor":
         return [dict(omega=w) for w in (1.96, 1.97, 1.975, 1.98, 1.985)]
-    return [dict(vectors_per_cta=v, residual_period=k) for v in (0, 8, 32) for k in (1, 4)]
+    return [dict(vectors_per_cta=v, residual_period=k) for v in (0, 8, 32) for k in (0, 1)]
 
 
 def tune(G, vin, g_wire=1 / 2.93, method="line", reps=3):

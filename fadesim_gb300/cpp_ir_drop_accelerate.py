@@ -35,7 +35,7 @@ class SolverOptions:
     method: str = os.environ.get("FADESIM_METHOD", "auto")
     tol_v: float = 1e-8
     max_iters: int = 0           # 0: method default
-    residual_period: int = 1     # precise residual every k line iterations (-1: FP32 only)
+    residual_period: int = 0     # 0: adaptive; k > 0: precise residual every k line iterations; -1: FP32 only
     omega: float = 0.0           # 0: adaptive (line) / size formula (rbsor)
     vectors_per_cta: int = 0     # 0: automatic
     residual: str = "ff"         # precise residual: "ff" (float-float on the FP32 pipe) or "fp64"

@@ -81,7 +81,7 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
                    cudaStream_t st) {
     const int L = a.n > a.m ? a.n : a.m;
     a.ctl.tol_v = (opts && opts->tol_v > 0) ? (float)opts->tol_v : 1e-8f;
-    a.ctl.residual_period = (opts && opts->residual_period != 0) ? opts->residual_period : 1;
+    a.ctl.residual_period = opts ? opts->residual_period : 0;  // 0: adaptive schedule
     a.ctl.residual_ff = (opts && opts->residual_kind == 1) ? 0 : 1;
     const int sms = device_sms();
     int grid = 0, ld = 0;

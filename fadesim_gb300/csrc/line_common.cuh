@@ -62,6 +62,40 @@ __device__ __forceinline__ float line_residual(float prev, float cur, float nxt,
     }
 }
 
+// The same residual divided by gw (volts), with gs = g / gw:
+//   r' = hl (prev - cur) + hr (nxt - cur) + gs src,  hl, hr in {0, 1}.
+// Solving T' d = r' with T' = T / gw gives the same correction without a
+// multiply by gw per node; the line kernels store gs and the multipliers
+// gw / pivot.
+template <bool WORD, int RES>
+__device__ __forceinline__ float line_residual_s(float prev, float cur, float nxt, float gs, float o, float vin,
+                                                 bool has_l, bool has_r) {
+    if (RES == 1) {
+        const double dp = widen_f64(prev), dc = widen_f64(cur), dn = widen_f64(nxt);
+        const double src = WORD ? (widen_f64(o) - widen_f64(vin)) - dc : (widen_f64(o) + widen_f64(vin)) - dc;
+        const double lap = (has_l ? dp - dc : 0.0) + (has_r ? dn - dc : 0.0);  // exact: widened FP32 inputs
+        return __double2float_rn(fma(widen_f64(gs), src, lap));
+    } else if (RES == 2) {
+        float sh, sl, th, tl, a1h, a1l, a2h, a2l, lh, ll;
+        two_sum(o, WORD ? -vin : vin, sh, sl);           // o -/+ vin
+        two_sum(sh, -cur, th, tl);                        // ... - own
+        two_sum(has_l ? prev : cur, -cur, a1h, a1l);      // left difference (0 if absent)
+        two_sum(has_r ? nxt : cur, -cur, a2h, a2l);       // right difference (0 if absent)
+        two_sum(a1h, a2h, lh, ll);
+        const float lap_lo = __fadd_rn(ll, __fadd_rn(a1l, a2l));
+        const float src_lo = __fadd_rn(tl, sl);
+        const float ph = __fmul_rn(gs, th), pl = __fmaf_rn(gs, th, -ph);
+        float rh, rl;
+        two_sum(lh, ph, rh, rl);
+        const float lo = __fadd_rn(__fadd_rn(rl, __fadd_rn(lap_lo, pl)), __fmul_rn(gs, src_lo));
+        return __fadd_rn(rh, lo);
+    } else {
+        const float src = WORD ? (o - vin) - cur : (o + vin) - cur;
+        const float lap = (has_l ? prev - cur : 0.f) + (has_r ? nxt - cur : 0.f);
+        return fmaf(gs, src, lap);
+    }
+}
+
 }  // namespace fadesim
 
 namespace fadesim {
@@ -76,18 +110,46 @@ namespace fadesim {
 //                   omega = 2 / (1 + sqrt(1 - rho_GS)) (Young, 2-block
 //                   partition), refined at iteration 12 from the observed SOR
 //                   rate lambda via mu^2 = (lambda + omega - 1)^2 / (lambda omega^2).
+//   precision       (adaptive schedule) the next iteration's residual is made
+//                   precise when it is expected to be the last one -- its
+//                   predicted estimate delta * rho * rho / (1 - rho) within 4x
+//                   of the tolerance -- or when its correction delta * rho is
+//                   expected to approach the FP32 residual noise (~64 ulps of
+//                   the largest deviation).  Before a rate has been observed,
+//                   rho is the first observed rate (delta_2 / delta_1) of the
+//                   previous vector of the same tile (hint), or unknown: the
+//                   rate of the first step, larger than the later ones, is
+//                   what the first prediction needs.
 struct LineStop {
     float omega;
     bool adapt;
     int it;
     float h0, h1, h2, h3;  // delta of this and the 3 previous iterations
+    float rho;             // rate used by the last update (0: unknown)
+    float hint;            // rate carried from the previous vector of the tile (0: none)
+    float first;           // delta_2 / delta_1 of this solve (0: not yet)
 
-    __device__ __forceinline__ void init(float omega_fixed) {
+    __device__ __forceinline__ void init(float omega_fixed, float rate_hint = 0.f) {
         adapt = !(omega_fixed > 0.f);
         omega = adapt ? 1.f : omega_fixed;
         it = 0;
         h0 = h1 = h2 = h3 = 0.f;
+        hint = rate_hint;
+        rho = rate_hint;
+        first = 0.f;
     }
+
+    // Whether the next iteration should compute its residual precisely.
+    __device__ __forceinline__ bool want_precise(float tol, float vm) const {
+        if (it == 0 || !(rho > 0.f) || rho >= 0.5f) return false;
+        const float next = h0 * rho;
+        const float est_next = next * rho / (1.f - rho);
+        const float floor_v = 4.f * 1.1920929e-07f * vm;
+        return est_next <= 4.f * fmaxf(tol, floor_v) || next <= 64.f * 1.1920929e-07f * vm;
+    }
+
+    // First-step rate of the finished solve, to seed the next vector of the tile.
+    __device__ __forceinline__ float final_rate() const { return first > 0.f ? first : hint; }
 
     __device__ __forceinline__ bool update(float delta, float vm, float tol) {
         ++it;
@@ -100,7 +162,8 @@ struct LineStop {
         const float floor_v = 4.f * 1.1920929e-07f * vm;
         const float ratio = prev > 0.f ? delta / prev : 0.f;
         const float rate3 = (it >= 4 && h3 > 0.f) ? cbrtf(delta / h3) : 0.f;
-        const float rho = fmaxf(fmaxf(ratio, rate3), omega - 1.f);
+        rho = fmaxf(fmaxf(ratio, rate3), omega - 1.f);
+        if (it == 2) first = ratio;
         const float est = rho < 0.999f ? delta * rho / (1.f - rho) : INFINITY;
         const bool stalled = delta <= floor_v && ratio >= 0.9f;
         if (adapt) {

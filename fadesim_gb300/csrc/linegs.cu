@@ -13,8 +13,9 @@
 // Numerics.  Unknowns are deviations from the ideal state (wordline u - vin,
 // bitline d), so FP32 resolves ~1e-9 V.  Each line solve is a correction
 // x += omega * T^-1 r with r the line's residual computed from differences of
-// neighbouring values (FP32, or FP64 every residual_period iterations and for
-// the final convergence test) and T the line's tridiagonal matrix factored
+// neighbouring values (FP32, or precise -- float-float or FP64 -- on the
+// iterations an adaptive schedule or residual_period picks, and always for the
+// final convergence test) and T the line's tridiagonal matrix factored
 // once per tile (FP64 pivots rounded to FP32).  Forming T's diagonal in FP32
 // loses the cell term, so a direct (non-residual) FP32 line solve would stall
 // near 1e-5 V; in residual form that rounding only slows convergence.
@@ -40,7 +41,7 @@ template <int LD>
 struct LineCfg;
 template <>
 struct LineCfg<128> {
-    static constexpr int NSEG = 8, SEG = 16, LPW = 4, T = 1024, NW = 32, MINB = 1;
+    static constexpr int NSEG = 4, SEG = 32, LPW = 8, T = 512, NW = 16, MINB = 1;
 };
 template <>
 struct LineCfg<64> {
@@ -60,7 +61,7 @@ struct LineCfg<32> {
 template <int LD>
 __device__ __forceinline__ int swz(int r, int c) {
     int x;
-    if (LD == 128) x = (((((r & 3) ^ ((r >> 4) & 3)) | (((r >> 6) & 1) << 2)) << 2) | ((c >> 5) & 3));
+    if (LD == 128) x = (r & 7) | ((((c >> 5) ^ (r >> 5)) & 3) << 3);
     else if (LD == 64) x = (r & 7) | (((((c >> 5) & 1) ^ ((r >> 4) & 1))) << 3) | (((r >> 5) & 1) << 4);
     else x = r & 31;
     return r * LD + (c ^ x);
@@ -72,12 +73,17 @@ __device__ __forceinline__ int vpad(int p) { return p + (p >> 4); }
 
 // One pass over all lines of one plane.  WORD: wordline rows (own plane = U
 // deviations, other = D); else bitline columns (own = D, other = U).
-template <int LD, bool WORD, int RES, bool NL>
+// FULL: an LD x LD tile, every line and node present (the bounds tests fold away).
+// Gs holds g / gw (linear cells) or the sinh cells' positions z (NL); cm the
+// chain multipliers gw / pivot; the pass solves T' d = r' (both divided by gw).
+template <int LD, bool WORD, int RES, bool NL, bool FULL>
 __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *__restrict__ oth,
                                           const float *__restrict__ Gs, const float *__restrict__ vin_s,
-                                          const float *__restrict__ piv, const float *__restrict__ segprod, int L,
-                                          int NLINES, float gw, float omega, float &dmax, float &vmax,
+                                          const float *__restrict__ cm, const float *__restrict__ segprod,
+                                          int L_in, int NLINES_in, float inv_gw, float omega, float &dmax, float &vmax,
                                           const SolveCtl &ctl) {
+    const int L = FULL ? LD : L_in;
+    const int NLINES = FULL ? LD : NLINES_in;
     constexpr int SEG = LineCfg<LD>::SEG;
     constexpr int T = LineCfg<LD>::T;
     constexpr int LPW = LineCfg<LD>::LPW;
@@ -86,14 +92,14 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     const int lane = tid & 31;
     const int s = lane / LPW;
     const int line = (tid >> 5) * LPW + (lane % LPW);
-    const bool line_ok = line < NLINES;
+    const bool line_ok = FULL || line < NLINES;
     const int p0 = s * SEG;
     auto at = [&](int p) { return WORD ? swz<LD>(line, p) : swz<LD>(p, line); };
     // Addresses of this segment's nodes.  The swizzle term is constant along a
     // wordline segment, so node k sits at Bw ^ k; along a bitline segment it
     // depends on k only through k % V, so node k sits at Rb[k % V] + k * LD
     // (an immediate offset from one of V registers).
-    constexpr int V = (LD == 128) ? 4 : 8;
+    constexpr int V = 8;
     const int Bw = swz<LD>(line & (LD - 1), p0);
     int Rb[V];
 #pragma unroll
@@ -108,39 +114,46 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     //       (ground below the last node, deviation 0).
     {
         const float vl = (WORD && line_ok) ? vin_s[vpad(line)] : 0.f;
-        float prev = (line_ok && p0 > 0 && p0 - 1 < L) ? own[at(p0 - 1)] : 0.f;
-        float cur = (line_ok && p0 < L) ? own[at(p0)] : 0.f;
+        float prev = (line_ok && p0 > 0 && (FULL || p0 - 1 < L)) ? own[at(p0 - 1)] : 0.f;
+        float cur = (line_ok && (FULL || p0 < L)) ? own[at(p0)] : 0.f;
 #pragma unroll
         for (int k = 0; k < SEG; ++k) {
             const int p = p0 + k;
-            const bool valid = line_ok && p < L;
-            const float nxt = (line_ok && p + 1 < L) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
+            const bool valid = FULL || (line_ok && p < L);
+            const bool has_next = (FULL && k + 1 < SEG) || (line_ok && p + 1 < L);
+            const float nxt = has_next ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
             float r = 0.f;
             if (valid) {
                 const int q = qk(k);
                 const float o = oth[q], vv = WORD ? vl : vin_s[vpad(p)];
-                // cell conductance: stored, or the sinh cell's at the present cell voltage
-                const float g = NL ? nl_geff(Gs[q], WORD ? (cur + vv) - o : (o + vv) - cur, ctl) : Gs[q];
-                r = line_residual<WORD, RES>(prev, cur, nxt, g, o, vv, WORD || p > 0, !WORD || p + 1 < L, gw);
+                // g / gw: stored, or the sinh cell's at the present cell voltage
+                const float gs =
+                    NL ? nl_geff(Gs[q], WORD ? (cur + vv) - o : (o + vv) - cur, ctl) * inv_gw : Gs[q];
+                const bool has_l = WORD || k > 0 || p0 > 0;
+                const bool has_r = !WORD || (FULL && k + 1 < SEG) || p + 1 < L;
+                r = line_residual_s<WORD, RES>(prev, cur, nxt, gs, o, vv, has_l, has_r);
             }
             x[k] = r;
             prev = cur;
             cur = nxt;
         }
     }
-    // ---- T^-1 r by Thomas, segmented over NSEG lanes ------------------------
-    // y_p = ip_p (r_p + gw y_{p-1}),  x_p = y_p + gw ip_p x_{p+1}.  A segment
-    // maps its incoming value v to (prod_seg gw ip) v + (result with v = 0); the
-    // product is a tile constant (segprod).  Padding nodes carry ip = 0 and
-    // r = 0, which breaks both chains at the line end; the first segment's
-    // incoming y and the last segment's incoming x are zero.
-    float ip[SEG];
+    // ---- T'^-1 r' by Thomas, segmented over NSEG lanes ----------------------
+    // With c_p = gw / pivot_p:  y_p = c_p r'_p + c_p y_{p-1},  d_p = y_p + c_p d_{p+1}.
+    // A segment maps its incoming value v to (prod_seg c) v + (result with
+    // v = 0); the product is a tile constant (segprod).  Padding nodes carry
+    // c = 0 and r' = 0, which breaks both chains at the line end; the first
+    // segment's incoming y and the last segment's incoming d are zero.
+    float c[SEG];
 #pragma unroll
-    for (int k = 0; k < SEG; ++k) ip[k] = piv[k * T + tid];
+    for (int k = 0; k < SEG; ++k) c[k] = cm[k * T + tid];
     const float C = segprod[tid];
     float Y = 0.f;
 #pragma unroll
-    for (int k = 0; k < SEG; ++k) Y = ip[k] * fmaf(gw, Y, x[k]);
+    for (int k = 0; k < SEG; ++k) {
+        x[k] *= c[k];
+        Y = fmaf(c[k], Y, x[k]);
+    }
     float Ci = C, Yi = Y;
 #pragma unroll
     for (int off = 1; off < NSEG; off <<= 1) {
@@ -155,12 +168,12 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     if (s == 0) y = 0.f;
 #pragma unroll
     for (int k = 0; k < SEG; ++k) {
-        y = ip[k] * fmaf(gw, y, x[k]);
+        y = fmaf(c[k], y, x[k]);
         x[k] = y;
     }
     float X = 0.f;
 #pragma unroll
-    for (int k = SEG - 1; k >= 0; --k) X = fmaf(gw * ip[k], X, x[k]);
+    for (int k = SEG - 1; k >= 0; --k) X = fmaf(c[k], X, x[k]);
     Ci = C;
     float Xi = X;
 #pragma unroll
@@ -176,7 +189,7 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     if (s == NSEG - 1) X = 0.f;
 #pragma unroll
     for (int k = SEG - 1; k >= 0; --k) {
-        X = fmaf(gw * ip[k], X, x[k]);
+        X = fmaf(c[k], X, x[k]);
         x[k] = X;
     }
     // ---- apply the correction ----------------------------------------------
@@ -185,7 +198,7 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
 #pragma unroll
     for (int k = 0; k < SEG; ++k) {
         const int p = p0 + k;
-        if (line_ok && p < L) {
+        if (FULL || (line_ok && p < L)) {
             const int q = qk(k);
             const float nv = fmaf(omega, x[k], own[q]);
             own[q] = nv;
@@ -196,8 +209,9 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     dmax = fmaxf(dmax, omega * dm);
 }
 
-// FP64 pivots of every line of the tile, written in the order each pass thread
-// reads them (k * T + tid).
+// Chain multipliers gw / pivot of every line of the tile (pivots in FP64),
+// written in the order each pass thread reads them (k * T + tid), and the
+// product of each segment's multipliers as the pass forms it.
 template <int LD>
 __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ piv, int n, int m, float gwf) {
     constexpr int SEG = LineCfg<LD>::SEG;
@@ -213,7 +227,6 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
         float *dst = word ? piv : piv + SEG * T;
         float *prod = piv + 2 * SEG * T + (word ? 0 : T);
         const int tw_base = (line / LPW) * 32 + (line % LPW);
-        const float gwf32 = gwf;
         double p = 1.0, ipv_prev = 0.0;
         float seg_prod = 1.f;
         for (int q = 0; q < LD; ++q) {
@@ -231,10 +244,9 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
                 ipv_prev = ipv;
             }
             const int tw = tw_base + (q / SEG) * LPW;
-            const float ipf = (float)ipv;
-            dst[(q % SEG) * T + tw] = ipf;
-            // product of the segment's chain multipliers gw*ip, as the pass forms them
-            seg_prod *= gwf32 * ipf;
+            const float cf = (float)(gw * ipv);
+            dst[(q % SEG) * T + tw] = cf;
+            seg_prod *= cf;
             if (q % SEG == SEG - 1) {
                 prod[tw] = seg_prod;
                 seg_prod = 1.f;
@@ -243,7 +255,7 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
     }
 }
 
-template <int LD, typename TIO, bool NL>
+template <int LD, typename TIO, bool NL, bool FULL>
 __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_kernel(SolveArgs a) {
     constexpr int T = LineCfg<LD>::T;
     constexpr int NW = LineCfg<LD>::NW;
@@ -257,19 +269,21 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
     __shared__ int nonfinite_flag;
 
     const int tid = threadIdx.x;
-    const int n = a.n, m = a.m;
+    const int n = FULL ? LD : a.n, m = FULL ? LD : a.m;
     const int ldG = a.numY * m;
     const TIO *inp = static_cast<const TIO *>(a.input);
     const TIO *Gg = static_cast<const TIO *>(a.G);
     TIO *out = static_cast<TIO *>(a.out);
     float *piv = a.scratch + (size_t)blockIdx.x * (2 * SEG * T + 2 * T);
     const float gw = a.gw;
+    const float inv_gw = 1.f / gw;
     const float tol = a.ctl.tol_v;
     const int kres = a.ctl.residual_period;
     const int maxit = a.ctl.max_iters;
     const bool ff = a.ctl.residual_ff != 0;  // precise residual in float-float instead of FP64
     const bool precise_first = kres == 1;    // every iteration precise
     long long cached_tile = -1;
+    float rate_hint = 0.f;                   // final rate of the previous vector of this tile
     __shared__ unsigned long long st_solves, st_iters;  // this CTA's counters (thread 0)
     __shared__ int st_max, st_or;
     if (tid == 0) {
@@ -294,6 +308,14 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             __syncthreads();
             line_pivots<LD>(Gs, piv, n, m, gw);
             __syncthreads();
+            if (!NL) {
+                // the passes work in units of gw: g / gw
+                for (int e = tid; e < n * m; e += T) {
+                    const int i = e / m, j = e - i * m;
+                    Gs[swz<LD>(i, j)] = __fdiv_rn(Gs[swz<LD>(i, j)], gw);
+                }
+                __syncthreads();
+            }
             if (NL) {
                 // the sinh cells keep their on/off position; the linear values served the pivots
                 for (int e = tid; e < n * m; e += T) {
@@ -303,6 +325,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 __syncthreads();
             }
             cached_tile = tile;
+            rate_hint = 0.f;
         }
         for (int b = b0; b < b1; ++b) {
             __syncthreads();
@@ -324,19 +347,19 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 __syncthreads();
             }
             LineStop stop;
-            stop.init(a.ctl.omega);
+            stop.init(a.ctl.omega, rate_hint);
             float omega = stop.omega;
             bool res64 = precise_first;
             int status = 0, it = 0, par = 0;
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
-                if (!res64) line_pass<LD, true, 0, NL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax, a.ctl);
-                else if (ff) line_pass<LD, true, 2, NL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax, a.ctl);
-                else line_pass<LD, true, 1, NL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, gw, omega, dmax, vmax, a.ctl);
+                if (!res64) line_pass<LD, true, 0, NL, FULL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, inv_gw, omega, dmax, vmax, a.ctl);
+                else if (ff) line_pass<LD, true, 2, NL, FULL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, inv_gw, omega, dmax, vmax, a.ctl);
+                else line_pass<LD, true, 1, NL, FULL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, inv_gw, omega, dmax, vmax, a.ctl);
                 __syncthreads();
-                if (!res64) line_pass<LD, false, 0, NL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax, a.ctl);
-                else if (ff) line_pass<LD, false, 2, NL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax, a.ctl);
-                else line_pass<LD, false, 1, NL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, gw, omega, dmax, vmax, a.ctl);
+                if (!res64) line_pass<LD, false, 0, NL, FULL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else if (ff) line_pass<LD, false, 2, NL, FULL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else line_pass<LD, false, 1, NL, FULL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, inv_gw, omega, dmax, vmax, a.ctl);
                 dmax = warp_max(dmax);
                 vmax = warp_max(vmax);
                 if ((tid & 31) == 0) {
@@ -365,7 +388,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     __syncthreads();
                     warm = false;
                     status |= FADESIM_ST_WARM_REJECTED;
-                    stop.init(a.ctl.omega);
+                    stop.init(a.ctl.omega, rate_hint);
                     omega = stop.omega;
                     res64 = precise_first;
                     continue;
@@ -381,13 +404,16 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     }
                     res64 = true;
                 } else {
-                    res64 = (kres > 0) && (it % kres == 0);
+                    // kres 0: adaptive (precise when the next iteration should be
+                    // the last or nears the FP32 residual noise); k > 0: every k
+                    res64 = kres > 0 ? (it % kres == 0) : (kres == 0 && stop.want_precise(tol, vm));
                 }
                 if (it >= maxit) {
                     status |= FADESIM_ST_MAXITER;
                     break;
                 }
             }
+            rate_hint = stop.final_rate();
             // ---- outputs ------------------------------------------------------
             if (tid == 0) nonfinite_flag = 0;
             __syncthreads();
@@ -419,7 +445,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                         if (i < n) {
                             const int q = swz<LD>(i, j);
                             const TIO V = ((TIO)U[q] + (TIO)vin_s[vpad(i)]) - (TIO)D[q];
-                            TIO Ic = (TIO)(NL ? nl_geff(Gs[q], (float)V, a.ctl) : Gs[q]) * V;
+                            TIO Ic = (TIO)(NL ? nl_geff(Gs[q], (float)V, a.ctl) : Gs[q] * gw) * V;
                             if (a.ctl.noise_sigma > 0.f)
                                 Ic *= (TIO)1 + (TIO)(a.ctl.noise_sigma *
                                                      normal_from(a.ctl.noise_seed,
@@ -468,13 +494,20 @@ size_t line_relax_smem(int ld) { return (size_t)(3 * ld * ld + ld + ld / 16 + 4 
 // pivots of both passes (2 x SEG x T = 2 x LD x LD floats) and segment products (2 x T)
 size_t line_relax_scratch_floats_per_cta(int ld) { return (size_t)2 * ld * ld + 2 * (size_t)nwarps(ld) * 32; }
 
+// Instantiations: linear cells on any tile, linear cells on a full LD x LD
+// tile, sinh cells on any tile.
 template <int LD, typename TIO>
 static cudaError_t prep_one() {
-    cudaError_t e = cudaFuncSetAttribute(line_relax_kernel<LD, TIO, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)line_relax_smem(LD));
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(line_relax_kernel<LD, TIO, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)line_relax_smem(LD));
+    const int sm = (int)line_relax_smem(LD);
+    cudaError_t e = cudaFuncSetAttribute(line_relax_kernel<LD, TIO, false, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(line_relax_kernel<LD, TIO, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(line_relax_kernel<LD, TIO, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 sm);
+    return e;
 }
 
 cudaError_t line_relax_prepare(int ld, int dtype) {
@@ -491,7 +524,7 @@ cudaError_t line_relax_prepare(int ld, int dtype) {
 
 template <int LD, typename TIO>
 static cudaError_t occ_one(int *n) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, line_relax_kernel<LD, TIO, false>, LineCfg<LD>::T,
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, line_relax_kernel<LD, TIO, false, false>, LineCfg<LD>::T,
                                                          line_relax_smem(LD));
 }
 
@@ -509,8 +542,10 @@ cudaError_t line_relax_occupancy(int ld, int dtype, int *ctas) {
 
 template <int LD, typename TIO>
 static cudaError_t launch_one(const SolveArgs &a, int grid, cudaStream_t st) {
-    if (a.ctl.nl) line_relax_kernel<LD, TIO, true><<<grid, LineCfg<LD>::T, line_relax_smem(LD), st>>>(a);
-    else line_relax_kernel<LD, TIO, false><<<grid, LineCfg<LD>::T, line_relax_smem(LD), st>>>(a);
+    const size_t sm = line_relax_smem(LD);
+    if (a.ctl.nl) line_relax_kernel<LD, TIO, true, false><<<grid, LineCfg<LD>::T, sm, st>>>(a);
+    else if (a.n == LD && a.m == LD) line_relax_kernel<LD, TIO, false, true><<<grid, LineCfg<LD>::T, sm, st>>>(a);
+    else line_relax_kernel<LD, TIO, false, false><<<grid, LineCfg<LD>::T, sm, st>>>(a);
     return cudaGetLastError();
 }
 

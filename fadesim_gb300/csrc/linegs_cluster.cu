@@ -412,6 +412,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
         st_or = 0;
     }
     long long cached_tile = -1;
+    float rate_hint = 0.f;  // final rate of the previous vector of this tile (cluster-uniform)
     for (long long item = cid; item < a.nitems; item += ncl) {
         const long long tile = item / a.nchunks;
         const int chunk = (int)(item % a.nchunks);
@@ -435,6 +436,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 __syncthreads();
             }
             cached_tile = tile;
+            rate_hint = 0.f;
         }
         for (int b = b0; b < b1; ++b) {
             __syncthreads();
@@ -446,7 +448,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             __syncthreads();
             cluster.sync();  // every band initialised before halos are read
             LineStop stop;
-            stop.init(a.ctl.omega);
+            stop.init(a.ctl.omega, rate_hint);
             float omega = stop.omega;
             bool res64 = kres == 1;
             int status = 0, it = 0, par = 0;
@@ -509,13 +511,14 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                     }
                     res64 = true;
                 } else {
-                    res64 = (kres > 0) && (it % kres == 0);
+                    res64 = kres > 0 ? (it % kres == 0) : (kres == 0 && stop.want_precise(tol, vm));
                 }
                 if (it >= maxit) {
                     status = FADESIM_ST_MAXITER;
                     break;
                 }
             }
+            rate_hint = stop.final_rate();
             // ---- outputs --------------------------------------------------------
             if (tid == 0) nonfinite_flag = 0;
             __syncthreads();

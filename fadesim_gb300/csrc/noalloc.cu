@@ -111,7 +111,7 @@ extern "C" int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G
     a.ret_V = 0;
     a.ctl.tol_v = 1e-8f;
     a.ctl.max_iters = 400;
-    a.ctl.residual_period = 1;
+    a.ctl.residual_period = 0;  // adaptive, as the default of the allocating entry
     a.ctl.omega = 0.f;
     a.ctl.residual_ff = 1;
     long long grid = (long long)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);

@@ -51,7 +51,9 @@ typedef struct fadesim_solve_opts {
     double tol_v;          /* target max node error in volts (converging methods); <=0: 1e-8 */
     int max_iters;         /* cap on line iterations / point sweeps; <=0: method default */
     int residual_period;   /* precise residual every k line iterations, and always for the final
-                              convergence test; 0: 1 (every iteration); <0: FP32 residuals only */
+                              convergence test; 0 (default): adaptive -- FP32 residuals while the
+                              corrections are far above the FP32 residual noise, precise on the
+                              iteration expected to be the last; <0: FP32 residuals only */
     double omega;          /* relaxation factor; <=0: adaptive (line) or autotuned table (rbsor) */
     int vectors_per_cta;   /* input vectors one CTA solves per work item; <=0: automatic */
     int residual_kind;     /* precise residual arithmetic: 0 = float-float (default: error-free FP32
