@@ -66,7 +66,8 @@ __device__ __forceinline__ float line_residual(float prev, float cur, float nxt,
 //   r' = hl (prev - cur) + hr (nxt - cur) + gs src,  hl, hr in {0, 1}.
 // Solving T' d = r' with T' = T / gw gives the same correction without a
 // multiply by gw per node; the line kernels store gs and the multipliers
-// gw / pivot.
+// gw / pivot.  RES 0 FP32, 1 FP64, 2 float-float, 3 float-float line
+// differences with an FP32 cell term.
 template <bool WORD, int RES>
 __device__ __forceinline__ float line_residual_s(float prev, float cur, float nxt, float gs, float o, float vin,
                                                  bool has_l, bool has_r) {
@@ -89,6 +90,17 @@ __device__ __forceinline__ float line_residual_s(float prev, float cur, float nx
         two_sum(lh, ph, rh, rl);
         const float lo = __fadd_rn(__fadd_rn(rl, __fadd_rn(lap_lo, pl)), __fmul_rn(gs, src_lo));
         return __fadd_rn(rh, lo);
+    } else if (RES == 3) {
+        // the line differences exactly (their rounding dominates when the wire
+        // carries a large gradient), the cell term in FP32: for tiles whose cell
+        // term is small enough that its rounding stays far below the tolerance
+        float a1h, a1l, a2h, a2l, lh, ll;
+        two_sum(has_l ? prev : cur, -cur, a1h, a1l);
+        two_sum(has_r ? nxt : cur, -cur, a2h, a2l);
+        two_sum(a1h, a2h, lh, ll);
+        const float lap_lo = __fadd_rn(ll, __fadd_rn(a1l, a2l));
+        const float src = WORD ? (o - vin) - cur : (o + vin) - cur;
+        return __fadd_rn(lh, __fmaf_rn(gs, src, lap_lo));
     } else {
         const float src = WORD ? (o - vin) - cur : (o + vin) - cur;
         const float lap = (has_l ? prev - cur : 0.f) + (has_r ? nxt - cur : 0.f);
@@ -104,7 +116,9 @@ namespace fadesim {
 // by every thread (and every CTA of a cluster) from the same per-iteration
 // maxima.  delta = largest correction of the iteration, vm = largest deviation.
 //   error estimate  delta * rho / (1 - rho), rho the larger of the last ratio,
-//                   the 3-iteration geometric rate and omega - 1;
+//                   the 3-iteration geometric rate and omega - 1, and at least
+//                   1/2 once over-relaxed (SOR modes oscillate: a single small
+//                   correction can hide an error several times larger);
 //   floor           4 ulps of the largest deviation (FP32 resolution);
 //   relaxation      block Gauss-Seidel for 3 iterations, then
 //                   omega = 2 / (1 + sqrt(1 - rho_GS)) (Young, 2-block
@@ -113,9 +127,10 @@ namespace fadesim {
 //   precision       (adaptive schedule) the next iteration's residual is made
 //                   precise when it is expected to be the last one -- its
 //                   predicted estimate delta * rho * rho / (1 - rho) within 4x
-//                   of the tolerance -- or when its correction delta * rho is
-//                   expected to approach the FP32 residual noise (~64 ulps of
-//                   the largest deviation).  Before a rate has been observed,
+//                   of the tolerance --, when the corrections have come within
+//                   ~1000 ulps of the largest deviation (where FP32 residual
+//                   noise can dominate), or when they stall (no 10% progress in
+//                   an iteration).  Before a rate has been observed,
 //                   rho is the first observed rate (delta_2 / delta_1) of the
 //                   previous vector of the same tile (hint), or unknown: the
 //                   rate of the first step, larger than the later ones, is
@@ -141,11 +156,12 @@ struct LineStop {
 
     // Whether the next iteration should compute its residual precisely.
     __device__ __forceinline__ bool want_precise(float tol, float vm) const {
-        if (it == 0 || !(rho > 0.f) || rho >= 0.5f) return false;
-        const float next = h0 * rho;
-        const float est_next = next * rho / (1.f - rho);
+        if (it == 0 || !(rho > 0.f)) return false;
+        const float r = fminf(rho, 0.999f);
+        const float next = h0 * r;
+        const float est_next = next * r / (1.f - r);
         const float floor_v = 4.f * 1.1920929e-07f * vm;
-        return est_next <= 4.f * fmaxf(tol, floor_v) || next <= 64.f * 1.1920929e-07f * vm;
+        return est_next <= 4.f * fmaxf(tol, floor_v) || h0 <= 1e-4f * vm || (it >= 3 && h0 >= 0.9f * h1);
     }
 
     // First-step rate of the finished solve, to seed the next vector of the tile.
@@ -163,6 +179,7 @@ struct LineStop {
         const float ratio = prev > 0.f ? delta / prev : 0.f;
         const float rate3 = (it >= 4 && h3 > 0.f) ? cbrtf(delta / h3) : 0.f;
         rho = fmaxf(fmaxf(ratio, rate3), omega - 1.f);
+        if (omega > 1.f) rho = fmaxf(rho, 0.5f);
         if (it == 2) first = ratio;
         const float est = rho < 0.999f ? delta * rho / (1.f - rho) : INFINITY;
         const bool stalled = delta <= floor_v && ratio >= 0.9f;

@@ -76,7 +76,9 @@ __device__ __forceinline__ int vpad(int p) { return p + (p >> 4); }
 // FULL: an LD x LD tile, every line and node present (the bounds tests fold away).
 // Gs holds g / gw (linear cells) or the sinh cells' positions z (NL); cm the
 // chain multipliers gw / pivot; the pass solves T' d = r' (both divided by gw).
-template <int LD, bool WORD, int RES, bool NL, bool FULL>
+// ZOWN / ZOTH: the own / other plane is known to be zero (the first iteration
+// from the ideal state): its loads are skipped and the planes need no clearing.
+template <int LD, bool WORD, int RES, bool NL, bool FULL, bool ZOWN, bool ZOTH>
 __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *__restrict__ oth,
                                           const float *__restrict__ Gs, const float *__restrict__ vin_s,
                                           const float *__restrict__ cm, const float *__restrict__ segprod,
@@ -114,18 +116,18 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     //       (ground below the last node, deviation 0).
     {
         const float vl = (WORD && line_ok) ? vin_s[vpad(line)] : 0.f;
-        float prev = (line_ok && p0 > 0 && (FULL || p0 - 1 < L)) ? own[at(p0 - 1)] : 0.f;
-        float cur = (line_ok && (FULL || p0 < L)) ? own[at(p0)] : 0.f;
+        float prev = (!ZOWN && line_ok && p0 > 0 && (FULL || p0 - 1 < L)) ? own[at(p0 - 1)] : 0.f;
+        float cur = (!ZOWN && line_ok && (FULL || p0 < L)) ? own[at(p0)] : 0.f;
 #pragma unroll
         for (int k = 0; k < SEG; ++k) {
             const int p = p0 + k;
             const bool valid = FULL || (line_ok && p < L);
             const bool has_next = (FULL && k + 1 < SEG) || (line_ok && p + 1 < L);
-            const float nxt = has_next ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
+            const float nxt = (!ZOWN && has_next) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
             float r = 0.f;
             if (valid) {
                 const int q = qk(k);
-                const float o = oth[q], vv = WORD ? vl : vin_s[vpad(p)];
+                const float o = ZOTH ? 0.f : oth[q], vv = WORD ? vl : vin_s[vpad(p)];
                 // g / gw: stored, or the sinh cell's at the present cell voltage
                 const float gs =
                     NL ? nl_geff(Gs[q], WORD ? (cur + vv) - o : (o + vv) - cur, ctl) * inv_gw : Gs[q];
@@ -200,7 +202,7 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
         const int p = p0 + k;
         if (FULL || (line_ok && p < L)) {
             const int q = qk(k);
-            const float nv = fmaf(omega, x[k], own[q]);
+            const float nv = ZOWN ? omega * x[k] : fmaf(omega, x[k], own[q]);
             own[q] = nv;
             dm = fmaxf(dm, fabsf(x[k]));
             vmax = fmaxf(vmax, fabsf(nv));
@@ -255,6 +257,31 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
     }
 }
 
+// One iteration: every wordline, then every bitline.  ZERO: both planes are
+// still zero (first iteration from the ideal state).
+template <int LD, int RES, bool NL, bool FULL, bool ZERO>
+__device__ __forceinline__ void line_iteration(float *U, float *D, const float *Gs, const float *vin_s,
+                                               const float *piv, int n, int m, float inv_gw, float omega,
+                                               float &dmax, float &vmax, const SolveCtl &ctl) {
+    constexpr int SEG = LineCfg<LD>::SEG;
+    constexpr int T = LineCfg<LD>::T;
+    line_pass<LD, true, RES, NL, FULL, ZERO, ZERO>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, inv_gw, omega,
+                                                   dmax, vmax, ctl);
+    __syncthreads();
+    line_pass<LD, false, RES, NL, FULL, ZERO, false>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m,
+                                                     inv_gw, omega, dmax, vmax, ctl);
+}
+
+// Largest of one value per thread, the same in every thread (two barriers).
+template <int NW>
+__device__ __forceinline__ float block_max(float v, float *scratch) {
+    v = warp_max(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+    __syncthreads();
+    return warp_max((threadIdx.x & 31) < NW ? scratch[threadIdx.x & 31] : 0.f);
+}
+
 template <int LD, typename TIO, bool NL, bool FULL>
 __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_kernel(SolveArgs a) {
     constexpr int T = LineCfg<LD>::T;
@@ -267,6 +294,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
     float *vin_s = D + LD * LD;
     float *red = vin_s + LD + LD / 16;  // [2][2][NW]
     __shared__ int nonfinite_flag;
+    __shared__ float bmax_scratch[NW];
 
     const int tid = threadIdx.x;
     const int n = FULL ? LD : a.n, m = FULL ? LD : a.m;
@@ -284,6 +312,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
     const bool precise_first = kres == 1;    // every iteration precise
     long long cached_tile = -1;
     float rate_hint = 0.f;                   // final rate of the previous vector of this tile
+    float gs_max = 0.f;                      // largest g / gw of the tile (linear cells)
     __shared__ unsigned long long st_solves, st_iters;  // this CTA's counters (thread 0)
     __shared__ int st_max, st_or;
     if (tid == 0) {
@@ -310,11 +339,14 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             __syncthreads();
             if (!NL) {
                 // the passes work in units of gw: g / gw
+                float gm = 0.f;
                 for (int e = tid; e < n * m; e += T) {
                     const int i = e / m, j = e - i * m;
-                    Gs[swz<LD>(i, j)] = __fdiv_rn(Gs[swz<LD>(i, j)], gw);
+                    const float gsv = __fdiv_rn(Gs[swz<LD>(i, j)], gw);
+                    Gs[swz<LD>(i, j)] = gsv;
+                    gm = fmaxf(gm, fabsf(gsv));
                 }
-                __syncthreads();
+                gs_max = block_max<NW>(gm, bmax_scratch);
             }
             if (NL) {
                 // the sinh cells keep their on/off position; the linear values served the pivots
@@ -329,14 +361,31 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
         }
         for (int b = b0; b < b1; ++b) {
             __syncthreads();
-            for (int e = tid; e < LD * LD; e += T) {
-                U[e] = 0.f;
-                D[e] = 0.f;
-            }
-            if (tid < LD) vin_s[vpad(tid)] = (tid < n) ? (float)inp[((size_t)b * a.numX + x) * n + tid] : 0.f;
-            __syncthreads();
-            // warm start: initial deviation planes [2][n][m] of this solve
+            // warm start: initial deviation planes [2][n][m] of this solve.  From
+            // the ideal state the planes are zero: the first iteration is then a
+            // ZERO iteration that reads neither plane, unless every iteration must
+            // be precise (the planes are cleared instead).
             bool warm = a.init != nullptr;
+            bool zero = !warm && !precise_first;
+            if (!warm && precise_first) {
+                for (int e = tid; e < LD * LD; e += T) {
+                    U[e] = 0.f;
+                    D[e] = 0.f;
+                }
+            }
+            float vabs = 0.f;
+            if (tid < LD) {
+                const float v = (tid < n) ? (float)inp[((size_t)b * a.numX + x) * n + tid] : 0.f;
+                vin_s[vpad(tid)] = v;
+                vabs = fabsf(v);
+            }
+            // precise iterations may keep the cell term in FP32 (RES 3) when its
+            // rounding, amplified by at most L^2/2 through a line solve, stays 8x
+            // under the tolerance: per node <= gs_max * 3 vin_max * 2^-23
+            const float vin_max = block_max<NW>(vabs, bmax_scratch);
+            const float Lmax = (float)max(n, m);
+            const bool semi = !NL && ff &&
+                              gs_max * 3.f * vin_max * 1.1920929e-07f * 0.5f * Lmax * Lmax <= 0.125f * tol;
             if (warm) {
                 const float *w0 = a.init + (((size_t)b * a.numX + x) * a.numY + y) * 2 * n * m;
                 for (int e = tid; e < n * m; e += T) {
@@ -353,13 +402,12 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             int status = 0, it = 0, par = 0;
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
-                if (!res64) line_pass<LD, true, 0, NL, FULL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, inv_gw, omega, dmax, vmax, a.ctl);
-                else if (ff) line_pass<LD, true, 2, NL, FULL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, inv_gw, omega, dmax, vmax, a.ctl);
-                else line_pass<LD, true, 1, NL, FULL>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, inv_gw, omega, dmax, vmax, a.ctl);
-                __syncthreads();
-                if (!res64) line_pass<LD, false, 0, NL, FULL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, inv_gw, omega, dmax, vmax, a.ctl);
-                else if (ff) line_pass<LD, false, 2, NL, FULL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, inv_gw, omega, dmax, vmax, a.ctl);
-                else line_pass<LD, false, 1, NL, FULL>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                if (zero) line_iteration<LD, 0, NL, FULL, true>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else if (!res64) line_iteration<LD, 0, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else if (semi) line_iteration<LD, 3, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else if (ff) line_iteration<LD, 2, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else line_iteration<LD, 1, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                zero = false;
                 dmax = warp_max(dmax);
                 vmax = warp_max(vmax);
                 if ((tid & 31) == 0) {
@@ -381,11 +429,14 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     // the prediction moved as much as the solution is large: discard
                     // it and start again from the ideal state
                     __syncthreads();
-                    for (int e = tid; e < LD * LD; e += T) {
-                        U[e] = 0.f;
-                        D[e] = 0.f;
+                    if (precise_first) {
+                        for (int e = tid; e < LD * LD; e += T) {
+                            U[e] = 0.f;
+                            D[e] = 0.f;
+                        }
+                        __syncthreads();
                     }
-                    __syncthreads();
+                    zero = !precise_first;
                     warm = false;
                     status |= FADESIM_ST_WARM_REJECTED;
                     stop.init(a.ctl.omega, rate_hint);
