@@ -229,6 +229,7 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
     a.ret_V = ret_V == 2 ? 2 : (ret_V ? 1 : 0);
     a.iters_out = per_solve_iters;
     a.init = g_warm_init;
+    a.f64 = dtype == FADESIM_F64 ? 1 : 0;
     if (a.init && (ret_V == 1 || !line_relax_ld(row_size, col_size)))
         return fail(FADESIM_E_UNSUPPORTED, "warm starts apply to tiles up to 128 x 128");
     if (nonlinear_cell_enable) {

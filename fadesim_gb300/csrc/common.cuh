@@ -32,6 +32,11 @@ struct SolveCtl {
     unsigned long long noise_seed;
 };
 
+// One element of an FP32 or FP64 input array, as FP32.
+__device__ __forceinline__ float load_io(const void *p, size_t i, bool f64) {
+    return f64 ? (float)static_cast<const double *>(p)[i] : static_cast<const float *>(p)[i];
+}
+
 // sinh(t)/t, t >= 0 (series below 1e-2: truncation < 1e-10)
 __device__ __forceinline__ float sinhc(float t) { return t < 1e-2f ? fmaf(t * t, 1.f / 6.f, 1.f) : sinhf(t) / t; }
 

@@ -23,6 +23,7 @@ struct SolveArgs {
     int *iters_out;     // optional [B, numX, numY]
     DevStats *stats;    // optional
     const float *init;  // optional warm start: deviation planes [B, numX, numY, 2, n, m] (u - vin, d)
+    int f64;            // input, G and out are FP64 (else FP32); the solve itself is FP32
 };
 
 // Block line relaxation, planes resident in shared memory (n, m <= 128).

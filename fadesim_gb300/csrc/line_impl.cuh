@@ -1,0 +1,583 @@
+// Block line relaxation for the crossbar nodal system (sm_103a).
+//
+// The reference relaxes one node at a time (split_arr_matmul.cu:27-119,
+// crossbarHspice/2dArray.cc:1551-1590).  Its two planes are coupled only
+// through the cell conductance, which is 1e-6..1e-3 of the wire conductance,
+// so the natural blocks are whole lines: every wordline row is a tridiagonal
+// system in its own unknowns once the bitline plane is fixed, and every
+// bitline column is one once the wordline plane is fixed.  One iteration here
+// solves all wordlines exactly, then all bitlines exactly (block Gauss-Seidel,
+// optionally over-relaxed).  It converges to the same fixed point as the
+// reference's point sweeps: the nodal solution.
+//
+// Numerics.  Unknowns are deviations from the ideal state (wordline u - vin,
+// bitline d), so FP32 resolves ~1e-9 V.  Each line solve is a correction
+// x += omega * T^-1 r with r the line's residual computed from differences of
+// neighbouring values (FP32, or precise -- float-float or FP64 -- on the
+// iterations an adaptive schedule or residual_period picks, and always for the
+// final convergence test) and T the line's tridiagonal matrix factored
+// once per tile (FP64 pivots rounded to FP32).  Forming T's diagonal in FP32
+// loses the cell term, so a direct (non-residual) FP32 line solve would stall
+// near 1e-5 V; in residual form that rounding only slows convergence.
+//
+// Mapping.  One CTA owns one tile at a time and solves its input vectors one
+// after another with the tile's conductances and both deviation planes in
+// shared memory (3 x LD x LD floats).  A warp handles 8 lines x 4 segments of
+// SEG = LD/4 nodes; a thread keeps its segment in registers, folds the Thomas
+// recurrences locally and joins segments with a 2-step affine scan over the
+// 4 lanes of its line (__shfl at stride 8).  Planes are stored row-major with
+// an XOR swizzle so that both the row walk (wordline pass) and the column walk
+// (bitline pass) hit 32 distinct banks.
+//
+// This header holds the kernel templates; linegs_32.cu, linegs_64.cu and
+// linegs_128.cu instantiate one tile size each (parallel compilation), and
+// linegs.cu dispatches between them.  Input and output types (FP32 or FP64)
+// are a run-time property of the launch: only the load and store code differs.
+#pragma once
+#include <math.h>
+
+#include "kernels.h"
+#include "line_common.cuh"
+
+namespace fadesim {
+
+// Per-size launch shape.  A warp holds LPW lines x NSEG segments of SEG nodes;
+// T threads cover all LD lines of one pass with one segment each.
+template <int LD>
+struct LineCfg;
+template <>
+struct LineCfg<128> {
+    static constexpr int NSEG = 4, SEG = 32, LPW = 8, T = 512, NW = 16, MINB = 1;
+};
+template <>
+struct LineCfg<64> {
+    static constexpr int NSEG = 4, SEG = 16, LPW = 8, T = 256, NW = 8, MINB = 3;
+};
+template <>
+struct LineCfg<32> {
+    static constexpr int NSEG = 4, SEG = 8, LPW = 8, T = 128, NW = 4, MINB = 8;
+};
+
+// Node (r, c) of an LD x LD plane in shared memory.  The XOR term touches only
+// the low 5 bits of c and depends on c only through c >> 5, so it permutes
+// every 32-column block of a row.  For each size it is chosen so that both
+// walks -- LPW rows x NSEG segments at one step of the wordline pass, LPW
+// columns x NSEG segments at one step of the bitline pass -- hit 32 distinct
+// banks (checked exhaustively when the layouts were designed).
+template <int LD>
+__device__ __forceinline__ int swz(int r, int c) {
+    int x;
+    if (LD == 128) x = (r & 7) | ((((c >> 5) ^ (r >> 5)) & 3) << 3);
+    else if (LD == 64) x = (r & 7) | (((((c >> 5) & 1) ^ ((r >> 4) & 1))) << 3) | (((r >> 5) & 1) << 4);
+    else x = r & 31;
+    return r * LD + (c ^ x);
+}
+
+// Input voltages in shared memory, one pad word per 16 rows: the bitline pass
+// reads rows 16s + k for NSEG segments s at once, which would otherwise share banks.
+__device__ __forceinline__ int vpad(int p) { return p + (p >> 4); }
+
+// One pass over all lines of one plane.  WORD: wordline rows (own plane = U
+// deviations, other = D); else bitline columns (own = D, other = U).
+// FULL: an LD x LD tile, every line and node present (the bounds tests fold away).
+// Gs holds g / gw (linear cells) or the sinh cells' positions z (NL); cm the
+// chain multipliers gw / pivot; the pass solves T' d = r' (both divided by gw).
+// ZOWN / ZOTH: the own / other plane is known to be zero (the first iteration
+// from the ideal state): its loads are skipped and the planes need no clearing.
+template <int LD, bool WORD, int RES, bool NL, bool FULL, bool ZOWN, bool ZOTH>
+__device__ __forceinline__ void line_pass(float *__restrict__ own, const float *__restrict__ oth,
+                                          const float *__restrict__ Gs, const float *__restrict__ vin_s,
+                                          const float *__restrict__ cm, const float *__restrict__ segprod,
+                                          int L_in, int NLINES_in, float inv_gw, float omega, float &dmax, float &vmax,
+                                          const SolveCtl &ctl) {
+    const int L = FULL ? LD : L_in;
+    const int NLINES = FULL ? LD : NLINES_in;
+    constexpr int SEG = LineCfg<LD>::SEG;
+    constexpr int T = LineCfg<LD>::T;
+    constexpr int LPW = LineCfg<LD>::LPW;
+    constexpr int NSEG = LineCfg<LD>::NSEG;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int s = lane / LPW;
+    const int line = (tid >> 5) * LPW + (lane % LPW);
+    const bool line_ok = FULL || line < NLINES;
+    const int p0 = s * SEG;
+    auto at = [&](int p) { return WORD ? swz<LD>(line, p) : swz<LD>(p, line); };
+    // Addresses of this segment's nodes.  The swizzle term is constant along a
+    // wordline segment, so node k sits at Bw ^ k; along a bitline segment it
+    // depends on k only through k % V, so node k sits at Rb[k % V] + k * LD
+    // (an immediate offset from one of V registers).
+    constexpr int V = 8;
+    const int Bw = swz<LD>(line & (LD - 1), p0);
+    int Rb[V];
+#pragma unroll
+    for (int t = 0; t < V; ++t) Rb[t] = swz<LD>(p0 + t, line & (LD - 1)) - t * LD;
+    auto qk = [&](int k) { return WORD ? (Bw ^ k) : (Rb[k % V] + k * LD); };
+
+    float x[SEG];
+    // ---- residual of the line equations at the current iterate -------------
+    // WORD: left link always present (the source at p == 0, deviation 0), right
+    //       link absent at the open end.
+    // BIT:  upper link absent at the open top, lower link always present
+    //       (ground below the last node, deviation 0).
+    {
+        const float vl = (WORD && line_ok) ? vin_s[vpad(line)] : 0.f;
+        float prev = (!ZOWN && line_ok && p0 > 0 && (FULL || p0 - 1 < L)) ? own[at(p0 - 1)] : 0.f;
+        float cur = (!ZOWN && line_ok && (FULL || p0 < L)) ? own[at(p0)] : 0.f;
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) {
+            const int p = p0 + k;
+            const bool valid = FULL || (line_ok && p < L);
+            const bool has_next = (FULL && k + 1 < SEG) || (line_ok && p + 1 < L);
+            const float nxt = (!ZOWN && has_next) ? own[k + 1 < SEG ? qk(k + 1) : at(p + 1)] : 0.f;
+            float r = 0.f;
+            if (valid) {
+                const int q = qk(k);
+                const float o = ZOTH ? 0.f : oth[q], vv = WORD ? vl : vin_s[vpad(p)];
+                // g / gw: stored, or the sinh cell's at the present cell voltage
+                const float gs =
+                    NL ? nl_geff(Gs[q], WORD ? (cur + vv) - o : (o + vv) - cur, ctl) * inv_gw : Gs[q];
+                const bool has_l = WORD || k > 0 || p0 > 0;
+                const bool has_r = !WORD || (FULL && k + 1 < SEG) || p + 1 < L;
+                r = line_residual_s<WORD, RES>(prev, cur, nxt, gs, o, vv, has_l, has_r);
+            }
+            x[k] = r;
+            prev = cur;
+            cur = nxt;
+        }
+    }
+    // ---- T'^-1 r' by Thomas, segmented over NSEG lanes ----------------------
+    // With c_p = gw / pivot_p:  y_p = c_p r'_p + c_p y_{p-1},  d_p = y_p + c_p d_{p+1}.
+    // A segment maps its incoming value v to (prod_seg c) v + (result with
+    // v = 0); the product is a tile constant (segprod).  Padding nodes carry
+    // c = 0 and r' = 0, which breaks both chains at the line end; the first
+    // segment's incoming y and the last segment's incoming d are zero.
+    float c[SEG];
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) c[k] = cm[k * T + tid];
+    const float C = segprod[tid];
+    float Y = 0.f;
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) {
+        x[k] *= c[k];
+        Y = fmaf(c[k], Y, x[k]);
+    }
+    float Ci = C, Yi = Y;
+#pragma unroll
+    for (int off = 1; off < NSEG; off <<= 1) {
+        const float Cp = __shfl_up_sync(0xffffffffu, Ci, LPW * off);
+        const float Yp = __shfl_up_sync(0xffffffffu, Yi, LPW * off);
+        if (s >= off) {
+            Yi = fmaf(Ci, Yp, Yi);
+            Ci *= Cp;
+        }
+    }
+    float y = __shfl_up_sync(0xffffffffu, Yi, LPW);
+    if (s == 0) y = 0.f;
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) {
+        y = fmaf(c[k], y, x[k]);
+        x[k] = y;
+    }
+    float X = 0.f;
+#pragma unroll
+    for (int k = SEG - 1; k >= 0; --k) X = fmaf(c[k], X, x[k]);
+    Ci = C;
+    float Xi = X;
+#pragma unroll
+    for (int off = 1; off < NSEG; off <<= 1) {
+        const float Cn = __shfl_down_sync(0xffffffffu, Ci, LPW * off);
+        const float Xn = __shfl_down_sync(0xffffffffu, Xi, LPW * off);
+        if (s + off < NSEG) {
+            Xi = fmaf(Ci, Xn, Xi);
+            Ci *= Cn;
+        }
+    }
+    X = __shfl_down_sync(0xffffffffu, Xi, LPW);
+    if (s == NSEG - 1) X = 0.f;
+#pragma unroll
+    for (int k = SEG - 1; k >= 0; --k) {
+        X = fmaf(c[k], X, x[k]);
+        x[k] = X;
+    }
+    // ---- apply the correction ----------------------------------------------
+    // (a NaN correction is not seen by fmaxf; the output stage flags it)
+    float dm = 0.f;
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) {
+        const int p = p0 + k;
+        if (FULL || (line_ok && p < L)) {
+            const int q = qk(k);
+            const float nv = ZOWN ? omega * x[k] : fmaf(omega, x[k], own[q]);
+            own[q] = nv;
+            dm = fmaxf(dm, fabsf(x[k]));
+            vmax = fmaxf(vmax, fabsf(nv));
+        }
+    }
+    dmax = fmaxf(dmax, omega * dm);
+}
+
+// Chain multipliers gw / pivot of every line of the tile (pivots in FP64),
+// written in the order each pass thread reads them (k * T + tid), and the
+// product of each segment's multipliers as the pass forms it.
+template <int LD>
+__device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ piv, int n, int m, float gwf) {
+    constexpr int SEG = LineCfg<LD>::SEG;
+    constexpr int T = LineCfg<LD>::T;
+    constexpr int LPW = LineCfg<LD>::LPW;
+    const double gw = gwf;
+    const int tid = threadIdx.x;
+    if (tid < 2 * LD) {
+        const bool word = tid < LD;
+        const int line = word ? tid : tid - LD;
+        const int L = word ? m : n;
+        const int NL = word ? n : m;
+        float *dst = word ? piv : piv + SEG * T;
+        float *prod = piv + 2 * SEG * T + (word ? 0 : T);
+        const int tw_base = (line / LPW) * 32 + (line % LPW);
+        double p = 1.0, ipv_prev = 0.0;
+        float seg_prod = 1.f;
+        for (int q = 0; q < LD; ++q) {
+            double ipv = 0.0;
+            if (line < NL && q < L) {
+                const double g = word ? Gs[swz<LD>(line, q)] : Gs[swz<LD>(q, line)];
+                // wordline: source link + right link (absent at the end) + cell
+                // bitline:  upper link (absent at the top) + lower link + cell
+                const double diag = word ? gw + (q + 1 < L ? gw : 0.0) + g : (q > 0 ? gw : 0.0) + gw + g;
+                p = (q == 0) ? diag : fma(-gw * gw, ipv_prev, diag);
+                // 1/p: correctly rounded FP32 reciprocal refined by one Newton
+                // step in FP64 (~1e-14 relative; FP64 division is slow here)
+                const double r0 = (double)__frcp_rn((float)p);
+                ipv = r0 * fma(-p, r0, 2.0);
+                ipv_prev = ipv;
+            }
+            const int tw = tw_base + (q / SEG) * LPW;
+            const float cf = (float)(gw * ipv);
+            dst[(q % SEG) * T + tw] = cf;
+            seg_prod *= cf;
+            if (q % SEG == SEG - 1) {
+                prod[tw] = seg_prod;
+                seg_prod = 1.f;
+            }
+        }
+    }
+}
+
+// One iteration: every wordline, then every bitline.  ZERO: both planes are
+// still zero (first iteration from the ideal state).
+template <int LD, int RES, bool NL, bool FULL, bool ZERO>
+__device__ __forceinline__ void line_iteration(float *U, float *D, const float *Gs, const float *vin_s,
+                                               const float *piv, int n, int m, float inv_gw, float omega,
+                                               float &dmax, float &vmax, const SolveCtl &ctl) {
+    constexpr int SEG = LineCfg<LD>::SEG;
+    constexpr int T = LineCfg<LD>::T;
+    line_pass<LD, true, RES, NL, FULL, ZERO, ZERO>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, inv_gw, omega,
+                                                   dmax, vmax, ctl);
+    __syncthreads();
+    line_pass<LD, false, RES, NL, FULL, ZERO, false>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m,
+                                                     inv_gw, omega, dmax, vmax, ctl);
+}
+
+// Largest of one value per thread, the same in every thread (two barriers).
+template <int NW>
+__device__ __forceinline__ float block_max(float v, float *scratch) {
+    v = warp_max(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = v;
+    __syncthreads();
+    return warp_max((threadIdx.x & 31) < NW ? scratch[threadIdx.x & 31] : 0.f);
+}
+
+// Outputs of one solve: both planes or cell voltages (ret_V), else the bitline
+// currents I_j = sum_i g_ij (u_ij - d_ij) in the bitline mapping, in the I/O type.
+template <int LD, typename TIO, bool NL>
+__device__ __forceinline__ void line_outputs(const SolveArgs &a, const float *Gs, const float *U, const float *D,
+                                             const float *vin_s, int n, int m, int b, int x, int y, float gw,
+                                             int &nonfinite_flag) {
+    constexpr int T = LineCfg<LD>::T;
+    constexpr int SEG = LineCfg<LD>::SEG;
+    const int tid = threadIdx.x;
+    TIO *out = static_cast<TIO *>(a.out);
+    const int ldG = a.numY * m;
+    if (a.ret_V) {
+        for (int e = tid; e < n * m; e += T) {
+            const int i = e / m, j = e - i * m;
+            const int q = swz<LD>(i, j);
+            const TIO uu = (TIO)U[q] + (TIO)vin_s[vpad(i)];
+            const size_t sol = ((size_t)b * a.numX + x) * a.numY + y;
+            if (!isfinite((float)uu) || !isfinite(D[q])) nonfinite_flag = 1;
+            if (a.ret_V == 2) {
+                out[(sol * 2 + 0) * n * m + (size_t)i * m + j] = uu;
+                out[(sol * 2 + 1) * n * m + (size_t)i * m + j] = (TIO)D[q];
+            } else {
+                out[(sol * n + i) * m + j] = uu - (TIO)D[q];
+            }
+        }
+    } else {
+        constexpr int LPW = LineCfg<LD>::LPW;
+        const int lane = tid & 31;
+        const int s = lane / LPW;
+        const int j = (tid >> 5) * LPW + (lane % LPW);
+        TIO acc = 0;
+        if (j < m) {
+            for (int k = 0; k < SEG; ++k) {
+                const int i = s * SEG + k;
+                if (i < n) {
+                    const int q = swz<LD>(i, j);
+                    const TIO V = ((TIO)U[q] + (TIO)vin_s[vpad(i)]) - (TIO)D[q];
+                    TIO Ic = (TIO)(NL ? nl_geff(Gs[q], (float)V, a.ctl) : Gs[q] * gw) * V;
+                    if (a.ctl.noise_sigma > 0.f)
+                        Ic *= (TIO)1 + (TIO)(a.ctl.noise_sigma *
+                                             normal_from(a.ctl.noise_seed,
+                                                         ((unsigned long long)b * a.numX + x) * a.numY + y,
+                                                         (unsigned long long)i * m + j));
+                    acc += Ic;
+                }
+            }
+        }
+#pragma unroll
+        for (int off = LPW; off < 32; off <<= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        if (s == 0 && j < m) out[((size_t)b * a.numX + x) * ldG + (size_t)y * m + j] = acc;
+        if (s == 0 && j < m && !isfinite((float)acc)) nonfinite_flag = 1;
+    }
+}
+
+template <int LD, bool NL, bool FULL>
+__global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_kernel(SolveArgs a) {
+    constexpr int T = LineCfg<LD>::T;
+    constexpr int NW = LineCfg<LD>::NW;
+    constexpr int SEG = LineCfg<LD>::SEG;
+    extern __shared__ float4 smem4[];
+    float *Gs = reinterpret_cast<float *>(smem4);
+    float *U = Gs + LD * LD;
+    float *D = U + LD * LD;
+    float *vin_s = D + LD * LD;
+    float *red = vin_s + LD + LD / 16;  // [2][2][NW]
+    __shared__ int nonfinite_flag;
+    __shared__ float bmax_scratch[NW];
+
+    const int tid = threadIdx.x;
+    const int n = FULL ? LD : a.n, m = FULL ? LD : a.m;
+    const int ldG = a.numY * m;
+    const bool f64 = a.f64 != 0;
+    float *piv = a.scratch + (size_t)blockIdx.x * (2 * SEG * T + 2 * T);
+    const float gw = a.gw;
+    const float inv_gw = 1.f / gw;
+    const float tol = a.ctl.tol_v;
+    const int kres = a.ctl.residual_period;
+    const int maxit = a.ctl.max_iters;
+    const bool ff = a.ctl.residual_ff != 0;  // precise residual in float-float instead of FP64
+    const bool precise_first = kres == 1;    // every iteration precise
+    long long cached_tile = -1;
+    float rate_hint = 0.f;                   // final rate of the previous vector of this tile
+    float gs_max = 0.f;                      // largest g / gw of the tile (linear cells)
+    __shared__ unsigned long long st_solves, st_iters;  // this CTA's counters (thread 0)
+    __shared__ int st_max, st_or;
+    if (tid == 0) {
+        st_solves = 0;
+        st_iters = 0;
+        st_max = 0;
+        st_or = 0;
+    }
+
+    for (long long item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+        const long long tile = item / a.nchunks;
+        const int chunk = (int)(item % a.nchunks);
+        const int x = (int)(tile / a.numY), y = (int)(tile % a.numY);
+        const int b0 = chunk * a.vchunk;
+        const int b1 = min(a.B, b0 + a.vchunk);
+        if (tile != cached_tile) {
+            __syncthreads();
+            for (int e = tid; e < n * m; e += T) {
+                const int i = e / m, j = e - i * m;
+                Gs[swz<LD>(i, j)] = load_io(a.G, ((size_t)x * n + i) * ldG + (size_t)y * m + j, f64);
+            }
+            __syncthreads();
+            line_pivots<LD>(Gs, piv, n, m, gw);
+            __syncthreads();
+            if (!NL) {
+                // the passes work in units of gw: g / gw
+                float gm = 0.f;
+                for (int e = tid; e < n * m; e += T) {
+                    const int i = e / m, j = e - i * m;
+                    const float gsv = __fdiv_rn(Gs[swz<LD>(i, j)], gw);
+                    Gs[swz<LD>(i, j)] = gsv;
+                    gm = fmaxf(gm, fabsf(gsv));
+                }
+                gs_max = block_max<NW>(gm, bmax_scratch);
+            }
+            if (NL) {
+                // the sinh cells keep their on/off position; the linear values served the pivots
+                for (int e = tid; e < n * m; e += T) {
+                    const int i = e / m, j = e - i * m;
+                    Gs[swz<LD>(i, j)] = nl_z(Gs[swz<LD>(i, j)], a.ctl);
+                }
+                __syncthreads();
+            }
+            cached_tile = tile;
+            rate_hint = 0.f;
+        }
+        for (int b = b0; b < b1; ++b) {
+            __syncthreads();
+            // warm start: initial deviation planes [2][n][m] of this solve.  From
+            // the ideal state the planes are zero: the first iteration is then a
+            // ZERO iteration that reads neither plane, unless every iteration must
+            // be precise (the planes are cleared instead).
+            bool warm = a.init != nullptr;
+            bool zero = !warm && !precise_first;
+            if (!warm && precise_first) {
+                for (int e = tid; e < LD * LD; e += T) {
+                    U[e] = 0.f;
+                    D[e] = 0.f;
+                }
+            }
+            float vabs = 0.f;
+            if (tid < LD) {
+                const float v = (tid < n) ? load_io(a.input, ((size_t)b * a.numX + x) * n + tid, f64) : 0.f;
+                vin_s[vpad(tid)] = v;
+                vabs = fabsf(v);
+            }
+            // precise iterations may keep the cell term in FP32 (RES 3) when its
+            // rounding, amplified by at most L^2/2 through a line solve, stays 8x
+            // under the tolerance: per node <= gs_max * 3 vin_max * 2^-23
+            const float vin_max = block_max<NW>(vabs, bmax_scratch);
+            const float Lmax = (float)max(n, m);
+            const bool semi = !NL && ff &&
+                              gs_max * 3.f * vin_max * 1.1920929e-07f * 0.5f * Lmax * Lmax <= 0.125f * tol;
+            if (warm) {
+                const float *w0 = a.init + (((size_t)b * a.numX + x) * a.numY + y) * 2 * n * m;
+                for (int e = tid; e < n * m; e += T) {
+                    const int i = e / m, j = e - i * m;
+                    U[swz<LD>(i, j)] = w0[e];
+                    D[swz<LD>(i, j)] = w0[(size_t)n * m + e];
+                }
+                __syncthreads();
+            }
+            LineStop stop;
+            stop.init(a.ctl.omega, rate_hint);
+            float omega = stop.omega;
+            bool res64 = precise_first;
+            int status = 0, it = 0, par = 0;
+            while (true) {
+                float dmax = 0.f, vmax = 0.f;
+                if (zero) line_iteration<LD, 0, NL, FULL, true>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else if (!res64) line_iteration<LD, 0, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else if (semi) line_iteration<LD, 3, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else if (ff) line_iteration<LD, 2, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                else line_iteration<LD, 1, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                zero = false;
+                dmax = warp_max(dmax);
+                vmax = warp_max(vmax);
+                if ((tid & 31) == 0) {
+                    red[(par * 2 + 0) * NW + (tid >> 5)] = dmax;
+                    red[(par * 2 + 1) * NW + (tid >> 5)] = vmax;
+                }
+                __syncthreads();
+                // every warp reduces the NW partial maxima itself (no second barrier)
+                const int ln = tid & 31;
+                float delta = warp_max(ln < NW ? red[(par * 2 + 0) * NW + ln] : 0.f);
+                float vm = warp_max(ln < NW ? red[(par * 2 + 1) * NW + ln] : 0.f);
+                par ^= 1;
+                ++it;
+                if (!isfinite(delta) || !isfinite(vm)) {
+                    status |= FADESIM_ST_NONFINITE;
+                    break;
+                }
+                if (warm && it == 1 && !(delta < vm)) {
+                    // the prediction moved as much as the solution is large: discard
+                    // it and start again from the ideal state
+                    __syncthreads();
+                    if (precise_first) {
+                        for (int e = tid; e < LD * LD; e += T) {
+                            U[e] = 0.f;
+                            D[e] = 0.f;
+                        }
+                        __syncthreads();
+                    }
+                    zero = !precise_first;
+                    warm = false;
+                    status |= FADESIM_ST_WARM_REJECTED;
+                    stop.init(a.ctl.omega, rate_hint);
+                    omega = stop.omega;
+                    res64 = precise_first;
+                    continue;
+                }
+                const bool small = stop.update(delta, vm, tol);
+                omega = stop.omega;
+                if (small) {
+                    // the final test must pass on an iteration whose residual was
+                    // FP64 (kres < 0: FP32 only, the FP32 test is final)
+                    if (res64 || kres < 0) {
+                        status |= FADESIM_ST_CONVERGED;
+                        break;
+                    }
+                    res64 = true;
+                } else {
+                    // kres 0: adaptive (precise when the next iteration should be
+                    // the last or nears the FP32 residual noise); k > 0: every k
+                    res64 = kres > 0 ? (it % kres == 0) : (kres == 0 && stop.want_precise(tol, vm));
+                }
+                if (it >= maxit) {
+                    status |= FADESIM_ST_MAXITER;
+                    break;
+                }
+            }
+            rate_hint = stop.final_rate();
+            // ---- outputs ------------------------------------------------------
+            if (tid == 0) nonfinite_flag = 0;
+            __syncthreads();
+            if (f64) line_outputs<LD, double, NL>(a, Gs, U, D, vin_s, n, m, b, x, y, gw, nonfinite_flag);
+            else line_outputs<LD, float, NL>(a, Gs, U, D, vin_s, n, m, b, x, y, gw, nonfinite_flag);
+            __syncthreads();
+            if (nonfinite_flag) status |= FADESIM_ST_NONFINITE;
+            if (tid == 0) {
+                if (a.iters_out) a.iters_out[((long long)b * a.numX + x) * a.numY + y] = it;
+                st_solves += 1;
+                st_iters += it;
+                st_max = max(st_max, it);
+                st_or |= status;
+            }
+        }
+    }
+    __syncthreads();
+    if (tid == 0 && a.stats && st_solves) {
+        atomicAdd(&a.stats->solves, st_solves);
+        atomicAdd(&a.stats->iters_sum, st_iters);
+        atomicMax(&a.stats->iters_max, st_max);
+        atomicOr(&a.stats->status_or, st_or);
+    }
+}
+
+// Launch helpers for one tile size (instantiated by linegs_<LD>.cu).
+// Instantiations: linear cells on any tile, linear cells on a full LD x LD
+// tile, sinh cells on any tile.
+inline size_t line_relax_smem_ld(int ld, int nw) { return (size_t)(3 * ld * ld + ld + ld / 16 + 4 * nw) * sizeof(float); }
+
+template <int LD>
+cudaError_t line_relax_prepare_t() {
+    const int sm = (int)line_relax_smem_ld(LD, LineCfg<LD>::NW);
+    cudaError_t e = cudaFuncSetAttribute(line_relax_kernel<LD, false, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(line_relax_kernel<LD, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(line_relax_kernel<LD, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    return e;
+}
+
+template <int LD>
+cudaError_t line_relax_occupancy_t(int *n) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(n, line_relax_kernel<LD, false, false>, LineCfg<LD>::T,
+                                                         line_relax_smem_ld(LD, LineCfg<LD>::NW));
+}
+
+template <int LD>
+cudaError_t launch_line_relax_t(const SolveArgs &a, int grid, cudaStream_t st) {
+    const size_t sm = line_relax_smem_ld(LD, LineCfg<LD>::NW);
+    if (a.ctl.nl) line_relax_kernel<LD, true, false><<<grid, LineCfg<LD>::T, sm, st>>>(a);
+    else if (a.n == LD && a.m == LD) line_relax_kernel<LD, false, true><<<grid, LineCfg<LD>::T, sm, st>>>(a);
+    else line_relax_kernel<LD, false, false><<<grid, LineCfg<LD>::T, sm, st>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace fadesim

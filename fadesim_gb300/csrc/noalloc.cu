@@ -109,6 +109,7 @@ extern "C" int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G
     a.numY = numY;
     a.gw = (float)g_wire;
     a.ret_V = 0;
+    a.f64 = 0;
     a.ctl.tol_v = 1e-8f;
     a.ctl.max_iters = 400;
     a.ctl.residual_period = 0;  // adaptive, as the default of the allocating entry

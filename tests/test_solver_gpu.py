@@ -192,21 +192,24 @@ def test_nonfinite_input_reports_status(acc):
 
 
 @pytest.mark.parametrize("tol", [5e-7, 1e-8])
-@pytest.mark.parametrize("cells,n", [("cfg1", 128), ("cfg1", 64), ("strong", 64)])
+@pytest.mark.parametrize("cells,n", [("cfg1", 128), ("cfg1", 64), ("strong", 64), ("cfg1", 256), ("strong", 256),
+                                     ("cfg1", 512)])
 def test_precision_schedule_meets_tolerance(acc, tol, cells, n):
     """The adaptive schedule (FP32 residuals, a precise one on the last
     iteration, per-tile choice of the cheaper precise form, rate carried between
     the vectors of a tile) against the FP64 oracle, with many vectors per work
-    item as in a throughput run; float64 I/O so the planes come back unrounded."""
-    B, X, Y = 24, 2, 1
+    item as in a throughput run; float64 I/O so the planes come back unrounded.
+    256 and 512 run on the cluster kernels."""
+    B, X, Y = (24, 2, 1) if n <= 128 else (6, 1, 1)
     inp, G = make_case(21 + n, B, X, Y, n, n, CFG1 if cells == "cfg1" else STRONG, 0.2 if cells == "cfg1" else 1.0)
     _, U, D = oracle_planes(inp, G, B, X, Y, n, n)
     got, st, _ = run(acc, inp, G, B, X, Y, n, n, dtype=torch.float64, method="line", tol_v=tol, vectors_per_cta=B)
     assert st["status_or"] == 1
-    # the stop test's floor: 4 ulps of the largest deviation (FP32 planes),
-    # ~1e-9 V for weak cells (1e-2 V drops), ~4e-7 V for strong ones (0.9 V)
+    # the stop test floors at 4 ulps of the largest deviation (FP32 planes); the
+    # error there is within ~8 ulps:
+    # ~1e-9 V for weak cells (1e-2 V drops), ~8e-7 V for strong ones (0.9 V)
     dev = max(np.abs(U - inp.reshape(B, X, 1, n, 1)).max(), np.abs(D).max())
-    floor = max(2e-9, 4 * 2.0 ** -23 * dev)
+    floor = max(2e-9, 8 * 2.0 ** -23 * dev)
     err = max(np.abs(got[:, :, :, 0] - U).max(), np.abs(got[:, :, :, 1] - D).max())
     assert err <= tol + floor, (err, st)
     # the every-iteration float-float schedule agrees with it to the same tolerance
