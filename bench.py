@@ -44,6 +44,12 @@ UNIT = "solves/s"
 # algorithmic HBM bytes per solve: G amortised over the tile's vectors, the
 # input vector and the output currents, FP32
 BYTES_PER_SOLVE = (ROWS * COLS * 4) / N_VEC + ROWS * 4 + COLS * 4
+# algorithmic shared-memory bytes per node update of a line pass: the node's own
+# value read for the residual and again for the update, one write, the other
+# plane's node, the cell conductance, and the input voltage on bitline passes
+SMEM_BYTES_PER_NODE_UPDATE = 4 * (2 + 1 + 1 + 1 + 0.5)
+SMEM_BYTES_PER_CLK_SM = 128  # shared-memory bandwidth per SM per clock (32 banks x 4 B)
+N_SMS = 152
 
 
 def peaks():
@@ -163,7 +169,7 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def mixed_batch(torch, n_tiles=4096, n_vec=64, seed=2, steps=3):
+def mixed_batch(torch, tol, n_tiles=4096, n_vec=64, seed=2, steps=3):
     """4096 tiles with sizes drawn uniformly from {64, 128, 256}^2 (square), 64
     Bernoulli 0.2 V vectors each, one CUDA-graph replay per step."""
     from fadesim_gb300.batched import TileBatch, TileGroup
@@ -176,7 +182,7 @@ def mixed_batch(torch, n_tiles=4096, n_vec=64, seed=2, steps=3):
         G = torch.from_numpy((1.0 / R_STATES)[states].astype(np.float32)).cuda()
         v = torch.from_numpy((rng.integers(0, 2, (n_vec, T, n)) * V_READ).astype(np.float32)).cuda()
         groups.append(TileGroup(G, v))
-    batch = TileBatch(groups, g_wire=1 / R_WIRE, tuned=False)
+    batch = TileBatch(groups, g_wire=1 / R_WIRE, tol_v=tol, tuned=False)
     st = batch.run(stats=True)
     batch.capture()
     batch.replay()
@@ -190,6 +196,7 @@ def mixed_batch(torch, n_tiles=4096, n_vec=64, seed=2, steps=3):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / steps
     return {"workload": "4096 tiles, sizes uniform in {64,128,256}^2, 64 vectors each, one CUDA graph",
+            "tol_v": tol,
             "tiles_by_size": {str(g.n): g.T for g in groups}, "solves_per_step": batch.solves,
             "ms_per_step": ms, "solves_per_s": batch.solves / (ms / 1e3),
             "nodes_per_s": sum(g.solves * 2 * g.n * g.n for g in groups) / (ms / 1e3),
@@ -344,7 +351,7 @@ def run_ours(args):
         variants[vname + "_solves_per_s"] = solves_per_step / (v0.elapsed_time(v1) / 1e3)
 
     # the mixed-size batch (tiles of 64, 128 and 256)
-    mixed = mixed_batch(torch) if not args.no_mixed else None
+    mixed = mixed_batch(torch, args.tol) if not args.no_mixed else None
     large = large_nonideal(torch, acc) if not args.no_mixed else None
     warm = None
     if not args.no_warm:
@@ -369,6 +376,10 @@ def run_ours(args):
     hbm_peak, peak_kind = peaks()
     achieved = BYTES_PER_SOLVE * solves_per_step / (kern_ms / 1e3) / 1e9
     traffic = profiled_traffic()
+    clk = clk_summary = clk.summary()
+    node_updates = stats["iters_sum"] / max(1, stats["solves"]) * 2 * ROWS * COLS * solves_per_step
+    smem_achieved = SMEM_BYTES_PER_NODE_UPDATE * node_updates / (kern_ms / 1e3) / 1e9
+    smem_peak = SMEM_BYTES_PER_CLK_SM * N_SMS * (clk_summary.get("sm_mhz") or 2070.0) * 1e6 / 1e9
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -392,11 +403,17 @@ def run_ours(args):
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "traffic": traffic * solves_per_step if traffic else None,
                      "algorithmic_bytes_per_launch": BYTES_PER_SOLVE * solves_per_step,
-                     "kernel": "line_relax_kernel<128,float>", "kernel_ms": kern_ms},
+                     "kernel": "line_relax_kernel<128,NL=0,FULL=1>", "kernel_ms": kern_ms,
+                     "smem": {"achieved": smem_achieved, "peak": smem_peak, "unit": "GB/s",
+                              "frac": smem_achieved / smem_peak, "peak_kind": "nominal 128 B/clk/SM at the sampled clock",
+                              "bytes_per_node_update": SMEM_BYTES_PER_NODE_UPDATE,
+                              "node_updates_per_launch": node_updates},
+                     "note": "HBM carries only G, inputs and currents; the line passes run on shared-memory "
+                             "planes and are bound by instruction issue (see profiles/)"},
         "e2e": {"value": e2e_value, "unit": UNIT,
                 "h2d_bytes_per_step": int(G.nbytes + vin.nbytes), "d2h_bytes_per_step": int(hout.numel() * 4)},
         "gpu_launches": args.steps,
-        "clocks": clk.summary(),
+        "clocks": clk_summary,
     }
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline()

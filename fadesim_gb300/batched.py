@@ -34,11 +34,11 @@ class TileGroup:
 class TileBatch:
     """Several TileGroups solved together (one group per shape)."""
 
-    def __init__(self, groups, g_wire=1 / 2.93, method="line", tol_v=1e-8, residual="ff", tuned=True):
+    def __init__(self, groups, g_wire=1 / 2.93, method="line", tol_v=None, residual="ff", tuned=True):
         self.groups = list(groups)
         self.g_wire = g_wire
         self.method = method
-        self.tol_v = tol_v
+        self.tol_v = tol_v  # None: the module-wide cpp_ir_drop_accelerate.options.tol_v
         self.residual = residual
         self.tuned = tuned
         self.streams = [torch.cuda.Stream() for _ in self.groups]
