@@ -204,10 +204,10 @@ def mixed_batch(torch, tol, n_tiles=4096, n_vec=64, seed=2, steps=3):
             "status_or": int(np.bitwise_or.reduce([s["status_or"] for s in st]))}
 
 
-def large_nonideal(torch, acc, n_tiles=64, n_vec=32, seed=5):
-    """512x512 tiles on 16-CTA clusters with sinh cells I = (V/R) sinh(2V)/(2V),
-    lognormal R variation (sigma 0.1), 1% Gaussian read noise, 32 inputs per tile
-    uniform in [0, 0.2] V: a bounded sample of the 1024-tile configuration."""
+def large_nonideal(torch, acc, n_tiles=1024, n_vec=32, seed=5):
+    """1024 tiles of 512x512 on 16-CTA clusters with sinh cells I = (V/R)
+    sinh(2V)/(2V), lognormal R variation (sigma 0.1), 1% Gaussian read noise, 32
+    inputs per tile uniform in [0, 0.2] V."""
     from fadesim_gb300.variation import add_variation_device
     rng = np.random.default_rng(seed)
     n = 512
@@ -353,6 +353,11 @@ def run_ours(args):
     # the mixed-size batch (tiles of 64, 128 and 256)
     mixed = mixed_batch(torch, args.tol) if not args.no_mixed else None
     large = large_nonideal(torch, acc) if not args.no_mixed else None
+    # the layer-level MLP inference (PimTorch Linear_sp path on crossbars)
+    mlp = None
+    if not args.no_mixed:
+        from fadesim_gb300 import mlp_eval
+        mlp = mlp_eval.evaluate(256)
     warm = None
     if not args.no_warm:
         from fadesim_gb300.warmstart_eval import train_and_evaluate
@@ -398,7 +403,7 @@ def run_ours(args):
                    "plain_rbsor_solves_per_s": rb_value,
                    "plain_rbsor_sweeps_mean": rb_stats["iters_sum"] / max(1, rb_stats["solves"]),
                    "speedup_vs_plain_rbsor": value / world / rb_value, **variants,
-                   "mixed_sizes": mixed, "large_nonideal": large, "learned_warm_start": warm},
+                   "mixed_sizes": mixed, "large_nonideal": large, "mlp_layers": mlp, "learned_warm_start": warm},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_kind": peak_kind,
                      "traffic": traffic * solves_per_step if traffic else None,
@@ -431,7 +436,7 @@ def main():
     ap.add_argument("--tiles", type=int, default=N_TILES, help="128x128 tiles per rank (64 vectors each)")
     ap.add_argument("--tol", type=float, default=TOL_V, help="stop tolerance, estimated max node error (V)")
     ap.add_argument("--no-mixed", action="store_true",
-                    help="skip the mixed-size (64/128/256) and large non-ideal (512) figures")
+                    help="skip the mixed-size (64/128/256), large non-ideal (512) and MLP-layer figures")
     ap.add_argument("--no-warm", action="store_true", help="skip training/evaluating the learned warm start")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident solve only (no e2e, comparator or CPU baseline); for profiling")

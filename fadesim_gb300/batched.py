@@ -34,14 +34,18 @@ class TileGroup:
 class TileBatch:
     """Several TileGroups solved together (one group per shape)."""
 
-    def __init__(self, groups, g_wire=1 / 2.93, method="line", tol_v=None, residual="ff", tuned=True):
+    def __init__(self, groups, g_wire=1 / 2.93, method="line", tol_v=None, residual="ff", tuned=True,
+                 concurrent=True):
         self.groups = list(groups)
         self.g_wire = g_wire
         self.method = method
         self.tol_v = tol_v  # None: the module-wide cpp_ir_drop_accelerate.options.tol_v
         self.residual = residual
         self.tuned = tuned
-        self.streams = [torch.cuda.Stream() for _ in self.groups]
+        # concurrent: one forked stream per group; else the groups run one after
+        # another on the caller's stream, largest tiles first
+        self.concurrent = concurrent
+        self.streams = [torch.cuda.Stream() for _ in self.groups] if concurrent else None
         self.graph = None
 
     @property
@@ -59,6 +63,10 @@ class TileBatch:
     def run(self, stats=False):
         """Solve every group; returns the per-group stats when ``stats``."""
         main = torch.cuda.current_stream()
+        if not self.concurrent:
+            order = sorted(range(len(self.groups)), key=lambda i: -self.groups[i].n * self.groups[i].m)
+            res = {i: self._launch(self.groups[i], main, stats) for i in order}
+            return [res[i] for i in range(len(self.groups))] if stats else None
         ev = torch.cuda.Event()
         ev.record(main)
         out = []

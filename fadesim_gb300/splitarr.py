@@ -90,14 +90,57 @@ def quantize(x, bit_width, pn):
     return q, s
 
 
-def default_solver(cfg):
+def default_solver(cfg, tol_v=None):
+    """The IR-drop solve of the drop-in module with the array's parameters
+    (tol_v None: the module-wide option)."""
     def solve(v, G, B, rows, cols, numX, numY, out):
         return _acc.ir_drop_gs_ex(v, G, B, rows, cols, numX, numY, iter_times=cfg.ir_drop_iter_time,
                                   g_wire=1 / cfg.r_wire, beta=cfg.ir_drop_GS_method_beta_scale,
                                   enable_break=cfg.ir_drop_less_than_thresholdBreak_enable,
                                   break_threshould=cfg.ir_drop_less_than_threshold,
                                   nonlinear_cell_enable=cfg.nonlinear_cell_enable,
-                                  nonlinear_params=cfg.nonlinear_params, return_stats=False, out=out)[0]
+                                  nonlinear_params=cfg.nonlinear_params, tol_v=tol_v, return_stats=False,
+                                  out=out)[0]
+    return solve
+
+
+def superposition_solver(cfg):
+    """IR-drop currents by linearity, for linear cells without read noise.
+
+    The bitline currents of a tile are then a linear map of its wordline
+    voltages, I = V M, M [rows, numY*cols] the tile's effective conductance
+    matrix.  M comes from one solver call with ``rows`` unit vectors per tile
+    (row r driven at the DAC level inputV, the others at 0 V), and every input
+    vector's currents are one FP32 matrix product: rows solves per tile instead
+    of one per vector, exact up to the solver tolerance.  A vector's currents
+    sum up to ``rows`` unit responses, so these are solved 500x tighter than the
+    module tolerance (down to the FP32 floor of the planes).  Used with the same
+    (v, G, B, rows, cols, numX, numY, out) interface as ``default_solver``; calls
+    with no more vectors than rows solve directly."""
+    direct = default_solver(cfg)
+    if getattr(cfg, "nonlinear_cell_enable", False):
+        raise ValueError("superposition needs linear cells: nonlinear (sinh) cells are not a linear map")
+
+    def solve(v, G, B, rows, cols, numX, numY, out):
+        if B <= rows:
+            return direct(v, G, B, rows, cols, numX, numY, out)
+        if _acc.options.read_noise_sigma > 0:
+            raise ValueError("superposition needs noise-free cells: read noise is not a linear map")
+        lv = float(v.abs().max().item()) or 1.0  # unit drive level: the largest input voltage
+        unit = torch.zeros((rows, numX, rows), dtype=v.dtype, device=v.device)
+        r = torch.arange(rows, device=v.device)
+        unit[r, :, r] = lv
+        M = default_solver(cfg, tol_v=_acc.options.tol_v * 2e-3)(unit, G, rows, rows, cols, numX, numY, None)
+        M = M.reshape(rows, numX, numY * cols).permute(1, 0, 2) * (1.0 / lv)
+        tf32 = torch.backends.cuda.matmul.allow_tf32
+        torch.backends.cuda.matmul.allow_tf32 = False  # full FP32 products
+        try:
+            res = torch.bmm(v.reshape(B, numX, rows).permute(1, 0, 2), M)  # [numX, B, numY*cols]
+        finally:
+            torch.backends.cuda.matmul.allow_tf32 = tf32
+        out = res.permute(1, 0, 2) if out is None else out.copy_(res.permute(1, 0, 2).reshape(out.shape))
+        return out
+
     return solve
 
 

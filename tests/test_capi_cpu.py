@@ -45,3 +45,10 @@ def test_argument_errors_without_gpu():
     assert rc == -1 and b"g_wire" in lib.fadesim_last_error()
     rc = lib.fadesim_ir_drop_gs_f32(None, fake, 1, 8, 8, 1, 1, 10, 0.34, 1.9, 0, 0.0, 0, None, 0, 0, fake, None)
     assert rc == -1
+
+
+def test_superposition_refuses_nonlinear_cells():
+    from fadesim_gb300 import splitarr
+    import pytest as _pt
+    with _pt.raises(ValueError):
+        splitarr.superposition_solver(splitarr.ArrayConfig(nonlinear_cell_enable=True))

@@ -147,3 +147,26 @@ def test_conv2d_sp_with_gpu_solver_matches_oracle(sa):
 
     ref = intstages.conv2d_sp(x, wgt, bias, p, padding=(1, 1), arr="Ref", solver=replay)
     assert np.array_equal(y.cpu().numpy(), ref)
+
+
+def test_superposition_solver_matches_direct(sa):
+    """Currents by linearity (unit responses of each tile, then one FP32 matrix
+    product) equal the direct per-vector solves to the solver tolerance."""
+    rng = np.random.default_rng(12)
+    cfg = sa.ArrayConfig(Ron=1e3, Roff=1e6, cellBits=2, arrRowSize=64, arrColSize=64, inputMaxVoltage=0.2)
+    B, numX, numY, n = 300, 2, 2, 64
+    states = rng.integers(0, 4, (numX, n, numY * n))
+    G = torch.tensor(states * cfg.cellDeltaConduct + cfg.cellMinConduct, dtype=torch.float32).cuda()
+    v = torch.tensor(rng.integers(0, 2, (B, numX, n)) * 0.2, dtype=torch.float32).cuda()
+    direct = sa.default_solver(cfg)(v, G, B, n, n, numX, numY, None)
+    sup = sa.superposition_solver(cfg)(v, G, B, n, n, numX, numY, torch.empty_like(direct))
+    assert (sup - direct).abs().max().item() <= 1e-5 * direct.abs().max().item()
+
+
+def test_mlp_layer_path_runs_both_strategies(sa):
+    """The layer-level MLP (784-512-512-10, 2-bit cells on 128x128 PN crossbars)
+    on a small batch: both solver strategies give nearly the same outputs."""
+    from fadesim_gb300 import mlp_eval
+    r = mlp_eval.evaluate(batch=20)   # 160 vectors per call: more than a tile's 128 rows
+    assert r["direct"]["solves_per_batch"] == sum(mlp_eval.solves_per_batch(20, mlp_eval.config()))
+    assert r["superposition"]["max_rel_current_diff_vs_direct"] < 1e-4   # the current contract
