@@ -52,6 +52,11 @@ EXPORTS = {
     "fadesim_map_conductance_ref_f32": [_vp] + [_i] * 10 + [ctypes.c_float, ctypes.c_float, _vp, _vp],
     "fadesim_adc_shift_add_ex_f32": [_vp] + [_i] * 7 + [ctypes.c_float] * 3 + [_i] * 5 + [ctypes.c_float, _vp, _i,
                                                                                          _vp, _vp],
+    "fadesim_ir2s": [_i, _vp, _vp] + [_i] * 6 + [_d, _i, _d, _i, _vp, _vp],
+    "fadesim_ir2s_ou_local": [_i, _vp, _vp] + [_i] * 6 + [_d, _d, _d, _i, _d, _vp, _vp],
+    "fadesim_ir2s_ou": [_i, _vp, _vp] + [_i] * 8 + [_d, _i, _d, _vp, _vp],
+    "fadesim_ir_gs_ou_local": [_i, _vp, _vp] + [_i] * 6 + [_d, _d, _d, _d, _i, _d, _vp, _vp],
+    "fadesim_ir_gs_ou": [_i, _vp, _vp] + [_i] * 8 + [_d, _d, _i, _d, _vp, _vp],
     "fadesim_noalloc_scratch_bytes": [],
     "fadesim_noalloc_last_error": [],
 }

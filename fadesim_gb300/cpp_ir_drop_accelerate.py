@@ -152,20 +152,82 @@ def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_tim
     return out, stats, it
 
 
-def _not_here(name, ref):
-    def f(*args, **kwargs):
-        raise NotImplementedError("%s (%s) is not implemented in this build; ir_drop_gs is" % (name, ref))
-    f.__name__ = name
-    return f
+def _family(cname, input, G, batch_size, row_size, col_size, numX, numY, out_rows, ret_V, nonlinear_cell_enable,
+            *cargs):
+    """Shared checks and launch of the IR2S / OU exports (their own iterates)."""
+    _check_input(input, "input")
+    _check_input(G, "G")
+    if row_size < 2:
+        raise RuntimeError("row_size should be >=2")
+    if col_size < 2:
+        raise RuntimeError("col_size should be >=2")
+    if input.dtype not in (torch.float32, torch.float64) or G.dtype != input.dtype:
+        raise RuntimeError("input and G must both be float32 or both float64")
+    if nonlinear_cell_enable:
+        raise NotImplementedError("%s with nonlinear cells is not implemented in this build; ir_drop_gs handles "
+                                  "them" % cname)
+    lib = _lib.load()
+    shape = (batch_size, numX, numY, row_size, col_size) if ret_V else (batch_size, out_rows, numY * col_size)
+    out = torch.empty(shape, dtype=input.dtype, device=input.device)
+    dtype = _lib.F64 if input.dtype == torch.float64 else _lib.F32
+    with torch.cuda.device(input.device):
+        stream = torch.cuda.current_stream(input.device).cuda_stream
+        rc = getattr(lib, "fadesim_" + cname)(dtype, input.data_ptr(), G.data_ptr(), *cargs, out.data_ptr(), stream)
+    _lib.check(rc)
+    return out
 
 
-# The reference module's other exports (split_arr_matmul.cu:1429-1437) belong to
-# the IR2S and OU solvers, which this build does not cover.
-ir2s = _not_here("ir2s", "split_arr_matmul.cu:419")
-ir2s_ou_local = _not_here("ir2s_ou_local", "split_arr_matmul.cu:565")
-ir2s_ou = _not_here("ir2s_ou", "split_arr_matmul.cu:953")
-ir_gs_ou_local = _not_here("ir_gs_ou_local", "split_arr_matmul.cu:690")
-ir_gs_ou = _not_here("ir_gs_ou", "split_arr_matmul.cu:1197")
+# The reference module's other exports (split_arr_matmul.cu:1429-1437): the IR2S
+# iteration and the operation-unit (OU) variants, reproducing their iterates.
+def ir2s(input, G, batch_size, row_size, col_size, numX, numY, iter_times, r_wire, enable_break, break_threshould,
+         nonlinear_cell_enable=False, nonlinear_params=(), ret_V=False):
+    """ir2s (split_arr_matmul.cu:419-545): the IR-drop-to-source iteration with
+    the wire resistance r_wire (also the source and ground loads)."""
+    return _family("ir2s", input, G, batch_size, row_size, col_size, numX, numY, numX, ret_V,
+                   nonlinear_cell_enable, batch_size, row_size, col_size, numX, numY, iter_times, float(r_wire),
+                   int(bool(enable_break)), float(break_threshould), int(bool(ret_V)))
+
+
+def ir2s_ou_local(input, G, batch_size, row_size, col_size, numX, numY, iter_times, r_wire, r_load_left,
+                  r_load_down, enable_break, break_threshould, nonlinear_cell_enable=False, nonlinear_params=()):
+    """ir2s_ou_local (split_arr_matmul.cu:565-680): ir2s of one OU-sized array
+    with source and ground load resistances."""
+    return _family("ir2s_ou_local", input, G, batch_size, row_size, col_size, numX, numY, numX, False,
+                   nonlinear_cell_enable, batch_size, row_size, col_size, numX, numY, iter_times, float(r_wire),
+                   float(r_load_left), float(r_load_down), int(bool(enable_break)), float(break_threshould))
+
+
+def ir2s_ou(input, G, batch_size, row_size, col_size, ou_row_size, ou_col_size, numX, numY, iter_times, r_wire,
+            enable_break, break_threshould, nonlinear_cell_enable=False, nonlinear_params=()):
+    """ir2s_ou (split_arr_matmul.cu:953-1084): every OU of the array at once, each
+    through the lumped wire outside it; currents per OU row group
+    [batch, numX * rows/ou_row_size, numY * cols]."""
+    return _family("ir2s_ou", input, G, batch_size, row_size, col_size, numX, numY,
+                   numX * (row_size // max(1, ou_row_size)), False, nonlinear_cell_enable, batch_size, row_size,
+                   col_size, ou_row_size, ou_col_size, numX, numY, iter_times, float(r_wire), int(bool(enable_break)),
+                   float(break_threshould))
+
+
+def ir_gs_ou_local(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, g_load_left,
+                   g_load_down, beta, enable_break, break_threshould, nonlinear_cell_enable=False,
+                   nonlinear_params=()):
+    """ir_gs_ou_local (split_arr_matmul.cu:690-813): the ir_drop_gs sweep of one
+    OU-sized array with source and ground load conductances."""
+    return _family("ir_gs_ou_local", input, G, batch_size, row_size, col_size, numX, numY, numX, False,
+                   nonlinear_cell_enable, batch_size, row_size, col_size, numX, numY, iter_times, float(g_wire),
+                   float(g_load_left), float(g_load_down), float(beta), int(bool(enable_break)),
+                   float(break_threshould))
+
+
+def ir_gs_ou(input, G, batch_size, row_size, col_size, ou_row_size, ou_col_size, numX, numY, iter_times, g_wire,
+             beta, enable_break, break_threshould, nonlinear_cell_enable=False, nonlinear_params=()):
+    """ir_gs_ou (split_arr_matmul.cu:1197-1310): the sweep on every OU of the
+    array at once; currents per OU row group [batch, numX * rows/ou_row_size,
+    numY * cols]."""
+    return _family("ir_gs_ou", input, G, batch_size, row_size, col_size, numX, numY,
+                   numX * (row_size // max(1, ou_row_size)), False, nonlinear_cell_enable, batch_size, row_size,
+                   col_size, ou_row_size, ou_col_size, numX, numY, iter_times, float(g_wire), float(beta),
+                   int(bool(enable_break)), float(break_threshould))
 
 
 def ir_drop_gs_warm(input, G, batch_size, row_size, col_size, numX, numY, init, g_wire=1 / 2.93, tol_v=None,

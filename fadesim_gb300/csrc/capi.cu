@@ -24,6 +24,10 @@ static int fail(int code, const std::string &msg) {
         if (e_ != cudaSuccess) return fail(FADESIM_E_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+namespace fadesim {
+int report_error(int code, const char *msg) { return fail(code, msg); }
+}  // namespace fadesim
+
 extern "C" const char *fadesim_last_error(void) { return g_err.c_str(); }
 extern "C" const char *fadesim_version(void) { return "fadesim_gb300 0.1 (sm_103a)"; }
 

@@ -26,6 +26,9 @@ struct SolveArgs {
     int f64;            // input, G and out are FP64 (else FP32); the solve itself is FP32
 };
 
+// Record msg as the message of fadesim_last_error() and return code.
+int report_error(int code, const char *msg);
+
 // Block line relaxation, planes resident in shared memory (n, m <= 128).
 // Returns the LD (32/64/128) used, or 0 if the shape does not fit.
 int line_relax_ld(int n, int m);

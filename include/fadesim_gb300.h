@@ -102,6 +102,36 @@ int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G, int batch
                           int n_nonlinear_params, int ret_V, void *out, const fadesim_solve_opts *opts,
                           fadesim_solve_stats *stats, int *per_solve_iters, void *stream);
 
+/* ---- the reference extension's other exports (split_arr_matmul.cu:1429-1437),
+ * reproducing their iterates: same arguments and meaning, dtype (FADESIM_F32 /
+ * FADESIM_F64) typing input, G and out; linear cells (nonlinear cells: ir_drop_gs).
+ * ou_* functions split every rows x cols tile into ou_row_size x ou_col_size
+ * operation units solved at once, each through the lumped wire outside it, and
+ * return currents per OU row group [batch, numX * rows / ou_row_size, numY * cols];
+ * the others return [batch, numX, numY * cols] (ir2s with ret_V: cell voltages
+ * [batch, numX, numY, rows, cols]). ---- */
+
+/* ir2s (split_arr_matmul.cu:419-545): IR-drop-to-source iteration, r_wire the wire and load resistance. */
+int fadesim_ir2s(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size, int numX,
+                 int numY, int iter_times, double r_wire, int enable_break, double break_threshould, int ret_V,
+                 void *out, void *stream);
+/* ir2s_ou_local (:565-680): ir2s with source and ground load resistances. */
+int fadesim_ir2s_ou_local(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
+                          int numX, int numY, int iter_times, double r_wire, double r_load_left, double r_load_down,
+                          int enable_break, double break_threshould, void *out, void *stream);
+/* ir2s_ou (:953-1084): ir2s on every OU at once. */
+int fadesim_ir2s_ou(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
+                    int ou_row_size, int ou_col_size, int numX, int numY, int iter_times, double r_wire,
+                    int enable_break, double break_threshould, void *out, void *stream);
+/* ir_gs_ou_local (:690-813): the ir_drop_gs sweep with source and ground load conductances. */
+int fadesim_ir_gs_ou_local(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
+                           int numX, int numY, int iter_times, double g_wire, double g_load_left, double g_load_down,
+                           double beta, int enable_break, double break_threshould, void *out, void *stream);
+/* ir_gs_ou (:1197-1310): the sweep on every OU at once. */
+int fadesim_ir_gs_ou(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
+                     int ou_row_size, int ou_col_size, int numX, int numY, int iter_times, double g_wire, double beta,
+                     int enable_break, double break_threshould, void *out, void *stream);
+
 /* ---- integer stages around the solve (bit-exact with the reference's float32
  * arithmetic given the same currents).  Device pointers, async on stream. ---- */
 

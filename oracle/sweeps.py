@@ -138,3 +138,120 @@ def ir_drop_gs_nonlinear(input_v, G, batch_size, row_size, col_size, numX, numY,
         cur_u, prev_u = prev_u, cur_u
         cur_d, prev_d = prev_d, cur_d
     return ((prev_u - prev_d) * g).sum(axis=3).reshape(B, X, Y * m)
+
+
+def ir_family(input_v, G, batch_size, row_size, col_size, numX, numY, iter_times, wire, mode, ou=None, loads=None,
+              beta=1.0, enable_break=False, break_threshold=0.0, ret_V=False):
+    """The reference extension's IR2S and operation-unit (OU) solvers
+    (split_arr_matmul.cu:336-1327), in the dtype of ``G``.
+
+    mode "gs": the ir_drop_gs sweep (wire = g_wire) -- ir_gs_ou_local with
+    ``loads`` = (g_load_left, g_load_down), ir_gs_ou with ``ou`` = (ou_rows,
+    ou_cols), each OU's source load g_wire / (first column + 1) and ground load
+    g_wire / (rows - last row) (:1086-1150).
+    mode "ir2s": the IR-drop-to-source iteration (wire = r_wire; :336-410,
+    816-930): Jacobi from the previous planes, per-segment line current sums
+    that persist between iterations, source and ground loads r_wire (ir2s),
+    ``loads`` = (r_load_left, r_load_down) (ir2s_ou_local) or, per OU,
+    r_wire * (first column + 1) and r_wire * (rows - last row) (ir2s_ou).
+    Returns currents [B, numX * rows / ou_rows, numY * cols] (one row group
+    without OUs), or cell voltages [B, numX, numY, rows, cols] with ret_V.
+    """
+    dt = np.asarray(G).dtype
+    S = dt.type
+    B, X, Y, n, m = batch_size, numX, numY, row_size, col_size
+    on, om = ou if ou is not None else (n, m)
+    nox, noy = n // on, m // om
+    w, b = S(wire), S(beta)
+    one = S(1)
+    inp = np.asarray(input_v, dt).reshape(B, X, n)
+    g = np.asarray(G, dt).reshape(X, n, Y, m).transpose(0, 2, 1, 3)[None]  # [1, X, Y, n, m]
+    U = np.broadcast_to(inp[:, :, None, :, None], (B, X, Y, n, m)).copy()
+    D = np.zeros((B, X, Y, n, m), dt)
+    scol = np.arange(noy) * om                       # first column of each OU column
+    srow = np.arange(nox) * on                       # first row of each OU row
+    if mode == "gs":
+        if ou is not None:
+            gl = np.array([w / S(s + 1) for s in scol], dt)
+            gd = np.array([w / S(n - (s + on - 1)) for s in srow], dt)
+        else:
+            gl = np.array([S(loads[0]) if loads else w], dt)
+            gd = np.array([S(loads[1]) if loads else w], dt)
+    else:
+        if ou is not None:
+            rl = np.array([w * S(s + 1) for s in scol], dt)
+            rd = np.array([w * S(n - (s + on - 1)) for s in srow], dt)
+        else:
+            rl = np.array([S(loads[0]) if loads else w], dt)
+            rd = np.array([S(loads[1]) if loads else w], dt)
+        Rs = np.zeros((B, X, Y, n, noy), dt)
+        Cs = np.zeros((B, X, Y, m, nox), dt)
+    src = inp[:, :, None, :, None]                    # [B, X, 1, n, 1]
+    for _ in range(iter_times):
+        U0, D0 = U.copy(), D.copy()
+        if mode == "gs":
+            for t in range(om):
+                c = scol + t
+                gj = g[..., c]
+                old = U[..., c]
+                other = D[..., c]
+                if t == 0:
+                    num = gl * src + w * U[..., c + 1] + gj * other
+                    sumg = w + gl + gj
+                elif t < om - 1:
+                    num = w * (U[..., c - 1] + U[..., c + 1]) + gj * other
+                    sumg = w * S(2) + gj
+                else:
+                    num = w * U[..., c - 1] + gj * other
+                    sumg = w + gj
+                U[..., c] = b * num / sumg + (one - b) * old
+            for t in range(on - 1, -1, -1):
+                r = srow + t
+                gi = g[..., r, :]
+                old = D[..., r, :]
+                other = U[..., r, :]
+                if t == on - 1:
+                    gdd = gd[:, None]
+                    num = w * D[..., r - 1, :] + gdd * S(0) + gi * other
+                    sumg = w + gdd + gi
+                elif t > 0:
+                    num = w * (D[..., r - 1, :] + D[..., r + 1, :]) + gi * other
+                    sumg = w * S(2) + gi
+                else:
+                    num = w * D[..., r + 1, :] + gi * other
+                    sumg = w + gi
+                D[..., r, :] = b * num / sumg + (one - b) * old
+        else:
+            cur = (U0 - D0) * g                       # cell currents from the previous iterate
+            Un = np.empty_like(U)
+            Dn = np.empty_like(D)
+            for t in range(om):
+                Rs += cur[..., scol + t].transpose(0, 1, 2, 3, 4)
+            for t in range(om):
+                c = scol + t
+                if t == 0:
+                    Un[..., c] = src - Rs * rl
+                else:
+                    Un[..., c] = Un[..., c - 1] - Rs * w
+                Rs -= cur[..., c]
+            for t in range(on):
+                Cs += np.moveaxis(cur[..., srow + t, :], 3, 4)
+            for t in range(on - 1, -1, -1):
+                r = srow + t
+                if t == on - 1:
+                    Dn[..., r, :] = np.moveaxis(Cs * rd, 4, 3)
+                else:
+                    Dn[..., r, :] = Dn[..., r + 1, :] + np.moveaxis(Cs * w, 4, 3)
+                Cs -= np.moveaxis(cur[..., r, :], 3, 4)
+            U, D = Un, Dn
+        if enable_break:
+            moved = int((np.abs(U - U0) > break_threshold).sum()) + int((np.abs(D - D0) > break_threshold).sum())
+            if moved == 0:
+                break
+    if ret_V:
+        return U - D
+    cur = (U - D) * g                                  # [B, X, Y, n, m]
+    out = np.zeros((B, X, nox, Y, m), dt)
+    for t in range(on):
+        out += cur[..., srow + t, :].transpose(0, 1, 3, 2, 4)
+    return out.reshape(B, X * nox, Y * m)

@@ -14,7 +14,7 @@ Runs only where the reference tree is present (it reads it from
    torch and there is no GPU here).  Nothing from that copy is kept.
 3. Their outputs, saved as small .npz files next to this script.
 
-Usage: python tests/golden/make_golden.py [sim] [pimtorch] [layers]
+Usage: python tests/golden/make_golden.py [sim] [pimtorch] [layers] [fcm] [ir2s]
 """
 import os
 import re
@@ -190,6 +190,60 @@ def pimtorch_fixtures():
         shutil.rmtree(td, ignore_errors=True)
 
 
+def ir2s_fixture():
+    """The reference's Python IR2S iteration (ir_drop_solve.py:35-72) on a seeded
+    layer, FP64, a few and many iterations."""
+    import torch
+    td, cc, ids, sa = import_pimtorch()
+    try:
+        P = cc.phyArrParams
+        rng = np.random.default_rng(17)
+        B, X, Y, n, m = 3, 2, 2, 8, 6
+        inp = (rng.integers(0, 2, (B, X, n)) * 0.2).astype(np.float64)
+        G = 1.0 / rng.choice([1e3, 2e4, 3e5, 1e6], size=(X, n, Y * m))
+        P.arrRowSize = n
+        P.r_wire = 2.93
+        P.ir_drop_less_than_thresholdBreak_enable = False
+        out = {}
+        for iters in (6, 300):
+            P.ir_drop_iter_time = iters
+            r = ids.ir_drop_ir2s_fastsolve(torch.tensor(inp), torch.tensor(G), B, X, Y, m)
+            out["iters_%d" % iters] = r.numpy()
+        np.savez_compressed(os.path.join(HERE, "pimtorch_ir2s_8x6.npz"), input=inp, G=G, B=B, numX=X, numY=Y,
+                            rows=n, cols=m, r_wire=2.93, **out)
+    finally:
+        shutil.rmtree(td, ignore_errors=True)
+
+
+def fcm_fixture():
+    """The reference's FCM export (``FCM gen``): the non-ideal conductance matrix
+    of a seeded 12x10 array from one unit-voltage solve per wordline
+    (crossbarHspice/2dArray.cc:949-1008), saved with the file text."""
+    rng = np.random.default_rng(31)
+    n, m = 12, 10
+    Rset = [2e6, 1.6e6, 1.3e6, 1e6]
+    st = rng.integers(0, 4, (n, m))
+    lines = ["useRtypeReRAMCell yes",
+             "cellRstates %d %s" % (len(Rset), " ".join("%.17g" % r for r in Rset)),
+             "arraySize %d %d" % (n, m), "selector no", "line_resistance %.17g" % 2.93]
+    for i in range(n):
+        for j in range(m):
+            lines.append("setCellR %d %d %d" % (i, j, st[i, j]))
+    lines += ["setUseLine left -1", "setUseLine down -1", "setLineV left -1 1", "setLineV down -1 0",
+              "senseBitlineI down -1", "FCM gen IR_FCM.conf"]
+    with tempfile.TemporaryDirectory() as td:
+        with open(os.path.join(td, "cfg"), "w") as f:
+            f.write("\n".join(lines) + "\n")
+        subprocess.run([SIM, "cfg"], cwd=td, capture_output=True, text=True, check=True)
+        with open(os.path.join(td, "IR_FCM.conf")) as f:
+            txt = f.read()
+    tok = txt.split()
+    assert int(tok[0]) == n and int(tok[1]) == m and int(tok[2]) == len(Rset)
+    g = np.array([float(t) for t in tok[3 + len(Rset) + n * m:]]).reshape(n, m)
+    np.savez_compressed(os.path.join(HERE, "sim_v1_fcm_12x10.npz"), states=st, Rset=np.array(Rset), r_wire=2.93,
+                        g_non_ideal=g, text=np.array(txt))
+
+
 def pimtorch_layer_fixtures():
     """Ref-column arrays, negative-pulse inputs and Conv2d_sp evaluation, through
     the reference's own splitArr_matmul_nn and Conv2d_sp with the droop solve."""
@@ -270,9 +324,13 @@ def pimtorch_layer_fixtures():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["sim", "pimtorch", "layers"]
+    which = sys.argv[1:] or ["sim", "pimtorch", "layers", "fcm", "ir2s"]
+    if "ir2s" in which:
+        ir2s_fixture()
     if "sim" in which:
         sim_fixtures()
+    if "fcm" in which:
+        fcm_fixture()
     if "pimtorch" in which:
         pimtorch_fixtures()
     if "layers" in which:

@@ -150,3 +150,49 @@ def test_converged_sweeps_reach_direct_solution():
     r = sweeps.ir_drop_gs(vin.reshape(1, 1, n), g.reshape(1, n, m), 1, n, m, 1, 1, 4000, GW, 1.5, ret_V=False)
     u, d = nodal.solve(g, GW, vin)
     np.testing.assert_allclose(r.reshape(m), nodal.currents(g, u, d), rtol=1e-10)
+
+
+def test_fcm_file_format_and_oracle(gold):
+    """The FCM export of the reference's sim (unit-voltage solve per wordline):
+    our writer reproduces its file text byte for byte from the same numbers, and
+    the FP64 oracle's unit responses give the same non-ideal conductances."""
+    from fadesim_gb300 import geff
+    z = gold("sim_v1_fcm_12x10.npz")
+    st, Rset, g_ref = z["states"], z["Rset"], z["g_non_ideal"]
+    assert geff.fcm_text(st, Rset, g_ref) == str(z["text"])
+    G = 1.0 / Rset[st]
+    n = G.shape[0]
+    u, d = nodal.solve(G, 1 / float(z["r_wire"]), np.eye(n))
+    g_or = nodal.currents(G, u, d)
+    assert np.abs(g_or - g_ref).max() <= 1e-9 * np.abs(g_ref).max()
+
+
+@pytest.mark.parametrize("iters", [6, 300])
+def test_ir2s_restatement_matches_reference(gold, iters):
+    """The IR2S iteration restated from the CUDA extension (persistent line
+    sums) against the reference's Python IR2S (sums recomputed each iteration):
+    the same iterates up to FP64 rounding."""
+    z = gold("pimtorch_ir2s_8x6.npz")
+    B, X, Y, n, m = (int(z[k]) for k in ("B", "numX", "numY", "rows", "cols"))
+    r = sweeps.ir_family(z["input"], z["G"], B, n, m, X, Y, iters, float(z["r_wire"]), "ir2s")
+    ref = z["iters_%d" % iters]
+    assert np.abs(r - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_ir_family_consistency():
+    """Structural identities of the OU and load variants: a whole-tile OU and
+    wire-valued loads reduce each to its plain solver; IR2S converges to the
+    nodal solution."""
+    rng = np.random.default_rng(1)
+    B, X, Y, n, m = 2, 2, 2, 8, 6
+    inp = rng.integers(0, 2, (B, X, n)) * 0.2
+    G = 1 / rng.choice([1e3, 2e4, 3e5, 1e6], size=(X, n, Y * m))
+    gs = sweeps.ir_drop_gs(inp, G, B, n, m, X, Y, 40, GW, 1.9)
+    for kw in (dict(), dict(ou=(n, m)), dict(loads=(GW, GW))):
+        r = sweeps.ir_family(inp, G, B, n, m, X, Y, 40, GW, "gs", beta=1.9, **kw)
+        assert np.abs(r - gs).max() <= 1e-13 * np.abs(gs).max()
+    conv = sweeps.ir_family(inp, G, B, n, m, X, Y, 400, 2.93, "ir2s")
+    assert np.abs(conv - nodal.solve_layer(inp, G, n, m, X, Y, GW)).max() <= 1e-12 * np.abs(conv).max()
+    for kw in (dict(ou=(n, m)), dict(loads=(2.93, 2.93))):
+        r = sweeps.ir_family(inp, G, B, n, m, X, Y, 400, 2.93, "ir2s", **kw)
+        assert np.abs(r - conv).max() <= 1e-13 * np.abs(conv).max()
