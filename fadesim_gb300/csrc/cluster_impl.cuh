@@ -468,7 +468,8 @@ __device__ __forceinline__ void cl_outputs(cg::cluster_group &cluster, int rank,
         for (int e = tid; e < nloc * m; e += CL_T) {
             const int lr = e / m, j = e - lr * m;
             const int q = cswz<LDM>(lr, j);
-            const TIO uu = (TIO)U[q] + (TIO)vin[lr];
+            const TIO uu = (TIO)U[q] + vin_exact<TIO>(a.input, ((size_t)b * a.numX + x) * n + row0 + lr, a.f64,
+                                                      vin[lr]);
             if (!isfinite((float)uu) || !isfinite(D[q])) nonfinite_flag = 1;
             const size_t sol = ((size_t)b * a.numX + x) * a.numY + y;
             const size_t i = (size_t)row0 + lr;

@@ -37,6 +37,19 @@ __device__ __forceinline__ float load_io(const void *p, size_t i, bool f64) {
     return f64 ? (float)static_cast<const double *>(p)[i] : static_cast<const float *>(p)[i];
 }
 
+// Input voltage i of a solve in the output type: the FP64 input unrounded when
+// both the input and the outputs are FP64 (the solve itself runs on the FP32
+// copy; its node deviations change by ~1e-7 of themselves with that rounding,
+// while the rounding of the wordline voltage itself, up to 6e-8 V per volt,
+// would otherwise reach every node of the row unchanged).
+template <typename TIO>
+__device__ __forceinline__ TIO vin_exact(const void *p, size_t i, bool f64, float staged) {
+    if constexpr (sizeof(TIO) == 8) {
+        if (f64) return static_cast<const double *>(p)[i];
+    }
+    return (TIO)staged;
+}
+
 // sinh(t)/t, t >= 0 (series below 1e-2: truncation < 1e-10)
 __device__ __forceinline__ float sinhc(float t) { return t < 1e-2f ? fmaf(t * t, 1.f / 6.f, 1.f) : sinhf(t) / t; }
 

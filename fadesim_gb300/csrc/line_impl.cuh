@@ -303,7 +303,8 @@ __device__ __forceinline__ void line_outputs(const SolveArgs &a, const float *Gs
         for (int e = tid; e < n * m; e += T) {
             const int i = e / m, j = e - i * m;
             const int q = swz<LD>(i, j);
-            const TIO uu = (TIO)U[q] + (TIO)vin_s[vpad(i)];
+            const TIO uu =
+                (TIO)U[q] + vin_exact<TIO>(a.input, ((size_t)b * a.numX + x) * n + i, a.f64, vin_s[vpad(i)]);
             const size_t sol = ((size_t)b * a.numX + x) * a.numY + y;
             if (!isfinite((float)uu) || !isfinite(D[q])) nonfinite_flag = 1;
             if (a.ret_V == 2) {
@@ -324,7 +325,9 @@ __device__ __forceinline__ void line_outputs(const SolveArgs &a, const float *Gs
                 const int i = s * SEG + k;
                 if (i < n) {
                     const int q = swz<LD>(i, j);
-                    const TIO V = ((TIO)U[q] + (TIO)vin_s[vpad(i)]) - (TIO)D[q];
+                    const TIO V =
+                        ((TIO)U[q] + vin_exact<TIO>(a.input, ((size_t)b * a.numX + x) * n + i, a.f64,
+                                                    vin_s[vpad(i)])) - (TIO)D[q];
                     TIO Ic = (TIO)(NL ? nl_geff(Gs[q], (float)V, a.ctl) : Gs[q] * gw) * V;
                     if (a.ctl.noise_sigma > 0.f)
                         Ic *= (TIO)1 + (TIO)(a.ctl.noise_sigma *

@@ -14,7 +14,7 @@ Runs only where the reference tree is present (it reads it from
    torch and there is no GPU here).  Nothing from that copy is kept.
 3. Their outputs, saved as small .npz files next to this script.
 
-Usage: python tests/golden/make_golden.py [sim] [pimtorch] [layers] [fcm] [ir2s]
+Usage: python tests/golden/make_golden.py [sim] [pimtorch] [layers] [fcm] [ir2s] [simtext]
 """
 import os
 import re
@@ -244,6 +244,64 @@ def fcm_fixture():
                         g_non_ideal=g, text=np.array(txt))
 
 
+SIM_TEXT_CFG = """% a 6x5 array in the reference's config language, exercising the commands
+// the fast path reads (comments, whole-array setters, per-line overrides) and
+// netlist-only ones that it skips
+topString .title twoDArray
+useRtypeReRAMCell yes
+cellRstates 4 2e6 1.6e6 1.3e6 1e6
+arraySize 6 5
+selector no
+line_resistance 2.93
+setCellR -1 -1 2
+setCellR 0 -1 3
+setCellR -1 4 0
+setCellR 2 1 1
+setCellR 5 3 3
+setUseLine left -1
+setUseLine down -1
+setLineV left -1 0.1
+setLineV left 1 0.25
+setLineV left 4 0
+setLineV down -1 0
+senseBitlineI down -1
+nodebasedGSMethod 100000 1.9 0 yes 1e-13
+FCM gen fcm.conf
+setLineV left 2 0.3
+FCM test fcm.conf
+"""
+
+
+def sim_text_fixture():
+    """The reference's own output files for a committed config: byte-level
+    layout of fastmode_nodebasedGS.out, IR_FCM.out (both modes) and the FCM
+    file, and the stdout lines that its scripts parse.  Every nodeBasedGS call
+    rewrites fastmode_nodebasedGS.out (FCM gen's unit solves too) and both FCM
+    modes write IR_FCM.out, so each file is taken from a run of the config cut
+    after the command that writes it."""
+    with open(os.path.join(HERE, "sim_v1_6x5.cfg"), "w") as f:
+        f.write(SIM_TEXT_CFG)
+
+    def run(upto, td):
+        cut = SIM_TEXT_CFG.index(upto) + len(upto)
+        with open(os.path.join(td, "config"), "w") as f:
+            f.write(SIM_TEXT_CFG[:cut] + "\n")
+        return subprocess.run([SIM], cwd=td, capture_output=True, text=True, check=True).stdout
+
+    with tempfile.TemporaryDirectory() as td:
+        out = run("nodebasedGSMethod 100000 1.9 0 yes 1e-13", td)
+        keep = [ln for ln in out.splitlines()
+                if re.match(r"(evalutate|threshould|error I sum|set array size|setCellR)", ln)]
+        with open(os.path.join(HERE, "sim_v1_6x5.stdout"), "w") as f:
+            f.write("\n".join(keep) + "\n")
+        shutil.copy(os.path.join(td, "fastmode_nodebasedGS.out"), os.path.join(HERE, "sim_v1_6x5.nodebasedGS.out"))
+        run("FCM gen fcm.conf", td)
+        shutil.copy(os.path.join(td, "IR_FCM.out"), os.path.join(HERE, "sim_v1_6x5.IR_FCM_gen.out"))
+        shutil.copy(os.path.join(td, "fcm.conf"), os.path.join(HERE, "sim_v1_6x5.fcm.conf"))
+        run("FCM test fcm.conf", td)
+        shutil.copy(os.path.join(td, "IR_FCM.out"), os.path.join(HERE, "sim_v1_6x5.IR_FCM_test.out"))
+
+
 def pimtorch_layer_fixtures():
     """Ref-column arrays, negative-pulse inputs and Conv2d_sp evaluation, through
     the reference's own splitArr_matmul_nn and Conv2d_sp with the droop solve."""
@@ -324,7 +382,9 @@ def pimtorch_layer_fixtures():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["sim", "pimtorch", "layers", "fcm", "ir2s"]
+    which = sys.argv[1:] or ["sim", "pimtorch", "layers", "fcm", "ir2s", "simtext"]
+    if "simtext" in which:
+        sim_text_fixture()
     if "ir2s" in which:
         ir2s_fixture()
     if "sim" in which:

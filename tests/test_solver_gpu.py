@@ -164,8 +164,8 @@ def test_dropin_signature_and_errors(acc):
         acc.ir_drop_gs(ti, tg, B, 1, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
     with pytest.raises(RuntimeError):
         acc.ir_drop_gs(ti, tg.double(), B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
-    with pytest.raises(NotImplementedError):
-        acc.ir2s(ti, tg)
+    with pytest.raises(NotImplementedError):  # sinh cells: the IR2S family runs linear cells only
+        acc.ir2s(ti, tg, B, n, m, X, Y, 10, 2.93, False, 1e-7, True, [1.0])
     empty = acc.ir_drop_gs(ti[:0], tg, 0, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
     assert empty.shape == (0, X, Y * m)
 
