@@ -2,6 +2,7 @@
 fast read (VMM) path, with the nodal solve on the GPU.
 
     python -m fadesim_gb300.sim [config] [-debug]
+    python -m fadesim_gb300.sim --v2 [config]      (the V2 simulator's dialect)
 
 The config is the reference's own command file (crossbarHspice/GenArray.cc:72-83:
 one command per line, ``%`` and ``//`` lines skipped), read into the same array
@@ -262,13 +263,16 @@ class Array2D:
         """The one wire conductance the GPU solve takes.  nodeBasedGS reads the
         wordline segments RULine[i][0..m-1] and the bitline segments
         RDLine[j][1..n] (2dArray.cc:1561-1587); they must all be equal."""
-        used = np.concatenate([self.RULine[:, :self.m].ravel(), self.RDLine[:, 1:].ravel()])
+        used = self._used_segments()
         if not used.size or np.any(used <= 0):
             raise SimError("line resistance not set (line_resistance)")
         if np.any(used != used[0]):
             raise SimError("the GPU solver takes one wire resistance; this config sets %d different line "
                            "segment values (setLineR / rload)" % len(np.unique(used)))
         return 1.0 / used[0]
+
+    def _used_segments(self):
+        return np.concatenate([self.RULine[:, :self.m].ravel(), self.RDLine[:, 1:].ravel()])
 
     def vmm_boundary(self):
         """check_status (2dArray.cc:85-101): wordlines driven from the left only,
@@ -432,6 +436,115 @@ class Array2D:
         self.g_eff = g_eff
 
 
+# Commands the V2 simulator registers (crossbarHspice/V2/main.cpp:84-115); any
+# other name is an error there.
+_V2_COMMANDS = {"empty", "arraySize", "line_resistance", "setLineR", "rload", "setUseLine", "setNotUseLine",
+                "setUseLine++", "setLineV", "setLineV++", "setCellR", "cellRStates", "inputVStates", "topString",
+                "bottomString", "build", "capacity", "capacitance", "senseCellV", "senseBitlineI",
+                "senseWordlineI", "simpleWriteOne", "simpleWriteZero", "randSetInputV", "useRtypeReRAMCell",
+                "randSetR", "dc", "ac", "simpleReadOut", "nodebasedGSMethod"}
+
+
+class Array2DV2(Array2D):
+    """The V2 simulator's dialect (crossbarHspice/V2): the same array state and
+    fast path, with its command names (``cellRStates``, ``inputVStates``), ``#``
+    comments, an error for any unregistered command or malformed argument list
+    (V2/command.h:63-118, caught in V2/main.cpp:27-31 with the line number), a
+    single ``nodebasedGSMethod`` solve with ``w`` read by stod and mode bits 0
+    and 2 refused (V2/concrete_command.h:1097-1135, 1186-1210), messages
+    collected into default.log, and wordline segments read from RDLine
+    (V2/concrete_command.h:1214 aliases RULine to it)."""
+
+    def __init__(self, out=None, cwd="."):
+        self.logbuf = []
+        super().__init__(out, cwd)
+
+    def log(self, *a):
+        self.logbuf.append(" ".join(str(x) for x in a))
+
+    def read_config(self, text):
+        """read_file_and_execute (V2/main.cpp:48-59); an error names its line."""
+        for no, line in enumerate(text.splitlines(), 1):
+            words = line.split(None, 1)
+            if not words or words[0] in ("%", "//", "#"):
+                continue
+            try:
+                self.set_paras(words[0], words[1] if len(words) > 1 else "")
+            except (SimError, ValueError, IndexError) as e:
+                raise SimError("line %d: %s" % (no, e)) from None
+
+    def set_paras(self, s, t):
+        if s not in _V2_COMMANDS:
+            raise SimError("Unknown command: " + s)
+        a = t.split()
+        if s in ("setUseLine", "setNotUseLine", "setUseLine++", "setLineV", "setLineV++") and a[0] not in _DIRS:
+            raise SimError("Arg str not matched Direction should be up|left|down|right.")
+        if s == "cellRStates":
+            return super().set_paras("cellRstates", t)
+        if s == "inputVStates":
+            return super().set_paras("inputVstates", t)
+        if s == "setLineR" and a[0] not in ("up", "down"):
+            raise SimError("Arg Direction not matched:setLineR up|down x:int y:int r:double")
+        if s == "arraySize":
+            self.set_array_size(int(a[0]), int(a[1]))
+            self.log("Set array size to ( %d, %d )" % (self.n, self.m))
+            return True
+        if s == "empty":
+            return True
+        return super().set_paras(s, t)
+
+    def _used_segments(self):
+        """Wordline segment (i, j) is RDLine[i][j] here, which exists in the
+        [m][n+1] RDLine only when n <= m <= n+1; any other shape reads past it
+        in the reference, so it needs one uniform resistance everywhere."""
+        if self.n <= self.m <= self.n + 1:
+            return np.concatenate([self.RDLine[:self.n, :self.m].ravel(), self.RDLine[:, 1:].ravel()])
+        return self.RDLine.ravel()
+
+    def _cmd_nodebased_gs(self, a):
+        if len(a) < 3:
+            raise SimError("args number not matched (<3)")
+        if len(a) > 3 and len(a) != 5:
+            raise SimError("args number not matched (!=5)")
+        iter_time, w, mode = int(a[0]), float(a[1]), int(a[2])
+        enable_break = len(a) > 3 and check_yes(a[3])
+        thr = float(a[4]) if enable_break else 0.0
+        if mode & 1:
+            raise SimError("mode bit 0 is not supported now")
+        if not (self.n >= 2 and self.m >= 2):
+            raise SimError("m and n should greater than 2")
+        if mode & 4:
+            raise SimError("mode bit 2 is not supported now")
+        if mode & 2:
+            raise SimError("nodebasedGSMethod mode bit 1 (write the initial estimate without iterating) is not "
+                           "provided by this front-end")
+        self._nodebased_gs(iter_time, w, enable_break, thr)
+
+    def _report(self, vup, vdown, iters, status, enable_break, elapsed):
+        self.log("time = %s s" % _fmt_g(elapsed))
+        from ._lib import ST_MAXITER, ST_NONFINITE
+        g = self.conductances()
+        if status & (ST_MAXITER | ST_NONFINITE):
+            self.log("warning: the line solve stopped without meeting its tolerance (status %d)" % status)
+        elif enable_break:
+            self.log("threshould break, iter times =  %d" % (iters - 1))
+        else:
+            self.log("iter times = %d" % iters)
+        iout = ((vup - vdown) * g).sum(axis=0)
+        err = self.err_i_sum(vup, vdown, g)
+        with open(self.path("fastmode_nodebasedGS.out"), "w") as f:
+            f.write(format_nodebased_out(err, vup, vdown, iout))
+        self.log("error I sum = " + _fmt_g(err))
+        self.solves.append((vup, vdown, iout, iters))
+
+    def write_log(self):
+        """print_log_to_default_file (V2/main.cpp:61-66)."""
+        with open(self.path("default.log"), "w") as f:
+            f.write("\n--------Operation Log---------\n\n")
+            f.write("".join(ln + "\n" for ln in self.logbuf))
+            f.write("--------Log end--------\n")
+
+
 def format_nodebased_out(err, vup, vdown, iout):
     """fastmode_nodebasedGS.out (2dArray.cc:1648-1679)."""
     lines = ["error I sum = " + _fmt_g(err), "vup = "]
@@ -459,10 +572,34 @@ def parse_nodebased_out(text):
     return err, rows(up_s), rows(dn_s), np.array([float(x) for x in io_s.split()])
 
 
+def main_v2(argv):
+    """V2/main.cpp:17-46: the config file (default ``config``), the log in
+    default.log, errors reported with their line."""
+    path = argv[0] if argv else "config"
+    arr = Array2DV2()
+    try:
+        with open(path) as f:
+            arr.read_config(f.read())
+    except SimError as e:
+        print("Error(s) occured in %s" % e)
+        print("\n--------Operation Log---------\n")
+        for ln in arr.logbuf:
+            print(ln)
+        print("--------Log end--------")
+        return 1
+    print("Log print to default.log")
+    arr.write_log()
+    print("--------Run end && Succeed---------")
+    return 0
+
+
 def main(argv=None):
     """main.cc:9-44: no argument reads ``config``; ``config -debug`` echoes every
-    command; ``-3DH`` (the 3-D netlist generator) is not provided."""
+    command; ``-3DH`` (the 3-D netlist generator) is not provided.  ``--v2``
+    first reads the config in the V2 simulator's dialect instead."""
     argv = sys.argv[1:] if argv is None else argv
+    if argv and argv[0] == "--v2":
+        return main_v2(argv[1:])
     if len(argv) > 2:
         print("argc number wrong")
         return 0

@@ -14,7 +14,7 @@ Runs only where the reference tree is present (it reads it from
    torch and there is no GPU here).  Nothing from that copy is kept.
 3. Their outputs, saved as small .npz files next to this script.
 
-Usage: python tests/golden/make_golden.py [sim] [pimtorch] [layers] [fcm] [ir2s] [simtext]
+Usage: python tests/golden/make_golden.py [sim] [pimtorch] [layers] [fcm] [ir2s] [simtext] [sim2text]
 """
 import os
 import re
@@ -302,6 +302,46 @@ def sim_text_fixture():
         shutil.copy(os.path.join(td, "IR_FCM.out"), os.path.join(HERE, "sim_v1_6x5.IR_FCM_test.out"))
 
 
+SIM2_TEXT_CFG = """# the V2 simulator's dialect: '#' comments, cellRStates, no selector command;
+% a 6x7 array (V2 reads wordline segments from the [m][n+1] bitline table, in
+// range for n <= m <= n+1)
+topString .title twoDArray
+useRtypeReRAMCell yes
+cellRStates 4 2e6 1.6e6 1.3e6 1e6
+arraySize 6 7
+line_resistance 2.93
+setCellR -1 -1 1
+setCellR 0 -1 3
+setCellR -1 6 0
+setCellR 2 1 2
+setCellR 5 3 3
+setUseLine left -1
+setUseLine down -1
+setLineV left -1 0.2
+setLineV left 3 0.05
+setLineV down -1 0
+senseBitlineI down -1
+nodebasedGSMethod 100000 1.9 0 yes 1e-13
+"""
+
+
+def sim2_text_fixture():
+    """The reference's V2 ``sim`` (``make -C oracle ref2``) on a committed V2
+    config: its fastmode_nodebasedGS.out and the solve lines of default.log."""
+    subprocess.run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "ref2"], check=True)
+    with open(os.path.join(HERE, "sim_v2_6x7.cfg"), "w") as f:
+        f.write(SIM2_TEXT_CFG)
+    with tempfile.TemporaryDirectory() as td:
+        shutil.copy(os.path.join(HERE, "sim_v2_6x7.cfg"), os.path.join(td, "config"))
+        out = subprocess.run([SIM + "2"], cwd=td, capture_output=True, text=True, check=True).stdout
+        assert "Run end && Succeed" in out, out
+        shutil.copy(os.path.join(td, "fastmode_nodebasedGS.out"), os.path.join(HERE, "sim_v2_6x7.nodebasedGS.out"))
+        with open(os.path.join(td, "default.log")) as f:
+            keep = [ln for ln in f.read().splitlines() if re.match(r"(threshould|error I sum|Set array size)", ln)]
+        with open(os.path.join(HERE, "sim_v2_6x7.log"), "w") as f:
+            f.write("\n".join(keep) + "\n")
+
+
 def pimtorch_layer_fixtures():
     """Ref-column arrays, negative-pulse inputs and Conv2d_sp evaluation, through
     the reference's own splitArr_matmul_nn and Conv2d_sp with the droop solve."""
@@ -382,7 +422,9 @@ def pimtorch_layer_fixtures():
 
 
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["sim", "pimtorch", "layers", "fcm", "ir2s", "simtext"]
+    which = sys.argv[1:] or ["sim", "pimtorch", "layers", "fcm", "ir2s", "simtext", "sim2text"]
+    if "sim2text" in which:
+        sim2_text_fixture()
     if "simtext" in which:
         sim_text_fixture()
     if "ir2s" in which:

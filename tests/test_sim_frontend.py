@@ -136,3 +136,69 @@ def test_rand_pick_keeps_reference_cumulative_sum():
     np.testing.assert_array_equal(got, [0, 1, 1, 2, 2, 2])
     with pytest.raises(sim.SimError):
         a._rand_pick([0.2, 0.3], 1, Seq([0]))
+
+
+# -- the V2 dialect (tests/golden/sim_v2_6x7.*: the reference's V2 sim) ------------
+
+def read_v2(cfg):
+    a = sim.Array2DV2(out=io.StringIO())
+    a.read_config(cfg)
+    return a
+
+
+def v2_config_upto(cmd):
+    cfg = text("sim_v2_6x7.cfg")
+    return cfg[:cfg.index("\n" + cmd) + 1]
+
+
+def test_v2_config_and_kcl_check():
+    a = read_v2(v2_config_upto("nodebasedGSMethod"))
+    assert a.logbuf[0] == text("sim_v2_6x7.log").splitlines()[0]      # "Set array size to ( 6, 7 )"
+    assert (a.n, a.m) == (6, 7) and a.cellR_states == [2e6, 1.6e6, 1.3e6, 1e6]
+    np.testing.assert_array_equal(a.v[1], [0.2, 0.2, 0.2, 0.05, 0.2, 0.2])
+    g = a.conductances()
+    # V2 reads w with stod (V1: stof)
+    up, dn, _, sweeps = augs.solve(g, a.v[1], 2.93, 100000, 1.9, True, 1e-13)
+    log = text("sim_v2_6x7.log").splitlines()
+    assert "threshould break, iter times =  %d" % (sweeps - 1) in log
+    assert "error I sum = " + sim._fmt_g(a.err_i_sum(up, dn, g)) in log
+    ref = sim.parse_nodebased_out(text("sim_v2_6x7.nodebasedGS.out"))
+    assert np.abs(up - ref[1]).max() < 1e-12 and np.abs(dn - ref[2]).max() < 1e-12
+    assert sim.format_nodebased_out(*ref) == text("sim_v2_6x7.nodebasedGS.out")
+
+
+@pytest.mark.parametrize("line, msg", [
+    ("selector no", "Unknown command: selector"),          # registered in V1 only
+    ("cellRstates 2 1e6 2e6", "Unknown command: cellRstates"),
+    ("setLineV middle 0 1", "Direction should be"),
+    ("setLineR left 0 0 1", "setLineR up\\|down"),
+    ("nodebasedGSMethod 100 1.9", "args number not matched \\(<3\\)"),
+    ("nodebasedGSMethod 100 1.9 0 yes", "args number not matched \\(!=5\\)"),
+    ("nodebasedGSMethod 100 1.9 1 yes 1e-9", "mode bit 0 is not supported now"),
+    ("nodebasedGSMethod 100 1.9 4 yes 1e-9", "mode bit 2 is not supported now"),
+])
+def test_v2_errors_name_the_line(line, msg):
+    cfg = v2_config_upto("nodebasedGSMethod")
+    with pytest.raises(sim.SimError, match="line %d: .*%s" % (cfg.count("\n") + 1, msg)):
+        read_v2(cfg + line + "\n")
+
+
+def test_v2_segment_table_shapes():
+    """V2 reads wordline segments from the bitline table: in range for
+    n <= m <= n+1, otherwise the whole table must be uniform."""
+    cfg = "arraySize 4 4\nline_resistance 2\nsetLineR down 3 0 9\n"
+    assert read(cfg)[0].wire_conductance() == 0.5     # V1: RDLine[3][0] is the open top of bitline 3
+    with pytest.raises(sim.SimError, match="one wire resistance"):
+        read_v2(cfg).wire_conductance()               # V2: also the driver segment of wordline 3
+    a = read_v2("arraySize 4 8\nline_resistance 2\nsetLineR down 7 0 9\n")
+    with pytest.raises(sim.SimError, match="one wire resistance"):
+        a.wire_conductance()
+
+
+def test_v2_main_reports_errors(tmp_path, monkeypatch, capsys):
+    (tmp_path / "config").write_text("arraySize 4 4\nselector no\n")
+    monkeypatch.chdir(tmp_path)
+    assert sim.main(["--v2"]) == 1
+    out = capsys.readouterr().out
+    assert out.startswith("Error(s) occured in line 2: Unknown command: selector")
+    assert "Set array size to ( 4, 4 )" in out

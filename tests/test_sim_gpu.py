@@ -123,3 +123,22 @@ def test_config_omega_runs_fixed_relaxation(sim, tmp_path, monkeypatch):
         _, ur, dr, _ = sim.parse_nodebased_out(text("sim_v1_6x5.nodebasedGS.out"))
         assert np.abs(u - ur).max() < 1e-10
     assert iters[1.0] < iters[1.8]
+
+
+def test_v2_config_end_to_end(sim, tmp_path, monkeypatch, capsys):
+    """The V2 dialect through its CLI: fastmode_nodebasedGS.out against the
+    reference V2 sim's converged file, default.log with the solve lines."""
+    (tmp_path / "config").write_text(text("sim_v2_6x7.cfg"))
+    monkeypatch.chdir(tmp_path)
+    assert sim.main(["--v2"]) == 0
+    assert capsys.readouterr().out.endswith("--------Run end && Succeed---------\n")
+    got = (tmp_path / "fastmode_nodebasedGS.out").read_text()
+    ref = text("sim_v2_6x7.nodebasedGS.out")
+    assert [len(ln) for ln in got.splitlines()[1:]] == [len(ln) for ln in ref.splitlines()[1:]]
+    _, u, d, i = sim.parse_nodebased_out(got)
+    _, ur, dr, ir = sim.parse_nodebased_out(ref)
+    assert np.abs(u - ur).max() < 1e-10 and np.abs(d - dr).max() < 1e-10
+    np.testing.assert_allclose(i, ir, rtol=1e-6)
+    log = (tmp_path / "default.log").read_text()
+    assert "Set array size to ( 6, 7 )" in log
+    assert re.search(r"^threshould break, iter times =  \d+$", log, re.M)
