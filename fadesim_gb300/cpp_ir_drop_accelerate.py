@@ -152,6 +152,63 @@ def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_tim
     return out, stats, it
 
 
+def ir_drop_gs_host(input, G, batch_size, row_size, col_size, numX, numY, iter_times=600, g_wire=1 / 2.93, beta=1.9,
+                    enable_break=False, break_threshould=1e-7, nonlinear_cell_enable=False, nonlinear_params=(),
+                    ret_V=False, out=None, group_x=0, return_stats=False, device=None, **opt):
+    """``ir_drop_gs`` on host (CPU) tensors: the library copies input and G in and
+    the result out itself, pipelined over groups of ``group_x`` values of numX
+    (0: automatic) so one group's copies overlap another's solve.  Pinned
+    (``pin_memory()``) tensors let the copies run asynchronously.  Returns the
+    CPU result (and the stats dict with ``return_stats``); ``opt`` takes the
+    ``SolverOptions`` fields per call, as ``ir_drop_gs_ex`` does."""
+    for t, name in ((input, "input"), (G, "G")):
+        if not isinstance(t, torch.Tensor) or t.is_cuda:
+            raise RuntimeError("%s must be a CPU tensor" % name)
+        if not t.is_contiguous():
+            raise RuntimeError("%s must be contiguous" % name)
+    if row_size < 2 or col_size < 2:
+        raise RuntimeError("row_size and col_size should be >=2")
+    if input.dtype not in (torch.float32, torch.float64) or G.dtype != input.dtype:
+        raise RuntimeError("input and G must both be float32 or both float64")
+    if input.numel() != batch_size * numX * row_size or G.numel() != numX * row_size * numY * col_size:
+        raise RuntimeError("input / G sizes do not match batch_size, numX, numY, row_size, col_size")
+    o = SolverOptions(**{k: v for k, v in vars(options).items()})
+    for k, v in opt.items():
+        if not hasattr(o, k):
+            raise TypeError("unknown solver option %r" % k)
+        setattr(o, k, v)
+    if ret_V == 2:
+        shape = (batch_size, numX, numY, 2, row_size, col_size)
+    elif ret_V:
+        shape = (batch_size, numX, numY, row_size, col_size)
+    else:
+        shape = (batch_size, numX, numY * col_size)
+    if out is None:
+        out = torch.empty(shape, dtype=input.dtype, pin_memory=input.is_pinned())
+    elif out.is_cuda or not out.is_contiguous() or out.dtype != input.dtype or out.numel() != math.prod(shape):
+        raise RuntimeError("out must be a contiguous CPU %s tensor of %d elements" % (input.dtype, math.prod(shape)))
+    lib = _lib.load()
+    params = [float(v) for v in (nonlinear_params or [])]
+    cparams = (ctypes.c_double * max(1, len(params)))(*params) if params else None
+    stats = _lib.SolveStats()
+    dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    with torch.cuda.device(dev):
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        rc = lib.fadesim_ir_drop_gs_host(_lib.F64 if input.dtype == torch.float64 else _lib.F32, input.data_ptr(),
+                                         G.data_ptr(), int(batch_size), int(row_size), int(col_size), int(numX),
+                                         int(numY), int(iter_times), float(g_wire), float(beta),
+                                         int(bool(enable_break)), float(break_threshould),
+                                         int(bool(nonlinear_cell_enable)), cparams, len(params),
+                                         2 if ret_V == 2 else int(bool(ret_V)), out.data_ptr(),
+                                         ctypes.byref(o.to_c()), ctypes.byref(stats) if return_stats else None,
+                                         int(group_x), stream)
+    _lib.check(rc)
+    if return_stats:
+        return out, dict(solves=int(stats.solves), iters_sum=int(stats.iters_sum), iters_max=int(stats.iters_max),
+                         status_or=int(stats.status_or))
+    return out
+
+
 def _family(cname, input, G, batch_size, row_size, col_size, numX, numY, out_rows, ret_V, nonlinear_cell_enable,
             *cargs):
     """Shared checks and launch of the IR2S / OU exports (their own iterates)."""

@@ -102,6 +102,22 @@ int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G, int batch
                           int n_nonlinear_params, int ret_V, void *out, const fadesim_solve_opts *opts,
                           fadesim_solve_stats *stats, int *per_solve_iters, void *stream);
 
+/* fadesim_ir_drop_gs_ex on HOST buffers: input, G and out are host memory (page-locked for the
+ * copies to overlap), laid out as for fadesim_ir_drop_gs_ex.  The library copies them in and out
+ * itself, pipelined over groups of group_x values of numX (0: about eight groups of whole
+ * multiples of the SM count of tiles) on three internal streams ordered after `stream`, so one
+ * group's copies overlap another's solve.  Returns when out holds the result.  Replaces the
+ * transfers the reference's callers make around ir_drop_gs, which takes device tensors
+ * (splitArrayArithmetic.py:485-511): .to(device) before and .cpu() after
+ * (splitArrayArithmetic.py:1082, 1124), serialised with the solve.  stats (host, may be NULL)
+ * sums the groups' statistics; asking for them makes every group wait for its own solve before
+ * the next group is queued. */
+int fadesim_ir_drop_gs_host(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
+                            int numX, int numY, int iter_times, double g_wire, double beta, int enable_break,
+                            double break_threshould, int nonlinear_cell_enable, const double *nonlinear_params,
+                            int n_nonlinear_params, int ret_V, void *out, const fadesim_solve_opts *opts,
+                            fadesim_solve_stats *stats, int group_x, void *stream);
+
 /* ---- the reference extension's other exports (split_arr_matmul.cu:1429-1437),
  * reproducing their iterates: same arguments and meaning, dtype (FADESIM_F32 /
  * FADESIM_F64) typing input, G and out; linear cells (nonlinear cells: ir_drop_gs).
