@@ -381,6 +381,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
         st_iters = 0;
         st_max = 0;
         st_or = 0;
+        nonfinite_flag = 0;
     }
 
     for (long long item = blockIdx.x; item < a.nitems; item += gridDim.x) {
@@ -421,7 +422,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             rate_hint = 0.f;
         }
         for (int b = b0; b < b1; ++b) {
-            __syncthreads();
+            // (the tile setup and the previous solve's outputs end with a barrier)
             // warm start: initial deviation planes [2][n][m] of this solve.  From
             // the ideal state the planes are zero: the first iteration is then a
             // ZERO iteration that reads neither plane, unless every iteration must
@@ -434,19 +435,22 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     D[e] = 0.f;
                 }
             }
-            float vabs = 0.f;
-            if (tid < LD) {
-                const float v = (tid < n) ? load_io(a.input, ((size_t)b * a.numX + x) * n + tid, f64) : 0.f;
-                vin_s[vpad(tid)] = v;
-                vabs = fabsf(v);
-            }
+            if (tid < LD)
+                vin_s[vpad(tid)] = (tid < n) ? load_io(a.input, ((size_t)b * a.numX + x) * n + tid, f64) : 0.f;
+            __syncthreads();
             // precise iterations may keep the cell term in FP32 (RES 3) when its
             // rounding, amplified by at most L^2/2 through a line solve, stays 8x
-            // under the tolerance: per node <= gs_max * 3 vin_max * 2^-23
-            const float vin_max = block_max<NW>(vabs, bmax_scratch);
-            const float Lmax = (float)max(n, m);
-            const bool semi = !NL && ff &&
-                              gs_max * 3.f * vin_max * 1.1920929e-07f * 0.5f * Lmax * Lmax <= 0.125f * tol;
+            // under the tolerance: per node <= gs_max * 3 vin_max * 2^-23.  Every
+            // warp takes the largest input from the shared copy itself, before
+            // the first iteration only when that one is precise (otherwise after
+            // its reduction barrier, where the warps wait anyway).
+            auto semi_now = [&]() {
+                float vmx = 0.f;
+                for (int i = tid & 31; i < n; i += 32) vmx = fmaxf(vmx, fabsf(vin_s[vpad(i)]));
+                const float Lmax = (float)max(n, m);
+                return !NL && ff && gs_max * 3.f * warp_max(vmx) * 1.1920929e-07f * 0.5f * Lmax * Lmax <= 0.125f * tol;
+            };
+            bool semi = precise_first ? semi_now() : false;
             if (warm) {
                 const float *w0 = a.init + (((size_t)b * a.numX + x) * a.numY + y) * 2 * n * m;
                 for (int e = tid; e < n * m; e += T) {
@@ -458,11 +462,12 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             }
             LineStop stop;
             stop.init(a.ctl.omega, rate_hint);
-            float omega = stop.omega;
+            float omega = stop.omega, omega_last = omega;
             bool res64 = precise_first;
             int status = 0, it = 0, par = 0;
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
+                omega_last = omega;
                 if (zero) line_iteration<LD, 0, NL, FULL, true>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
                 else if (!res64) line_iteration<LD, 0, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
                 else if (semi) line_iteration<LD, 3, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
@@ -480,6 +485,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 const int ln = tid & 31;
                 float delta = warp_max(ln < NW ? red[(par * 2 + 0) * NW + ln] : 0.f);
                 float vm = warp_max(ln < NW ? red[(par * 2 + 1) * NW + ln] : 0.f);
+                if (it == 0 && !precise_first) semi = semi_now();
                 par ^= 1;
                 ++it;
                 if (!isfinite(delta) || !isfinite(vm)) {
@@ -526,14 +532,29 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 }
             }
             rate_hint = stop.final_rate();
-            // ---- outputs ------------------------------------------------------
-            if (tid == 0) nonfinite_flag = 0;
+            // ---- outputs (the planes are complete: the last reduction barrier) --
+            if (!NL && !a.ret_V && !(a.ctl.noise_sigma > 0.f) && omega_last == 1.f) {
+                // After a bitline pass at omega 1 every bitline equation holds, and
+                // summed down a column they telescope to
+                //   sum_i g_ij (u_ij - d_ij) = gw d_(n-1)j :
+                // the column current is the current through its last wire segment
+                // to ground (to the FP32 rounding of that node, ~1e-7 relative).
+                for (int j = tid; j < m; j += T) {
+                    const float dl = D[swz<LD>(n - 1, j)];
+                    const size_t o = ((size_t)b * a.numX + x) * ldG + (size_t)y * m + j;
+                    if (f64) static_cast<double *>(a.out)[o] = (double)gw * (double)dl;
+                    else static_cast<float *>(a.out)[o] = gw * dl;
+                    if (!isfinite(dl)) nonfinite_flag = 1;
+                }
+            } else if (f64) {
+                line_outputs<LD, double, NL>(a, Gs, U, D, vin_s, n, m, b, x, y, gw, nonfinite_flag);
+            } else {
+                line_outputs<LD, float, NL>(a, Gs, U, D, vin_s, n, m, b, x, y, gw, nonfinite_flag);
+            }
             __syncthreads();
-            if (f64) line_outputs<LD, double, NL>(a, Gs, U, D, vin_s, n, m, b, x, y, gw, nonfinite_flag);
-            else line_outputs<LD, float, NL>(a, Gs, U, D, vin_s, n, m, b, x, y, gw, nonfinite_flag);
-            __syncthreads();
-            if (nonfinite_flag) status |= FADESIM_ST_NONFINITE;
             if (tid == 0) {
+                if (nonfinite_flag) status |= FADESIM_ST_NONFINITE;
+                nonfinite_flag = 0;
                 if (a.iters_out) a.iters_out[((long long)b * a.numX + x) * a.numY + y] = it;
                 st_solves += 1;
                 st_iters += it;
