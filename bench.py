@@ -246,11 +246,17 @@ def check_accuracy(acc, G, vin, torch, k=8):
     planes, _, _ = acc.ir_drop_gs_ex(ti, tg, nv, ROWS, COLS, k, 1, g_wire=1 / R_WIRE, ret_V=2, method="line",
                                      vectors_per_cta=nv)
     planes = planes.cpu().numpy()
-    err = 0.0
+    # the currents as the timed run returns them (FP32 in and out)
+    cur, _, _ = acc.ir_drop_gs_ex(ti.float(), tg.float(), nv, ROWS, COLS, k, 1, g_wire=1 / R_WIRE, method="line",
+                                  vectors_per_cta=nv)
+    cur = cur.double().cpu().numpy()
+    err = cerr = 0.0
     for x in range(k):
         u, d = nodal.solve(G[x].astype(np.float64), 1 / R_WIRE, vin[:, x].astype(np.float64))
         err = max(err, np.abs(planes[:, x, 0, 0] - u).max(), np.abs(planes[:, x, 0, 1] - d).max())
-    return err
+        ref = nodal.currents(G[x].astype(np.float64), u, d)
+        cerr = max(cerr, np.abs(cur[:, x] - ref).max() / np.abs(ref).max())
+    return err, cerr
 
 
 def run_ours(args):
@@ -273,7 +279,7 @@ def run_ours(args):
     ti = torch.from_numpy(vin).cuda()
     B, X, Y = N_VEC, args.tiles, 1
     gw = 1 / R_WIRE
-    err = check_accuracy(acc, G, vin, torch)
+    err, cerr = check_accuracy(acc, G, vin, torch)
     stream = torch.cuda.current_stream()
 
     def step():
@@ -311,7 +317,8 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "quick": True, "tiles": X,
                               "kernel_ms": kern_ms, "line_iters_mean": stats["iters_sum"] / max(1, stats["solves"]),
-                              "max_node_err_v_sample": err, "clocks": clk.summary()}))
+                              "max_node_err_v_sample": err, "max_rel_current_err_sample": cerr,
+                              "clocks": clk.summary()}))
         if dist:
             dist.destroy_process_group()
         return
@@ -409,10 +416,11 @@ def run_ours(args):
                    "solver": "block line relaxation: FP32 tridiagonal line solves; residual in FP32, and in "
                              "float-float (FP64-class) arithmetic on the iteration expected to be the last, which "
                              "must pass the stop test; tol %.0e V (estimated max node error)" % args.tol,
-                   "accuracy_sample": "%d tiles x %d vectors solved as timed, FP64 oracle, both planes"
-                                      % (8, N_VEC),
+                   "accuracy_sample": "%d tiles x %d vectors solved as timed, FP64 oracle, both planes and "
+                                      "the FP32 currents" % (8, N_VEC),
                    "l2": "inputs %.0f MB vs 129 MB L2, no flush" % ((G.nbytes + vin.nbytes) / 1e6),
-                   "max_node_err_v_sample": err, "line_iters_mean": stats["iters_sum"] / max(1, stats["solves"]),
+                   "max_node_err_v_sample": err, "max_rel_current_err_sample": cerr,
+                   "line_iters_mean": stats["iters_sum"] / max(1, stats["solves"]),
                    "line_iters_max": stats["iters_max"],
                    "plain_rbsor_solves_per_s": rb_value,
                    "plain_rbsor_sweeps_mean": rb_stats["iters_sum"] / max(1, rb_stats["solves"]),

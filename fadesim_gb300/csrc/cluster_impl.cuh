@@ -656,11 +656,12 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                               gs_max * 3.f * vin_max * 1.1920929e-07f * 0.5f * Lmax * Lmax <= 0.125f * tol;
             LineStop stop;
             stop.init(a.ctl.omega, rate_hint);
-            float omega = stop.omega;
+            float omega = stop.omega, omega_last = omega;
             bool res64 = precise_first;
             int status = 0, it = 0, par = 0;
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
+                omega_last = omega;
                 const int mode = zero ? 4 : (!res64 ? 0 : (semi ? 3 : (ff ? 2 : 1)));
                 const float *pW = piv, *sW = piv + 2 * SEG * CL_T;
                 switch (mode) {
@@ -738,31 +739,52 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             }
             rate_hint = stop.final_rate();
             // ---- outputs --------------------------------------------------------
-            if (tid == 0) nonfinite_flag = 0;
-            __syncthreads();
-            if (f64)
-                cl_outputs<LDM, double, NL>(cluster, rank, a, Gs, U, D, vin, part, n, m, nloc, row0, b, x, y, gw,
-                                            nonfinite_flag);
-            else
-                cl_outputs<LDM, float, NL>(cluster, rank, a, Gs, U, D, vin, part, n, m, nloc, row0, b, x, y, gw,
-                                           nonfinite_flag);
-            if (nonfinite_flag) status |= FADESIM_ST_NONFINITE;
+            if (!NL && !a.ret_V && !(a.ctl.noise_sigma > 0.f) && omega_last == 1.f) {
+                // After a bitline pass at omega 1 the bitline equations hold, and a
+                // column's equations telescope to sum_i g_ij (u_ij - d_ij) = gw d_(n-1)j:
+                // the CTA holding the last row writes every current from its band
+                // alone (no cluster exchange); it records a non-finite value itself.
+                if (row0 <= n - 1 && n - 1 < row0 + nloc) {
+                    const int lr = n - 1 - row0;
+                    bool bad = false;
+                    for (int j = tid; j < m; j += CL_T) {
+                        const float dl = D[cswz<LDM>(lr, j)];
+                        const size_t o = ((size_t)b * a.numX + x) * ldG + (size_t)y * m + j;
+                        if (f64) static_cast<double *>(a.out)[o] = (double)gw * (double)dl;
+                        else static_cast<float *>(a.out)[o] = gw * dl;
+                        bad |= !isfinite(dl);
+                    }
+                    if (bad) atomicOr(&st_or, FADESIM_ST_NONFINITE);
+                }
+            } else {
+                if (tid == 0) nonfinite_flag = 0;
+                __syncthreads();
+                if (f64)
+                    cl_outputs<LDM, double, NL>(cluster, rank, a, Gs, U, D, vin, part, n, m, nloc, row0, b, x, y, gw,
+                                                nonfinite_flag);
+                else
+                    cl_outputs<LDM, float, NL>(cluster, rank, a, Gs, U, D, vin, part, n, m, nloc, row0, b, x, y, gw,
+                                               nonfinite_flag);
+                if (nonfinite_flag) status |= FADESIM_ST_NONFINITE;
+            }
             if (tid == 0 && rank == 0) {
                 if (a.iters_out) a.iters_out[((long long)b * a.numX + x) * a.numY + y] = it;
                 st_solves += 1;
                 st_iters += it;
                 st_max = max(st_max, it);
-                st_or |= status;
+                atomicOr(&st_or, status);  // the last row's CTA may flag it too
             }
         }
     }
     __syncthreads();
     cluster.sync();  // no CTA leaves while another may still read its shared memory
-    if (tid == 0 && rank == 0 && a.stats && st_solves) {
-        atomicAdd(&a.stats->solves, st_solves);
-        atomicAdd(&a.stats->iters_sum, st_iters);
-        atomicMax(&a.stats->iters_max, st_max);
-        atomicOr(&a.stats->status_or, st_or);
+    if (tid == 0 && a.stats) {
+        if (rank == 0 && st_solves) {
+            atomicAdd(&a.stats->solves, st_solves);
+            atomicAdd(&a.stats->iters_sum, st_iters);
+            atomicMax(&a.stats->iters_max, st_max);
+        }
+        if (st_or) atomicOr(&a.stats->status_or, st_or);  // rank 0's, or a flag of the last row's CTA
     }
 }
 
