@@ -47,6 +47,25 @@ def test_argument_errors_without_gpu():
     assert rc == -1
 
 
+def test_host_entry_argument_errors_without_gpu():
+    """The host-buffer entry checks its arguments before touching the device;
+    an empty batch is a no-op."""
+    from fadesim_gb300 import _lib
+    lib = _lib.load()
+    fake = ctypes.c_void_p(16)
+    args = lambda dtype, B, rows, inp, ret_V: (dtype, inp, fake, B, rows, 8, 1, 1, 10, 0.34, 1.9, 0, 0.0, 0, None, 0,
+                                               ret_V, fake, None, None, 0, None)
+    rc = lib.fadesim_ir_drop_gs_host(*args(7, 1, 8, fake, 0))
+    assert rc == -1 and b"dtype" in lib.fadesim_last_error()
+    rc = lib.fadesim_ir_drop_gs_host(*args(_lib.F32, 1, 1, fake, 0))
+    assert rc == -1 and b"row_size" in lib.fadesim_last_error()
+    rc = lib.fadesim_ir_drop_gs_host(*args(_lib.F32, 1, 8, fake, 3))
+    assert rc == -1 and b"ret_V" in lib.fadesim_last_error()
+    rc = lib.fadesim_ir_drop_gs_host(*args(_lib.F32, 1, 8, None, 0))
+    assert rc == -1 and b"null host buffer" in lib.fadesim_last_error()
+    assert lib.fadesim_ir_drop_gs_host(*args(_lib.F32, 0, 8, None, 0)) == 0
+
+
 def test_superposition_refuses_nonlinear_cells():
     from fadesim_gb300 import splitarr
     import pytest as _pt
