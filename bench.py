@@ -150,9 +150,9 @@ def cpu_baseline(seconds=12.0, max_solves=4096):
 
 
 def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
+    from fadesim_gb300.ranks import rank_env
+    if rank_env()[0] != 0:
+        return  # the host-core reference runs once, on rank 0
     steps = []
     for _ in range(args.warmup):
         cpu_baseline(seconds=2.0)
@@ -234,12 +234,13 @@ def large_nonideal(torch, acc, n_tiles=1024, n_vec=32, seed=5):
             "line_iters_mean": st["iters_sum"] / st["solves"], "status_or": st["status_or"]}
 
 
-def check_accuracy(acc, G, vin, torch, k=8):
+def check_accuracy(acc, G, vin, torch, k=None):
     """Max node error over both planes of k tiles x all their vectors, solved as
     the timed run solves them (same options, one work item per tile), against
     the FP64 oracle.  Float64 inputs give float64 planes, so the comparison is
     not limited by FP32 rounding of the output (the solve itself is FP32)."""
     from oracle import nodal
+    k = k or (8 if ROWS <= 128 else 2)
     nv = vin.shape[0]
     tg = torch.from_numpy(G[:k].astype(np.float64)).cuda()
     ti = torch.from_numpy(np.ascontiguousarray(vin[:, :k]).astype(np.float64)).cuda()
@@ -261,9 +262,8 @@ def check_accuracy(acc, G, vin, torch, k=8):
 
 def run_ours(args):
     import torch
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from fadesim_gb300 import ranks
+    rank, world, local = ranks.rank_env()
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
@@ -274,7 +274,7 @@ def run_ours(args):
     build()
     acc.options.tol_v = args.tol  # every call below, the drop-in included
 
-    G, vin = make_workload(1000 + rank, n_tiles=args.tiles)
+    G, vin = make_workload(ranks.workload_seed(1000, rank), n_tiles=args.tiles)
     tg = torch.from_numpy(G).cuda()
     ti = torch.from_numpy(vin).cuda()
     B, X, Y = N_VEC, args.tiles, 1
@@ -305,17 +305,14 @@ def run_ours(args):
         torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    ms = t0.elapsed_time(t1)
     kern_ms = statistics.mean(a.elapsed_time(b) for a, b in ev)
-    if dist:
-        tt = torch.tensor([ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = ranks.max_over_ranks(t0.elapsed_time(t1), dist, "cuda")
     solves_per_step = B * X * Y
-    value = solves_per_step * args.steps * world / (ms / 1e3)
+    value = ranks.job_rate(solves_per_step * args.steps, world, ms)
     if args.quick:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "quick": True, "tiles": X,
+                              "tile_size": ROWS,
                               "kernel_ms": kern_ms, "line_iters_mean": stats["iters_sum"] / max(1, stats["solves"]),
                               "max_node_err_v_sample": err, "max_rel_current_err_sample": cerr,
                               "clocks": clk.summary()}))
@@ -339,12 +336,8 @@ def run_ours(args):
     for _ in range(args.steps):
         acc.ir_drop_gs_host(hv, hG, B, ROWS, COLS, X, Y, 600, gw, out=hout)
     torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - h0) * 1e3
-    if dist:
-        tt = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
-    e2e_value = solves_per_step * args.steps * world / (e2e_ms / 1e3)
+    e2e_ms = ranks.max_over_ranks((time.perf_counter() - h0) * 1e3, dist, "cuda")
+    e2e_value = ranks.job_rate(solves_per_step * args.steps, world, e2e_ms)
     # the same through the device-buffer drop-in with the caller's own copies
     # (copy in, solve, copy out in sequence on one stream), for comparison
     e0 = torch.cuda.Event(enable_timing=True)
@@ -356,7 +349,8 @@ def run_ours(args):
         hout.copy_(o, non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_serial_value = solves_per_step * args.steps * world / (e0.elapsed_time(e1) / 1e3)
+    e2e_serial_value = ranks.job_rate(solves_per_step * args.steps, world,
+                                      ranks.max_over_ranks(e0.elapsed_time(e1), dist, "cuda"))
 
     # the same step under the other residual precisions (one timed step each)
     variants = {}
@@ -465,7 +459,14 @@ def main():
     ap.add_argument("--no-warm", action="store_true", help="skip training/evaluating the learned warm start")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident solve only (no e2e, comparator or CPU baseline); for profiling")
+    ap.add_argument("--size", type=int, default=128,
+                    help="with --quick: tile size N (N x N tiles; 256 and 512 run on the cluster kernels)")
     args = ap.parse_args()
+    if args.size != 128:
+        if not args.quick:
+            ap.error("--size is a --quick (profiling) option; the metric is quoted on 128x128 tiles")
+        global ROWS, COLS
+        ROWS = COLS = args.size
     if args.impl == "reference":
         run_reference(args)
     else:
