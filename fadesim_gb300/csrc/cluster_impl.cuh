@@ -523,6 +523,10 @@ __device__ __forceinline__ void cl_outputs(cg::cluster_group &cluster, int rank,
 template <int LDM, bool NL, bool FULL>
 __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a) {
     constexpr int C = CCfg<LDM>::C, RPC = CCfg<LDM>::RPC, SEG = CL_SEG;
+    // The wordline pass keeps its bounds tests even on full tiles: without them
+    // the compiler hoists a whole segment's loads and spills (measured); the
+    // bitline pass, where the cross-band scans dominate, drops them.
+    constexpr bool WFULL = false;
     constexpr int LPW_B = CCfg<LDM>::LPW_B;
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
@@ -665,11 +669,11 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 const int mode = zero ? 4 : (!res64 ? 0 : (semi ? 3 : (ff ? 2 : 1)));
                 const float *pW = piv, *sW = piv + 2 * SEG * CL_T;
                 switch (mode) {
-                    case 4: cl_word_pass<LDM, 0, NL, true, true, FULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    case 0: cl_word_pass<LDM, 0, NL, false, false, FULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    case 3: cl_word_pass<LDM, 3, NL, false, false, FULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    case 2: cl_word_pass<LDM, 2, NL, false, false, FULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    default: cl_word_pass<LDM, 1, NL, false, false, FULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
+                    case 4: cl_word_pass<LDM, 0, NL, true, true, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
+                    case 0: cl_word_pass<LDM, 0, NL, false, false, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
+                    case 3: cl_word_pass<LDM, 3, NL, false, false, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
+                    case 2: cl_word_pass<LDM, 2, NL, false, false, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
+                    default: cl_word_pass<LDM, 1, NL, false, false, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
                 }
                 __syncthreads();
                 for (int j = tid; j < LDM; j += CL_T) {
@@ -791,8 +795,10 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
 // Launch helpers for one size (instantiated by linegs_cluster_<LDM>.cu).
 template <int LDM>
 cudaError_t cl_launch_cfg_t(int *clusters, const SolveArgs *a, int grid, cudaStream_t st) {
+    // full tiles (n = m = LDM) of linear cells run the bounds-free bitline pass
     void (*kern)(SolveArgs) = (a && a->ctl.nl) ? line_relax_cluster_kernel<LDM, true, false>
-                                               : line_relax_cluster_kernel<LDM, false, false>;
+                              : (a && a->n == LDM && a->m == LDM) ? line_relax_cluster_kernel<LDM, false, true>
+                                                                  : line_relax_cluster_kernel<LDM, false, false>;
     const size_t smem = cl_smem_floats<LDM>() * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
