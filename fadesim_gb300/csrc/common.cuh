@@ -50,16 +50,33 @@ __device__ __forceinline__ TIO vin_exact(const void *p, size_t i, bool f64, floa
     return (TIO)staged;
 }
 
-// sinh(t)/t, t >= 0 (series below 1e-2: truncation < 1e-10)
-__device__ __forceinline__ float sinhc(float t) { return t < 1e-2f ? fmaf(t * t, 1.f / 6.f, 1.f) : sinhf(t) / t; }
+// sinh(t)/t, t >= 0.  Below t = 1 its Maclaurin series sum_k t^(2k) / (2k+1)!
+// in Horner form in u = t^2, through t^12 / 13! (the first omitted term,
+// t^14 / 15! < 8e-13, is far below FP32 resolution); above, sinhf(t) / t.
+// Cell voltages of a read stay well under 1 / a, so the series is the path.
+__device__ __forceinline__ float sinhc(float t) {
+    if (t < 1.f) {
+        const float u = t * t;
+        float p = 1.f / 6227020800.f;        // 1 / 13!
+        p = fmaf(p, u, 1.f / 39916800.f);    // 1 / 11!
+        p = fmaf(p, u, 1.f / 362880.f);      // 1 / 9!
+        p = fmaf(p, u, 1.f / 5040.f);        // 1 / 7!
+        p = fmaf(p, u, 1.f / 120.f);         // 1 / 5!
+        p = fmaf(p, u, 1.f / 6.f);           // 1 / 3!
+        return fmaf(p, u, 1.f);
+    }
+    return sinhf(t) / t;
+}
 
 // Chord conductance I(V)/V of the reference's sinh cell at cell voltage V for
 // a cell at position z between the on and off states:
-// 1/R(V), R(V) = (1-z) |V| / (b_on sinh(a_on |V|)) + z |V| / (b_off sinh(a_off |V|)).
+// 1/R(V), R(V) = (1-z) |V| / (b_on sinh(a_on |V|)) + z |V| / (b_off sinh(a_off |V|)),
+// i.e. with s = sinh(a x) / (a x) and r0 = 1 / (a b):  R = (1-z) r0_on / s_on + z r0_off / s_off,
+// evaluated as s_on s_off / ((1-z) r0_on s_off + z r0_off s_on) -- one division.
 __device__ __forceinline__ float nl_geff(float z, float V, const SolveCtl &c) {
     const float x = fabsf(V);
-    const float R = (1.f - z) * c.nl_r0_on / sinhc(c.nl_a_on * x) + z * c.nl_r0_off / sinhc(c.nl_a_off * x);
-    return 1.f / R;
+    const float s_on = sinhc(c.nl_a_on * x), s_off = sinhc(c.nl_a_off * x);
+    return __fdividef(s_on * s_off, fmaf((1.f - z) * c.nl_r0_on, s_off, z * c.nl_r0_off * s_on));
 }
 
 __device__ __forceinline__ float nl_z(float g, const SolveCtl &c) {
