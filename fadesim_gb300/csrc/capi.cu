@@ -245,6 +245,7 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
         a.ctl.nl_a_off = (float)q[4];
         a.ctl.nl_r0_on = (float)(1.0 / (q[2] * q[3]));
         a.ctl.nl_r0_off = (float)(1.0 / (q[4] * q[5]));
+        a.ctl.nl_single_a = q[2] == q[4] ? 1 : 0;
     }
     if (opts && opts->read_noise_sigma > 0) {
         a.ctl.noise_sigma = (float)opts->read_noise_sigma;

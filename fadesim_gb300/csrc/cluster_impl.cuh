@@ -231,7 +231,7 @@ __device__ __forceinline__ void cl_word_pass(float *__restrict__ U, const float 
             if (FULL || (ok && p < m)) {
                 const int q = Bw ^ k;
                 const float o = ZOTH ? 0.f : D[q];
-                const float gs = NL ? nl_geff(Gs[q], (cur + vl) - o, ctl) * inv_gw : Gs[q];
+                const float gs = NL ? nl_gs(Gs[q], (cur + vl) - o, ctl, inv_gw) : Gs[q];
                 r = line_residual_s<true, RES>(prev, cur, nxt, gs, o, vl, true, (FULL && k + 1 < SEG) || p + 1 < m);
             }
             x[k] = r;
@@ -302,7 +302,7 @@ __device__ __forceinline__ void cl_bit_pass(cg::cluster_group &cluster, int rank
             if (FULL || (ok && lr < nloc)) {
                 const int q = qk(k);
                 const float o = U[q];
-                const float gs = NL ? nl_geff(Gs[q], (o + vin[lr]) - cur, ctl) * inv_gw : Gs[q];
+                const float gs = NL ? nl_gs(Gs[q], (o + vin[lr]) - cur, ctl, inv_gw) : Gs[q];
                 r = line_residual_s<false, RES>(prev, cur, nxt, gs, o, vin[lr], k > 0 || p0 > 0 || row0 > 0, true);
             }
             x[k] = r;
@@ -492,7 +492,7 @@ __device__ __forceinline__ void cl_outputs(cg::cluster_group &cluster, int rank,
                 if (lr < nloc) {
                     const int q = cswz<LDM>(lr, j);
                     const float V = (U[q] + vin[lr]) - D[q];
-                    float Ic = (NL ? nl_geff(Gs[q], V, a.ctl) : Gs[q] * gw) * V;
+                    float Ic = (NL ? nl_g(Gs[q], V, a.ctl, gw) : Gs[q] * gw) * V;
                     if (a.ctl.noise_sigma > 0.f)
                         Ic *= 1.f + a.ctl.noise_sigma * normal_from(a.ctl.noise_seed,
                                                                     ((unsigned long long)b * a.numX + x) * a.numY + y,
@@ -612,7 +612,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 // the sinh cells keep their on/off position; the linear values served the pivots
                 for (int e = tid; e < RPC * LDM; e += CL_T) {
                     const int q = cswz<LDM>(e / LDM, e % LDM);
-                    Gs[q] = nl_z(Gs[q], a.ctl);
+                    Gs[q] = nl_cell(Gs[q], a.ctl, inv_gw);
                 }
                 __syncthreads();
             }

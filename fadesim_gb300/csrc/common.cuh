@@ -27,6 +27,7 @@ struct SolveCtl {
     float nl_R_on, nl_inv_dR;        // z = (1/g_lin - R_on) / (R_off - R_on), clamped at 0
     float nl_a_on, nl_a_off;         // a of I = b sinh(a V)
     float nl_r0_on, nl_r0_off;       // 1 / (a b): the state's resistance at V -> 0
+    int nl_single_a;                 // a_on == a_off: g(V) = g(0) sinh(a V) / (a V) for every cell
     // additive read noise on every cell current: N(0, (sigma I_cell)^2)
     float noise_sigma;
     unsigned long long noise_seed;
@@ -81,6 +82,25 @@ __device__ __forceinline__ float nl_geff(float z, float V, const SolveCtl &c) {
 
 __device__ __forceinline__ float nl_z(float g, const SolveCtl &c) {
     return g > 0.f ? fmaxf(0.f, (1.f / g - c.nl_R_on) * c.nl_inv_dR) : 0.f;
+}
+
+// What the line kernels keep per sinh cell, from its linear conductance g:
+// its position z -- or, when both states share a (nl_single_a), its V -> 0
+// conductance over gw, 1 / (gw ((1-z) r0_on + z r0_off)): then the chord
+// conductance is that times sinh(a|V|) / (a|V|), with no division per use.
+__device__ __forceinline__ float nl_cell(float g, const SolveCtl &c, float inv_gw) {
+    const float z = nl_z(g, c);
+    return c.nl_single_a ? inv_gw / fmaf(1.f - z, c.nl_r0_on, z * c.nl_r0_off) : z;
+}
+
+// Chord conductance over gw at cell voltage V, from the value nl_cell keeps.
+__device__ __forceinline__ float nl_gs(float cell, float V, const SolveCtl &c, float inv_gw) {
+    return c.nl_single_a ? cell * sinhc(c.nl_a_on * fabsf(V)) : nl_geff(cell, V, c) * inv_gw;
+}
+
+// Chord conductance at cell voltage V, from the value nl_cell keeps.
+__device__ __forceinline__ float nl_g(float cell, float V, const SolveCtl &c, float gw) {
+    return c.nl_single_a ? (cell * gw) * sinhc(c.nl_a_on * fabsf(V)) : nl_geff(cell, V, c);
 }
 
 // Standard normal from a counter (splitmix64 hash, Box-Muller): the same value

@@ -136,7 +136,7 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
                 const float o = ZOTH ? 0.f : oth[q], vv = WORD ? vl : vin_s[vpad(p)];
                 // g / gw: stored, or the sinh cell's at the present cell voltage
                 const float gs =
-                    NL ? nl_geff(Gs[q], WORD ? (cur + vv) - o : (o + vv) - cur, ctl) * inv_gw : Gs[q];
+                    NL ? nl_gs(Gs[q], WORD ? (cur + vv) - o : (o + vv) - cur, ctl, inv_gw) : Gs[q];
                 const bool has_l = WORD || k > 0 || p0 > 0;
                 const bool has_r = !WORD || (FULL && k + 1 < SEG) || p + 1 < L;
                 r = line_residual_s<WORD, RES>(prev, cur, nxt, gs, o, vv, has_l, has_r);
@@ -328,7 +328,7 @@ __device__ __forceinline__ void line_outputs(const SolveArgs &a, const float *Gs
                     const TIO V =
                         ((TIO)U[q] + vin_exact<TIO>(a.input, ((size_t)b * a.numX + x) * n + i, a.f64,
                                                     vin_s[vpad(i)])) - (TIO)D[q];
-                    TIO Ic = (TIO)(NL ? nl_geff(Gs[q], (float)V, a.ctl) : Gs[q] * gw) * V;
+                    TIO Ic = (TIO)(NL ? nl_g(Gs[q], (float)V, a.ctl, gw) : Gs[q] * gw) * V;
                     if (a.ctl.noise_sigma > 0.f)
                         Ic *= (TIO)1 + (TIO)(a.ctl.noise_sigma *
                                              normal_from(a.ctl.noise_seed,
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 // the sinh cells keep their on/off position; the linear values served the pivots
                 for (int e = tid; e < n * m; e += T) {
                     const int i = e / m, j = e - i * m;
-                    Gs[swz<LD>(i, j)] = nl_z(Gs[swz<LD>(i, j)], a.ctl);
+                    Gs[swz<LD>(i, j)] = nl_cell(Gs[swz<LD>(i, j)], a.ctl, inv_gw);
                 }
                 __syncthreads();
             }
