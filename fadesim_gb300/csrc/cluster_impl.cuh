@@ -792,13 +792,13 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
     }
 }
 
-// Launch helpers for one size (instantiated by linegs_cluster_<LDM>.cu).
-template <int LDM>
+// Launch helpers for one size and cell law (instantiated by linegs_cluster_<LDM>[nl].cu).
+template <int LDM, bool NL>
 cudaError_t cl_launch_cfg_t(int *clusters, const SolveArgs *a, int grid, cudaStream_t st) {
-    // full tiles (n = m = LDM) of linear cells run the bounds-free bitline pass
-    void (*kern)(SolveArgs) = (a && a->ctl.nl) ? line_relax_cluster_kernel<LDM, true, false>
-                              : (a && a->n == LDM && a->m == LDM) ? line_relax_cluster_kernel<LDM, false, true>
-                                                                  : line_relax_cluster_kernel<LDM, false, false>;
+    // full tiles (n = m = LDM) run the bounds-free bitline pass
+    const bool full = a && a->n == LDM && a->m == LDM;
+    void (*kern)(SolveArgs) =
+        full ? line_relax_cluster_kernel<LDM, NL, true> : line_relax_cluster_kernel<LDM, NL, false>;
     const size_t smem = cl_smem_floats<LDM>() * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

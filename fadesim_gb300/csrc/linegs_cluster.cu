@@ -6,6 +6,8 @@ namespace fadesim {
 
 cudaError_t cl_launch_cfg_256(int *clusters, const SolveArgs *a, int grid, cudaStream_t st);
 cudaError_t cl_launch_cfg_512(int *clusters, const SolveArgs *a, int grid, cudaStream_t st);
+cudaError_t cl_launch_cfg_256_nl(int *clusters, const SolveArgs *a, int grid, cudaStream_t st);
+cudaError_t cl_launch_cfg_512_nl(int *clusters, const SolveArgs *a, int grid, cudaStream_t st);
 
 int cluster_relax_ld(int n, int m) {
     const int L = n > m ? n : m;
@@ -27,8 +29,10 @@ cudaError_t cluster_relax_occupancy(int ld, int, int *clusters) {
 }
 
 cudaError_t launch_cluster_relax(const SolveArgs &a, int ld, int, int grid, cudaStream_t st) {
-    if (ld == 256) return cl_launch_cfg_256(nullptr, &a, grid, st);
-    if (ld == 512) return cl_launch_cfg_512(nullptr, &a, grid, st);
+    if (ld == 256)
+        return a.ctl.nl ? cl_launch_cfg_256_nl(nullptr, &a, grid, st) : cl_launch_cfg_256(nullptr, &a, grid, st);
+    if (ld == 512)
+        return a.ctl.nl ? cl_launch_cfg_512_nl(nullptr, &a, grid, st) : cl_launch_cfg_512(nullptr, &a, grid, st);
     return cudaErrorInvalidValue;
 }
 
