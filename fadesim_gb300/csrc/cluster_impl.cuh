@@ -163,39 +163,41 @@ __device__ __forceinline__ void seg_apply_bwd(float (&x)[SEG], const float (&c)[
 
 // The value entering this CTA's part of a bitline: the affine maps (c, y) the
 // CTAs above published, composed in order onto 0 (forward), or those of the
-// CTAs below, bottom up (backward).  Remote maps are fetched four at a time so
-// that their latencies overlap.
+// CTAs below, bottom up (backward).  Remote maps are fetched four (16-CTA
+// clusters: eight) at a time so that their latencies overlap.
 template <int C>
 __device__ __forceinline__ float compose_above(cg::cluster_group &cluster, const float *agg, int col, int rank) {
+    constexpr int K = C > 8 ? 8 : 4;
     float v = 0.f;
 #pragma unroll 1
-    for (int r0 = 0; r0 < rank; r0 += 4) {
-        float2 mp[4];
+    for (int r0 = 0; r0 < rank; r0 += K) {
+        float2 mp[K];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
+        for (int t = 0; t < K; ++t) {
             const int r = r0 + t;
             mp[t] = (r < C && r < rank) ? *reinterpret_cast<const float2 *>(cluster.map_shared_rank(agg, r) + 2 * col)
                                         : make_float2(1.f, 0.f);
         }
 #pragma unroll
-        for (int t = 0; t < 4; ++t) v = fmaf(mp[t].x, v, mp[t].y);
+        for (int t = 0; t < K; ++t) v = fmaf(mp[t].x, v, mp[t].y);
     }
     return v;
 }
 template <int C>
 __device__ __forceinline__ float compose_below(cg::cluster_group &cluster, const float *agg, int col, int rank) {
+    constexpr int K = C > 8 ? 8 : 4;
     float v = 0.f;
 #pragma unroll 1
-    for (int r0 = C - 1; r0 > rank; r0 -= 4) {
-        float2 mp[4];
+    for (int r0 = C - 1; r0 > rank; r0 -= K) {
+        float2 mp[K];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
+        for (int t = 0; t < K; ++t) {
             const int r = r0 - t;
             mp[t] = (r >= 0 && r > rank) ? *reinterpret_cast<const float2 *>(cluster.map_shared_rank(agg, r) + 2 * col)
                                          : make_float2(1.f, 0.f);
         }
 #pragma unroll
-        for (int t = 0; t < 4; ++t) v = fmaf(mp[t].x, v, mp[t].y);
+        for (int t = 0; t < K; ++t) v = fmaf(mp[t].x, v, mp[t].y);
     }
     return v;
 }
