@@ -217,15 +217,21 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     dmax = fmaxf(dmax, omega * dm);
 }
 
-// Chain multipliers gw / pivot of every line of the tile (pivots in FP64),
-// written in the order each pass thread reads them (k * T + tid), and the
-// product of each segment's multipliers as the pass forms it.
+// Chain multipliers gw / pivot of every line of the tile, written in the order
+// each pass thread reads them (k * T + tid), and the product of each segment's
+// multipliers as the pass forms it.  In units of gw the pivots follow
+//   P_0 = D_0,  P_q = D_q - 1 / P_(q-1),  D_q = (1 or 2) + g_q / gw,  c_q = 1 / P_q,
+// and g / gw is ~1e-6 of the link terms, so D and P are carried in float-float
+// (hi + lo, error-free FP32 transforms) -- FP64 precision on the FP32 pipe:
+// the FP64 pipe of this part is slow, and this recurrence is serial.  The
+// reciprocal is the correctly rounded FP32 one corrected by one float-float
+// step.  Matches an FP64 evaluation of the same recurrence to 1 ulp of the
+// FP32 multipliers.
 template <int LD>
-__device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ piv, int n, int m, float gwf) {
+__device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ piv, int n, int m, float gw) {
     constexpr int SEG = LineCfg<LD>::SEG;
     constexpr int T = LineCfg<LD>::T;
     constexpr int LPW = LineCfg<LD>::LPW;
-    const double gw = gwf;
     const int tid = threadIdx.x;
     if (tid < 2 * LD) {
         const bool word = tid < LD;
@@ -235,24 +241,33 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
         float *dst = word ? piv : piv + SEG * T;
         float *prod = piv + 2 * SEG * T + (word ? 0 : T);
         const int tw_base = (line / LPW) * 32 + (line % LPW);
-        double p = 1.0, ipv_prev = 0.0;
+        float rh = 0.f, rl = 0.f;  // 1 / P_(q-1) in float-float
         float seg_prod = 1.f;
         for (int q = 0; q < LD; ++q) {
-            double ipv = 0.0;
+            float cf = 0.f;
             if (line < NL && q < L) {
-                const double g = word ? Gs[swz<LD>(line, q)] : Gs[swz<LD>(q, line)];
+                const float gs = __fdiv_rn(word ? Gs[swz<LD>(line, q)] : Gs[swz<LD>(q, line)], gw);
                 // wordline: source link + right link (absent at the end) + cell
                 // bitline:  upper link (absent at the top) + lower link + cell
-                const double diag = word ? gw + (q + 1 < L ? gw : 0.0) + g : (q > 0 ? gw : 0.0) + gw + g;
-                p = (q == 0) ? diag : fma(-gw * gw, ipv_prev, diag);
-                // 1/p: correctly rounded FP32 reciprocal refined by one Newton
-                // step in FP64 (~1e-14 relative; FP64 division is slow here)
-                const double r0 = (double)__frcp_rn((float)p);
-                ipv = r0 * fma(-p, r0, 2.0);
-                ipv_prev = ipv;
+                const float base = word ? (q + 1 < L ? 2.f : 1.f) : (q > 0 ? 2.f : 1.f);
+                float dh, dl;
+                two_sum(base, gs, dh, dl);
+                float ph = dh, pl = dl;
+                if (q > 0) {
+                    float sh, sl;
+                    two_sum(dh, -rh, sh, sl);
+                    sl = __fadd_rn(sl, __fsub_rn(dl, rl));
+                    ph = __fadd_rn(sh, sl);
+                    pl = __fsub_rn(sl, __fsub_rn(ph, sh));
+                }
+                const float r = __frcp_rn(ph);
+                float e = __fmaf_rn(-ph, r, 1.f);  // exact: 1 - ph * RN(1/ph)
+                e = __fmaf_rn(-pl, r, e);
+                rh = r;
+                rl = __fmul_rn(e, r);
+                cf = __fadd_rn(rh, rl);
             }
             const int tw = tw_base + (q / SEG) * LPW;
-            const float cf = (float)(gw * ipv);
             dst[(q % SEG) * T + tw] = cf;
             seg_prod *= cf;
             if (q % SEG == SEG - 1) {
