@@ -356,15 +356,51 @@ __device__ __forceinline__ void cl_bit_pass(cg::cluster_group &cluster, int rank
     dmax = fmaxf(dmax, omega * dm);
 }
 
+// Float-float helpers for the band products below (error-free FP32 transforms).
+struct FF {
+    float h, l;
+};
+__device__ __forceinline__ FF ff_norm(float s, float e) {
+    const float h = __fadd_rn(s, e);
+    return {h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+// x * y - z
+__device__ __forceinline__ FF ff_mul_sub(FF x, FF y, FF z) {
+    const float ph = __fmul_rn(x.h, y.h);
+    const float pl = __fmaf_rn(x.h, y.h, -ph) + (__fmul_rn(x.h, y.l) + __fmul_rn(x.l, y.h));
+    float sh, sl;
+    two_sum(ph, -z.h, sh, sl);
+    return ff_norm(sh, __fadd_rn(sl, __fsub_rn(pl, z.l)));
+}
+// x * y + z * w
+__device__ __forceinline__ FF ff_dot2(FF x, FF y, FF z, FF w) {
+    const float ph = __fmul_rn(x.h, y.h), qh = __fmul_rn(z.h, w.h);
+    const float pl = __fmaf_rn(x.h, y.h, -ph) + (__fmul_rn(x.h, y.l) + __fmul_rn(x.l, y.h));
+    const float ql = __fmaf_rn(z.h, w.h, -qh) + (__fmul_rn(z.h, w.l) + __fmul_rn(z.l, w.h));
+    float sh, sl;
+    two_sum(ph, qh, sh, sl);
+    return ff_norm(sh, __fadd_rn(sl, __fadd_rn(pl, ql)));
+}
+// x * 2^k (exact)
+__device__ __forceinline__ FF ff_scale(FF x, float p2) { return {x.h * p2, x.l * p2}; }
+// 2^-e with 2^e the binade of |v| (v finite, nonzero): keeps composed states near 1
+__device__ __forceinline__ float inv_binade(float v) {
+    const int e = ((__float_as_int(v) >> 23) & 0xff) - 127;
+    return __int_as_float((127 - e) << 23);
+}
+
 // Chain multipliers gw / pivot of the CTA's wordline rows and of its part of
-// every bitline column (pivots in FP64), written in the order the pass threads
-// read them, with each segment's product; uses mob (4 doubles per column) as
-// scratch read by the other CTAs.
+// every bitline column, written in the order the pass threads read them, with
+// each segment's product; uses mob (8 floats per column) as scratch read by the
+// other CTAs.  Everything in units of gw and in float-float (FP64-class
+// precision on the FP32 pipe; the FP64 pipe of this part is slow): the row
+// recurrences step by ff_pivot_step; a bitline's pivot entering a band comes
+// from the bands above as a product of Moebius maps P -> D - 1 / P, i.e.
+// [num; den] <- [[D, -1], [1, 0]] [num; den] with P = num / den.
 template <int LDM>
 __device__ void cl_pivots(cg::cluster_group &cluster, int rank, const float *__restrict__ Gs, float *__restrict__ piv,
-                          double *__restrict__ mob, int row0, int nloc, int n, int m, float gwf) {
+                          float *__restrict__ mob, int row0, int nloc, int n, int m, float gw) {
     constexpr int RPC = CCfg<LDM>::RPC, SEG = CL_SEG, LPW_W = CCfg<LDM>::LPW_W, LPW_B = CCfg<LDM>::LPW_B;
-    const double gw = gwf, gw2 = (double)gwf * (double)gwf;
     float *pivW = piv, *pivB = piv + SEG * CL_T, *prodW = piv + 2 * SEG * CL_T, *prodB = prodW + CL_T;
     // 1. each column's 2x2 product over the band (jobs < LDM) and the wordline
     //    rows' multipliers (jobs LDM .. LDM + RPC - 1)
@@ -372,20 +408,15 @@ __device__ void cl_pivots(cg::cluster_group &cluster, int rank, const float *__r
         if (job >= LDM) {
             const int lr = job - LDM;
             const int tw_base = (lr / LPW_W) * 32 + (lr % LPW_W);
-            double p = 1.0, ipp = 0.0;
-            float sp = 1.f;
+            float rh = 0.f, rl = 0.f, sp = 1.f;
             for (int c = 0; c < LDM; ++c) {
-                double ipv = 0.0;
+                float f = 0.f;
                 if (lr < nloc && c < m) {
-                    const double diag = gw + (c + 1 < m ? gw : 0.0) + (double)Gs[cswz<LDM>(lr, c)];
-                    p = (c == 0) ? diag : fma(-gw2, ipp, diag);
-                    // 1/p: correctly rounded FP32 reciprocal refined by one Newton step in FP64
-                    const double r0 = (double)__frcp_rn((float)p);
-                    ipv = r0 * fma(-p, r0, 2.0);
-                    ipp = ipv;
+                    // source link + right link (absent at the end) + cell
+                    const float gs = __fdiv_rn(Gs[cswz<LDM>(lr, c)], gw);
+                    f = ff_pivot_step(c + 1 < m ? 2.f : 1.f, gs, c == 0, rh, rl);
                 }
                 const int tw = tw_base + (c / SEG) * LPW_W;
-                const float f = (float)(gw * ipv);
                 pivW[(c % SEG) * CL_T + tw] = f;
                 sp *= f;
                 if (c % SEG == SEG - 1) {
@@ -394,55 +425,61 @@ __device__ void cl_pivots(cg::cluster_group &cluster, int rank, const float *__r
                 }
             }
         } else {
-            // p_r = num/den with [num; den] <- [[diag_r, -gw^2], [1, 0]] [num; den]
+            // the band's map: the product of its rows' [[D, -1], [1, 0]], from
+            // the identity; entries grow at most ~linearly with the rows for
+            // D near 2, so the band needs no rescaling until its end
             const int jb = job;
-            double a = 1, b = 0, c = 0, d = 1;  // band product, starts as identity
+            FF a = {1.f, 0.f}, b = {0.f, 0.f}, c = {0.f, 0.f}, d = {1.f, 0.f};
             if (jb < m) {
                 for (int lr = 0; lr < nloc; ++lr) {
-                    const double diag = (row0 + lr > 0 ? gw : 0.0) + gw + (double)Gs[cswz<LDM>(lr, jb)];
-                    const double na = diag * a - gw2 * c, nb = diag * b - gw2 * d;
+                    // upper link (absent at the top) + lower link + cell
+                    FF D;
+                    two_sum(row0 + lr > 0 ? 2.f : 1.f, __fdiv_rn(Gs[cswz<LDM>(lr, jb)], gw), D.h, D.l);
+                    const FF na = ff_mul_sub(D, a, c), nb = ff_mul_sub(D, b, d);
                     c = a;
                     d = b;
                     a = na;
                     b = nb;
-                    const double sc = 1.0 / fmax(fmax(fabs(a), fabs(b)), fmax(fabs(c), fabs(d)));
-                    a *= sc;
-                    b *= sc;
-                    c *= sc;
-                    d *= sc;
                 }
+                const float k = inv_binade(fmaxf(fmaxf(fabsf(a.h), fabsf(b.h)), fmaxf(fabsf(c.h), fabsf(d.h))));
+                a = ff_scale(a, k);
+                b = ff_scale(b, k);
+                c = ff_scale(c, k);
+                d = ff_scale(d, k);
             }
-            mob[4 * jb + 0] = a;
-            mob[4 * jb + 1] = b;
-            mob[4 * jb + 2] = c;
-            mob[4 * jb + 3] = d;
+            float *M = mob + 8 * jb;
+            M[0] = a.h; M[1] = a.l; M[2] = b.h; M[3] = b.l;
+            M[4] = c.h; M[5] = c.l; M[6] = d.h; M[7] = d.l;
         }
     }
     cluster.sync();
     for (int jb = threadIdx.x; jb < LDM; jb += CL_T) {
         // state entering this band: [1; 0] (no row above the first) through the bands above
-        double num = 1.0, den = 0.0;
+        FF num = {1.f, 0.f}, den = {0.f, 0.f};
         for (int r = 0; r < rank; ++r) {
-            const double *M = cluster.map_shared_rank(mob, r) + 4 * jb;
-            const double nn = M[0] * num + M[1] * den, dd = M[2] * num + M[3] * den;
-            const double sc = 1.0 / fmax(fabs(nn), fabs(dd));
-            num = nn * sc;
-            den = dd * sc;
+            const float *M = cluster.map_shared_rank(mob, r) + 8 * jb;
+            const FF nn = ff_dot2({M[0], M[1]}, num, {M[2], M[3]}, den);
+            const FF dd = ff_dot2({M[4], M[5]}, num, {M[6], M[7]}, den);
+            const float k = inv_binade(fmaxf(fabsf(nn.h), fabsf(dd.h)));
+            num = ff_scale(nn, k);
+            den = ff_scale(dd, k);
+        }
+        // 1 / P of the row above the band: den / num in float-float
+        float rh = 0.f, rl = 0.f;
+        if (rank > 0 && num.h != 0.f) {
+            rh = __fdiv_rn(den.h, num.h);
+            const float e = __fmaf_rn(-num.h, rh, den.h) + __fsub_rn(den.l, __fmul_rn(rh, num.l));
+            rl = __fdiv_rn(e, num.h);
         }
         const int tb_base = (jb / LPW_B) * 32 + (jb % LPW_B);
-        double ipp = (rank > 0 && num != 0.0) ? den / num : 0.0;  // 1 / p of the row above the band
         float sp = 1.f;
         for (int lr = 0; lr < RPC; ++lr) {
-            double ipv = 0.0;
+            float f = 0.f;
             if (jb < m && lr < nloc) {
-                const double diag = (row0 + lr > 0 ? gw : 0.0) + gw + (double)Gs[cswz<LDM>(lr, jb)];
-                const double p = (row0 + lr == 0) ? diag : fma(-gw2, ipp, diag);
-                const double r0 = (double)__frcp_rn((float)p);
-                ipv = r0 * fma(-p, r0, 2.0);
-                ipp = ipv;
+                const float gs = __fdiv_rn(Gs[cswz<LDM>(lr, jb)], gw);
+                f = ff_pivot_step(row0 + lr > 0 ? 2.f : 1.f, gs, row0 + lr == 0, rh, rl);
             }
             const int tb = tb_base + (lr / SEG) * LPW_B;
-            const float f = (float)(gw * ipv);
             pivB[(lr % SEG) * CL_T + tb] = f;
             sp *= f;
             if (lr % SEG == SEG - 1) {
@@ -539,7 +576,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
     float *hup = D + RPC * LDM;
     float *hdn = hup + LDM;
     float *vin = hdn + LDM;
-    float *aux = vin + RPC;         // 8 * LDM floats: 2x2 FP64 products, or aggF/aggB/partial currents
+    float *aux = vin + RPC;         // 8 * LDM floats: 2x2 float-float band products, or aggF/aggB/partial currents
     float *red = aux + 8 * LDM;     // [2][2][CL_NW]
     float *cred = red + 4 * CL_NW;  // [2][2] this CTA's maxima, read by the cluster
     float *aggF = aux, *aggB = aux + 2 * LDM, *part = aux + 4 * LDM;
@@ -584,7 +621,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                                          : 0.f;
             }
             __syncthreads();
-            cl_pivots<LDM>(cluster, rank, Gs, piv, reinterpret_cast<double *>(aux), row0, nloc, n, m, gw);
+            cl_pivots<LDM>(cluster, rank, Gs, piv, aux, row0, nloc, n, m, gw);
             __syncthreads();
             if (!NL) {
                 // the passes work in units of gw: g / gw

@@ -23,6 +23,32 @@ __device__ __forceinline__ double widen_f64(float f) {
     return __hiloint2double((int)hi, (int)((b & 7u) << 29));
 }
 
+// One step of a line's pivot recurrence in units of gw, in float-float:
+//   P = D - 1 / P_prev (P = D on the first node),  D = base + gs,
+// base the node's link count (1 or 2) and gs = g / gw ~1e-6 of it, so D and P
+// need more than FP32 (FP64-class precision on the FP32 pipe).  (rh, rl) holds
+// 1 / P_prev on entry and 1 / P on return: the correctly rounded FP32
+// reciprocal corrected by one float-float step.  Returns the chain multiplier
+// gw / pivot = 1 / P rounded to FP32.
+__device__ __forceinline__ float ff_pivot_step(float base, float gs, bool first, float &rh, float &rl) {
+    float dh, dl;
+    two_sum(base, gs, dh, dl);
+    float ph = dh, pl = dl;
+    if (!first) {
+        float sh, sl;
+        two_sum(dh, -rh, sh, sl);
+        sl = __fadd_rn(sl, __fsub_rn(dl, rl));
+        ph = __fadd_rn(sh, sl);
+        pl = __fsub_rn(sl, __fsub_rn(ph, sh));
+    }
+    const float r = __frcp_rn(ph);
+    float e = __fmaf_rn(-ph, r, 1.f);  // exact: 1 - ph * RN(1/ph)
+    e = __fmaf_rn(-pl, r, e);
+    rh = r;
+    rl = __fmul_rn(e, r);
+    return __fadd_rn(rh, rl);
+}
+
 // Residual of one node's line equation at the current iterate (amperes):
 //   r = gl (prev - cur) + gr (nxt - cur) + g src,
 //   src = (o - vin) - cur on a wordline (o = bitline node, cur = u - vin),
@@ -135,6 +161,8 @@ namespace fadesim {
 //                   previous vector of the same tile (hint), or unknown: the
 //                   rate of the first step, larger than the later ones, is
 //                   what the first prediction needs.
+// (The per-iteration quotients use the fast division: the estimates need a
+// few digits, and every thread evaluates them after every iteration.)
 struct LineStop {
     float omega;
     bool adapt;
@@ -159,7 +187,7 @@ struct LineStop {
         if (it == 0 || !(rho > 0.f)) return false;
         const float r = fminf(rho, 0.999f);
         const float next = h0 * r;
-        const float est_next = next * r / (1.f - r);
+        const float est_next = __fdividef(next * r, 1.f - r);
         const float floor_v = 4.f * 1.1920929e-07f * vm;
         return est_next <= 4.f * fmaxf(tol, floor_v) || h0 <= 1e-4f * vm || (it >= 3 && h0 >= 0.9f * h1);
     }
@@ -176,12 +204,12 @@ struct LineStop {
         h0 = delta;
         if (it == 1) return delta <= 0.f;
         const float floor_v = 4.f * 1.1920929e-07f * vm;
-        const float ratio = prev > 0.f ? delta / prev : 0.f;
+        const float ratio = prev > 0.f ? __fdividef(delta, prev) : 0.f;
         const float rate3 = (it >= 4 && h3 > 0.f) ? cbrtf(delta / h3) : 0.f;
         rho = fmaxf(fmaxf(ratio, rate3), omega - 1.f);
         if (omega > 1.f) rho = fmaxf(rho, 0.5f);
         if (it == 2) first = ratio;
-        const float est = rho < 0.999f ? delta * rho / (1.f - rho) : INFINITY;
+        const float est = rho < 0.999f ? __fdividef(delta * rho, 1.f - rho) : INFINITY;
         const bool stalled = delta <= floor_v && ratio >= 0.9f;
         if (adapt) {
             if (it == 3 && ratio > 0.05f && ratio < 1.f) {

@@ -222,11 +222,9 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
 // multipliers as the pass forms it.  In units of gw the pivots follow
 //   P_0 = D_0,  P_q = D_q - 1 / P_(q-1),  D_q = (1 or 2) + g_q / gw,  c_q = 1 / P_q,
 // and g / gw is ~1e-6 of the link terms, so D and P are carried in float-float
-// (hi + lo, error-free FP32 transforms) -- FP64 precision on the FP32 pipe:
-// the FP64 pipe of this part is slow, and this recurrence is serial.  The
-// reciprocal is the correctly rounded FP32 one corrected by one float-float
-// step.  Matches an FP64 evaluation of the same recurrence to 1 ulp of the
-// FP32 multipliers.
+// (ff_pivot_step) -- FP64 precision on the FP32 pipe: the FP64 pipe of this
+// part is slow, and this recurrence is serial.  Matches an FP64 evaluation of
+// the same recurrence to 1 ulp of the FP32 multipliers.
 template <int LD>
 __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ piv, int n, int m, float gw) {
     constexpr int SEG = LineCfg<LD>::SEG;
@@ -250,22 +248,7 @@ __device__ void line_pivots(const float *__restrict__ Gs, float *__restrict__ pi
                 // wordline: source link + right link (absent at the end) + cell
                 // bitline:  upper link (absent at the top) + lower link + cell
                 const float base = word ? (q + 1 < L ? 2.f : 1.f) : (q > 0 ? 2.f : 1.f);
-                float dh, dl;
-                two_sum(base, gs, dh, dl);
-                float ph = dh, pl = dl;
-                if (q > 0) {
-                    float sh, sl;
-                    two_sum(dh, -rh, sh, sl);
-                    sl = __fadd_rn(sl, __fsub_rn(dl, rl));
-                    ph = __fadd_rn(sh, sl);
-                    pl = __fsub_rn(sl, __fsub_rn(ph, sh));
-                }
-                const float r = __frcp_rn(ph);
-                float e = __fmaf_rn(-ph, r, 1.f);  // exact: 1 - ph * RN(1/ph)
-                e = __fmaf_rn(-pl, r, e);
-                rh = r;
-                rl = __fmul_rn(e, r);
-                cf = __fadd_rn(rh, rl);
+                cf = ff_pivot_step(base, gs, q == 0, rh, rl);
             }
             const int tw = tw_base + (q / SEG) * LPW;
             dst[(q % SEG) * T + tw] = cf;
