@@ -606,6 +606,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
     }
     long long cached_tile = -1;
     float rate_hint = 0.f;  // first-step rate of the previous vector of this tile (cluster-uniform)
+    float omega_prev = 0.f; // final relaxation factor of that vector (cluster-uniform)
     float gs_max = 0.f;     // largest g / gw of the tile (cluster-uniform, linear cells)
     for (long long item = cid; item < a.nitems; item += ncl) {
         const long long tile = item / a.nchunks;
@@ -657,6 +658,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             }
             cached_tile = tile;
             rate_hint = 0.f;
+            omega_prev = 0.f;
         }
         for (int b = b0; b < b1; ++b) {
             __syncthreads();
@@ -698,7 +700,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             const bool semi = !NL && ff &&
                               gs_max * 3.f * vin_max * 1.1920929e-07f * 0.5f * Lmax * Lmax <= 0.125f * tol;
             LineStop stop;
-            stop.init(a.ctl.omega, rate_hint);
+            stop.init(a.ctl.omega, rate_hint, omega_prev);
             float omega = stop.omega, omega_last = omega;
             bool res64 = precise_first;
             int status = 0, it = 0, par = 0;
@@ -781,6 +783,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 }
             }
             rate_hint = stop.final_rate();
+            omega_prev = stop.omega;
             // ---- outputs --------------------------------------------------------
             if (!NL && !a.ret_V && !(a.ctl.noise_sigma > 0.f) && omega_last == 1.f) {
                 // After a bitline pass at omega 1 the bitline equations hold, and a

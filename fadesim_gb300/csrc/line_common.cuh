@@ -149,7 +149,11 @@ namespace fadesim {
 //   relaxation      block Gauss-Seidel for 3 iterations, then
 //                   omega = 2 / (1 + sqrt(1 - rho_GS)) (Young, 2-block
 //                   partition), refined at iteration 12 from the observed SOR
-//                   rate lambda via mu^2 = (lambda + omega - 1)^2 / (lambda omega^2).
+//                   rate lambda via mu^2 = (lambda + omega - 1)^2 / (lambda omega^2);
+//                   a vector after the first of a tile takes, at iteration 3,
+//                   the final omega of the previous one instead (same matrix:
+//                   the early rates underestimate rho_GS, the refined omega
+//                   does not).
 //   precision       (adaptive schedule) the next iteration's residual is made
 //                   precise when it is expected to be the last one -- its
 //                   predicted estimate delta * rho * rho / (1 - rho) within 4x
@@ -171,9 +175,11 @@ struct LineStop {
     float rho;             // rate used by the last update (0: unknown)
     float hint;            // rate carried from the previous vector of the tile (0: none)
     float first;           // delta_2 / delta_1 of this solve (0: not yet)
+    float omega_hint;      // final omega of the previous vector of the tile (<= 1: none)
 
-    __device__ __forceinline__ void init(float omega_fixed, float rate_hint = 0.f) {
+    __device__ __forceinline__ void init(float omega_fixed, float rate_hint = 0.f, float omega_prev = 0.f) {
         adapt = !(omega_fixed > 0.f);
+        omega_hint = omega_prev;
         omega = adapt ? 1.f : omega_fixed;
         it = 0;
         h0 = h1 = h2 = h3 = 0.f;
@@ -212,7 +218,9 @@ struct LineStop {
         const float est = rho < 0.999f ? __fdividef(delta * rho, 1.f - rho) : INFINITY;
         const bool stalled = delta <= floor_v && ratio >= 0.9f;
         if (adapt) {
-            if (it == 3 && ratio > 0.05f && ratio < 1.f) {
+            if (it == 3 && omega_hint > 1.f) {
+                omega = omega_hint;
+            } else if (it == 3 && ratio > 0.05f && ratio < 1.f) {
                 omega = fminf(1.95f, 2.f / (1.f + sqrtf(1.f - ratio)));
             } else if (it == 12 && omega > 1.f && rate3 > omega - 1.f + 0.02f && rate3 < 1.f) {
                 const float mu2 = (rate3 + omega - 1.f) * (rate3 + omega - 1.f) / (rate3 * omega * omega);

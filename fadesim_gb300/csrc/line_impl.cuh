@@ -371,6 +371,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
     const bool precise_first = kres == 1;    // every iteration precise
     long long cached_tile = -1;
     float rate_hint = 0.f;                   // final rate of the previous vector of this tile
+    float omega_prev = 0.f;                  // final relaxation factor of that vector
     float gs_max = 0.f;                      // largest g / gw of the tile (linear cells)
     __shared__ unsigned long long st_solves, st_iters;  // this CTA's counters (thread 0)
     __shared__ int st_max, st_or;
@@ -418,6 +419,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             }
             cached_tile = tile;
             rate_hint = 0.f;
+            omega_prev = 0.f;
         }
         for (int b = b0; b < b1; ++b) {
             // (the tile setup and the previous solve's outputs end with a barrier)
@@ -459,7 +461,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 __syncthreads();
             }
             LineStop stop;
-            stop.init(a.ctl.omega, rate_hint);
+            stop.init(a.ctl.omega, rate_hint, omega_prev);
             float omega = stop.omega, omega_last = omega;
             bool res64 = precise_first;
             int status = 0, it = 0, par = 0;
@@ -504,7 +506,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     zero = !precise_first;
                     warm = false;
                     status |= FADESIM_ST_WARM_REJECTED;
-                    stop.init(a.ctl.omega, rate_hint);
+                    stop.init(a.ctl.omega, rate_hint, omega_prev);
                     omega = stop.omega;
                     res64 = precise_first;
                     continue;
@@ -530,6 +532,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 }
             }
             rate_hint = stop.final_rate();
+            omega_prev = stop.omega;
             // ---- outputs (the planes are complete: the last reduction barrier) --
             if (!NL && !a.ret_V && !(a.ctl.noise_sigma > 0.f) && omega_last == 1.f) {
                 // After a bitline pass at omega 1 every bitline equation holds, and
