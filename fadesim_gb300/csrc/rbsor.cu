@@ -9,7 +9,9 @@
 //
 // One CTA solves one (tile, vector) pair at a time with both deviation planes
 // and the conductances in shared memory; every half-sweep each cell updates
-// exactly one of its two nodes (branch-free pointer selection).  Updates are
+// exactly one of its two nodes (branch-free pointer selection).  Thread t owns
+// column t % 128 at rows t / 128 + 8k: consecutive lanes walk consecutive
+// columns (conflict-free), and no index is divided per cell.  Updates are
 // in residual form, v += omega * r / diag, on deviations from the ideal state
 // (FP32 throughout).  The stop test runs every CHECK sweeps on the observed
 // contraction of the sweep-to-sweep change.
@@ -22,6 +24,7 @@ namespace fadesim {
 constexpr int RB_THREADS = 1024;
 constexpr int RB_CHECK = 8;
 constexpr int RB_MAXL = 128;
+constexpr int RB_ROWSTEP = RB_THREADS / RB_MAXL;  // rows between a thread's cells
 
 __host__ __device__ inline int rb_ld(int m) { return m + 1; }
 
@@ -45,6 +48,7 @@ __global__ void __launch_bounds__(RB_THREADS, 1) rbsor_kernel(SolveArgs a) {
     TIO *out = static_cast<TIO *>(a.out);
     const float gw = a.gw;
     const float omega = a.ctl.omega;
+    const int col = tid % RB_MAXL, row0 = tid / RB_MAXL;  // this thread's column and first row
     long long cached_tile = -1;
 
     for (long long item = blockIdx.x; item < a.nitems; item += gridDim.x) {
@@ -82,31 +86,34 @@ __global__ void __launch_bounds__(RB_THREADS, 1) rbsor_kernel(SolveArgs a) {
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
                 for (int c = 0; c < 2; ++c) {
-                    for (int e = tid; e < n * m; e += RB_THREADS) {
-                        const int i = e / m, j = e - i * m;
-                        const bool isU = ((i + j) & 1) == c;
-                        const int q = i * LDP + j;
+                    // thread -> cells (i0 + 8k, j): along its rows the colour of a cell
+                    // does not change, so a thread relaxes one plane per half-sweep
+                    if (col < m) {
+                        const bool isU = ((row0 + col) & 1) == c;
                         float *self = isU ? U : D;
                         const float *oth = isU ? D : U;
-                        // neighbours along the line: wordline (j-1, j+1), bitline (i-1, i+1)
-                        const bool has1 = isU ? true : (i > 0);        // source link / upper link
-                        const bool in1 = isU ? (j > 0) : (i > 0);      // neighbour is an unknown
-                        const bool has2 = isU ? (j + 1 < m) : true;    // right link / lower link
-                        const bool in2 = isU ? (j + 1 < m) : (i + 1 < n);
-                        const int o1 = isU ? -1 : -LDP, o2 = isU ? 1 : LDP;
-                        const float v = self[q];
-                        const float n1 = in1 ? self[q + o1] : 0.f;
-                        const float n2 = in2 ? self[q + o2] : 0.f;
-                        const float g = Gs[q];
-                        const float vi = vin_s[i];
-                        const float src = isU ? (oth[q] - vi) - v : (oth[q] + vi) - v;
-                        const float g1 = has1 ? gw : 0.f, g2 = has2 ? gw : 0.f;
-                        const float r = g1 * (n1 - v) + g2 * (n2 - v) + g * src;
-                        const float dv = __fdividef(omega * r, g1 + g2 + g);
-                        const float nv = v + dv;
-                        self[q] = nv;
-                        dmax = isfinite(nv) ? fmaxf(dmax, fabsf(dv)) : INFINITY;
-                        vmax = fmaxf(vmax, fabsf(nv));
+                        const int o = isU ? 1 : LDP;  // neighbour stride along the line
+                        for (int i = row0; i < n; i += RB_ROWSTEP) {
+                            const int q = i * LDP + col;
+                            // neighbours along the line: wordline (j-1, j+1), bitline (i-1, i+1)
+                            const bool has1 = isU ? true : (i > 0);        // source link / upper link
+                            const bool in1 = isU ? (col > 0) : (i > 0);      // neighbour is an unknown
+                            const bool has2 = isU ? (col + 1 < m) : true;    // right link / lower link
+                            const bool in2 = isU ? (col + 1 < m) : (i + 1 < n);
+                            const float v = self[q];
+                            const float n1 = in1 ? self[q - o] : 0.f;
+                            const float n2 = in2 ? self[q + o] : 0.f;
+                            const float g = Gs[q];
+                            const float vi = vin_s[i];
+                            const float src = isU ? (oth[q] - vi) - v : (oth[q] + vi) - v;
+                            const float g1 = has1 ? gw : 0.f, g2 = has2 ? gw : 0.f;
+                            const float r = g1 * (n1 - v) + g2 * (n2 - v) + g * src;
+                            const float dv = __fdividef(omega * r, g1 + g2 + g);
+                            const float nv = v + dv;
+                            self[q] = nv;
+                            dmax = isfinite(nv) ? fmaxf(dmax, fabsf(dv)) : INFINITY;
+                            vmax = fmaxf(vmax, fabsf(nv));
+                        }
                     }
                     __syncthreads();
                 }
