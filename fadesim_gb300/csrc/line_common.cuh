@@ -88,6 +88,20 @@ __device__ __forceinline__ float line_residual(float prev, float cur, float nxt,
     }
 }
 
+// The line part of a residual, (prev - cur) [if has_l] + (nxt - cur) [if has_r],
+// as hi + lo with hi + lo equal to it up to one rounding of the low part:
+// (prev + nxt) exactly by TwoSum, then minus k cur (k = 1 or 2 links, exact
+// scaling) by a second TwoSum -- two error-free sums where the differences
+// taken one by one need three.
+__device__ __forceinline__ void lap_exact(float prev, float cur, float nxt, bool has_l, bool has_r, float &hi,
+                                          float &lo) {
+    float sh, sl, th, tl;
+    two_sum(has_l ? prev : 0.f, has_r ? nxt : 0.f, sh, sl);
+    two_sum(sh, -((has_l && has_r) ? 2.f * cur : (has_l || has_r ? cur : 0.f)), th, tl);
+    hi = th;
+    lo = __fadd_rn(tl, sl);
+}
+
 // The same residual divided by gw (volts), with gs = g / gw:
 //   r' = hl (prev - cur) + hr (nxt - cur) + gs src,  hl, hr in {0, 1}.
 // Solving T' d = r' with T' = T / gw gives the same correction without a
@@ -103,13 +117,11 @@ __device__ __forceinline__ float line_residual_s(float prev, float cur, float nx
         const double lap = (has_l ? dp - dc : 0.0) + (has_r ? dn - dc : 0.0);  // exact: widened FP32 inputs
         return __double2float_rn(fma(widen_f64(gs), src, lap));
     } else if (RES == 2) {
-        float sh, sl, th, tl, a1h, a1l, a2h, a2l, lh, ll;
+        float sh, sl, th, tl, lh, ll;
         two_sum(o, WORD ? -vin : vin, sh, sl);           // o -/+ vin
         two_sum(sh, -cur, th, tl);                        // ... - own
-        two_sum(has_l ? prev : cur, -cur, a1h, a1l);      // left difference (0 if absent)
-        two_sum(has_r ? nxt : cur, -cur, a2h, a2l);       // right difference (0 if absent)
-        two_sum(a1h, a2h, lh, ll);
-        const float lap_lo = __fadd_rn(ll, __fadd_rn(a1l, a2l));
+        float lap_lo;
+        lap_exact(prev, cur, nxt, has_l, has_r, lh, lap_lo);
         const float src_lo = __fadd_rn(tl, sl);
         const float ph = __fmul_rn(gs, th), pl = __fmaf_rn(gs, th, -ph);
         float rh, rl;
@@ -120,11 +132,8 @@ __device__ __forceinline__ float line_residual_s(float prev, float cur, float nx
         // the line differences exactly (their rounding dominates when the wire
         // carries a large gradient), the cell term in FP32: for tiles whose cell
         // term is small enough that its rounding stays far below the tolerance
-        float a1h, a1l, a2h, a2l, lh, ll;
-        two_sum(has_l ? prev : cur, -cur, a1h, a1l);
-        two_sum(has_r ? nxt : cur, -cur, a2h, a2l);
-        two_sum(a1h, a2h, lh, ll);
-        const float lap_lo = __fadd_rn(ll, __fadd_rn(a1l, a2l));
+        float lh, lap_lo;
+        lap_exact(prev, cur, nxt, has_l, has_r, lh, lap_lo);
         const float src = WORD ? (o - vin) - cur : (o + vin) - cur;
         return __fadd_rn(lh, __fmaf_rn(gs, src, lap_lo));
     } else {
