@@ -49,45 +49,6 @@ __device__ __forceinline__ float ff_pivot_step(float base, float gs, bool first,
     return __fadd_rn(rh, rl);
 }
 
-// Residual of one node's line equation at the current iterate (amperes):
-//   r = gl (prev - cur) + gr (nxt - cur) + g src,
-//   src = (o - vin) - cur on a wordline (o = bitline node, cur = u - vin),
-//   src = (o + vin) - cur on a bitline (o = wordline deviation, cur = d),
-// gl = gw if has_l else 0, gr = gw if has_r else 0.  Unknowns are deviations
-// from the ideal state, so every difference is between nearby values.
-// RES 0: FP32.  RES 1: FP64 (widened on the integer pipe).  RES 2: float-float,
-// error-free FP32 transforms carrying every difference and product exactly.
-template <bool WORD, int RES>
-__device__ __forceinline__ float line_residual(float prev, float cur, float nxt, float g, float o, float vin,
-                                               bool has_l, bool has_r, float gw) {
-    if (RES == 1) {
-        const double dp = widen_f64(prev), dc = widen_f64(cur), dn = widen_f64(nxt);
-        const double src = WORD ? (widen_f64(o) - widen_f64(vin)) - dc : (widen_f64(o) + widen_f64(vin)) - dc;
-        // second difference along the line (exact: widened FP32 inputs)
-        const double lap = (has_l && has_r) ? fma(-2.0, dc, dp + dn) : (has_l ? dp - dc : (has_r ? dn - dc : 0.0));
-        return __double2float_rn(fma((double)gw, lap, widen_f64(g) * src));
-    } else if (RES == 2) {
-        float sh, sl, th, tl, a1h, a1l, a2h, a2l, lh, ll;
-        two_sum(o, WORD ? -vin : vin, sh, sl);           // o -/+ vin
-        two_sum(sh, -cur, th, tl);                        // ... - own
-        two_sum(has_l ? prev : cur, -cur, a1h, a1l);      // left difference (0 if absent)
-        two_sum(has_r ? nxt : cur, -cur, a2h, a2l);       // right difference (0 if absent)
-        two_sum(a1h, a2h, lh, ll);
-        const float lap_lo = __fadd_rn(ll, __fadd_rn(a1l, a2l));
-        const float src_lo = __fadd_rn(tl, sl);
-        const float p1h = __fmul_rn(gw, lh), p1l = __fmaf_rn(gw, lh, -p1h);
-        const float p2h = __fmul_rn(g, th), p2l = __fmaf_rn(g, th, -p2h);
-        float rh, rl;
-        two_sum(p1h, p2h, rh, rl);
-        const float lo = __fadd_rn(__fadd_rn(rl, __fadd_rn(p1l, p2l)), __fmaf_rn(gw, lap_lo, __fmul_rn(g, src_lo)));
-        return __fadd_rn(rh, lo);
-    } else {
-        const float gl = has_l ? gw : 0.f, gr = has_r ? gw : 0.f;
-        const float src = WORD ? (o - vin) - cur : (o + vin) - cur;
-        return gl * (prev - cur) + gr * (nxt - cur) + g * src;
-    }
-}
-
 // The line part of a residual, (prev - cur) [if has_l] + (nxt - cur) [if has_r],
 // as hi + lo with hi + lo equal to it up to one rounding of the low part:
 // (prev + nxt) exactly by TwoSum, then minus k cur (k = 1 or 2 links, exact
@@ -102,8 +63,13 @@ __device__ __forceinline__ void lap_exact(float prev, float cur, float nxt, bool
     lo = __fadd_rn(tl, sl);
 }
 
-// The same residual divided by gw (volts), with gs = g / gw:
-//   r' = hl (prev - cur) + hr (nxt - cur) + gs src,  hl, hr in {0, 1}.
+// Residual of one node's line equation at the current iterate, divided by gw
+// (volts), with gs = g / gw:
+//   r' = hl (prev - cur) + hr (nxt - cur) + gs src,  hl, hr in {0, 1},
+//   src = (o - vin) - cur on a wordline (o = bitline node, cur = u - vin),
+//   src = (o + vin) - cur on a bitline (o = wordline deviation, cur = d);
+// unknowns are deviations from the ideal state, so every difference is
+// between nearby values.
 // Solving T' d = r' with T' = T / gw gives the same correction without a
 // multiply by gw per node; the line kernels store gs and the multipliers
 // gw / pivot.  RES 0 FP32, 1 FP64, 2 float-float, 3 float-float line
