@@ -42,6 +42,7 @@ EXPORTS = {
                                 ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _i, _vp],
     "fadesim_ir_drop_gs_warm": [_i, _vp, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp, ctypes.POINTER(SolveOpts),
                                 ctypes.POINTER(SolveStats), _vp, _vp],
+    "fadesim_release_memory": [],
     "fadesim_last_error": [],
     "fadesim_version": [],
     "fadesim_ir_drop_gs_noalloc_f32": [_vp, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp],

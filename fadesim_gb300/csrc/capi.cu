@@ -1,10 +1,12 @@
 // C ABI of the solver (include/fadesim_gb300.h): argument checks, method
-// choice, scratch and launches.  Scratch is stream-ordered (cudaMallocAsync /
-// cudaFreeAsync on the caller's stream), so a call never synchronises unless
-// the caller asks for stats or the reference's delta break.
+// choice, scratch and launches.  Scratch is stream-ordered (from the library's
+// memory pool, freed with cudaFreeAsync, on the caller's stream), so a call
+// never synchronises unless the caller asks for stats or the reference's
+// delta break.
 #include <math.h>
 #include <stdio.h>
 
+#include <mutex>
 #include <string>
 
 #include "kernels.h"
@@ -26,7 +28,55 @@ static int fail(int code, const std::string &msg) {
 
 namespace fadesim {
 int report_error(int code, const char *msg) { return fail(code, msg); }
+
+namespace {
+constexpr int MAX_DEVICES = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pools[MAX_DEVICES] = {};
+
+cudaError_t lib_pool(cudaMemPool_t *pool) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        e = cudaMemPoolCreate(&g_pools[dev], &props);
+        if (e != cudaSuccess) {
+            g_pools[dev] = nullptr;
+            return e;
+        }
+        // keep what the pool has mapped between calls (fadesim_release_memory trims it)
+        unsigned long long keep = ~0ull;
+        e = cudaMemPoolSetAttribute(g_pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+        if (e != cudaSuccess) return e;
+    }
+    *pool = g_pools[dev];
+    return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t lib_malloc_async(void **p, size_t bytes, cudaStream_t st) {
+    cudaMemPool_t pool;
+    cudaError_t e = lib_pool(&pool);
+    if (e != cudaSuccess) return e;
+    return cudaMallocFromPoolAsync(p, bytes, pool, st);
+}
 }  // namespace fadesim
+
+extern "C" int fadesim_release_memory(void) {
+    std::lock_guard<std::mutex> lock(fadesim::g_pool_mutex);
+    for (int d = 0; d < fadesim::MAX_DEVICES; ++d) {
+        if (!fadesim::g_pools[d]) continue;
+        const cudaError_t e = cudaMemPoolTrimTo(fadesim::g_pools[d], 0);
+        if (e != cudaSuccess) return fail(FADESIM_E_CUDA, std::string("cudaMemPoolTrimTo: ") + cudaGetErrorString(e));
+    }
+    return FADESIM_OK;
+}
 
 extern "C" const char *fadesim_last_error(void) { return g_err.c_str(); }
 extern "C" const char *fadesim_version(void) { return "fadesim_gb300 0.1 (sm_103a)"; }
@@ -130,7 +180,7 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
     Scratch scr;
     scr.st = st;
     const size_t bytes = scratch_floats * sizeof(float) + sizeof(DevStats) + 256;
-    CUDA_TRY(cudaMallocAsync(&scr.p, bytes, st));
+    CUDA_TRY(lib_malloc_async(&scr.p, bytes, st));
     DevStats *dst = reinterpret_cast<DevStats *>(scr.p);
     a.stats = dst;
     a.scratch = reinterpret_cast<float *>(reinterpret_cast<char *>(scr.p) + 256);
@@ -152,7 +202,7 @@ int run_sweeps(int dtype, SolveArgs a, int iter_times, double gw, double beta, i
     const size_t plane = (size_t)a.B * a.numX * a.numY * a.n * a.m * es;
     Scratch scr;
     scr.st = st;
-    CUDA_TRY(cudaMallocAsync(&scr.p, 2 * plane + 256, st));
+    CUDA_TRY(lib_malloc_async(&scr.p, 2 * plane + 256, st));
     unsigned int *moved = reinterpret_cast<unsigned int *>(scr.p);
     void *U = reinterpret_cast<char *>(scr.p) + 256;
     void *D = reinterpret_cast<char *>(U) + plane;

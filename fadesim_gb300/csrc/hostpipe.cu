@@ -15,6 +15,7 @@
 // are strided by numX in host memory; a group's slice is one pitched copy.
 #include <string.h>
 
+#include <mutex>
 #include <string>
 
 #include "kernels.h"
@@ -22,19 +23,45 @@
 namespace {
 
 constexpr int NSLOT = 3;
+constexpr int MAX_DEVICES = 64;
 
+// The slot streams of each device, created on first use and kept for the
+// process (calls from several host threads share them: their work then
+// queues behind each other, each call with its own buffers).
+std::mutex g_stream_mutex;
+cudaStream_t g_streams[MAX_DEVICES][NSLOT] = {};
+
+cudaError_t slot_streams(cudaStream_t *out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_stream_mutex);
+    for (int s = 0; s < NSLOT; ++s) {
+        if (!g_streams[dev][s]) {
+            e = cudaStreamCreateWithFlags(&g_streams[dev][s], cudaStreamNonBlocking);
+            if (e != cudaSuccess) {
+                g_streams[dev][s] = nullptr;
+                return e;
+            }
+        }
+        out[s] = g_streams[dev][s];
+    }
+    return cudaSuccess;
+}
+
+// This call's slot buffers: freed (stream-ordered, back to the library's
+// pool) once the slots' work is done, on every return path.
 struct SlotSet {
     cudaStream_t st[NSLOT] = {};
     void *buf[NSLOT] = {};
+    int n = 0;
     ~SlotSet() {
-        for (int s = 0; s < NSLOT; ++s) {
-            if (st[s]) {
-                cudaStreamSynchronize(st[s]);
-                if (buf[s]) cudaFreeAsync(buf[s], st[s]);
-                cudaStreamSynchronize(st[s]);
-                cudaStreamDestroy(st[s]);
-            }
+        for (int s = 0; s < n; ++s) {
+            cudaStreamSynchronize(st[s]);
+            if (buf[s]) cudaFreeAsync(buf[s], st[s]);
         }
+        for (int s = 0; s < n; ++s) cudaStreamSynchronize(st[s]);
     }
 };
 
@@ -92,10 +119,14 @@ extern "C" int fadesim_ir_drop_gs_host(int dtype, const void *input, const void 
     e = cudaEventRecord(start, caller);
     SlotSet slots;
     const int nslot = ngroups < NSLOT ? ngroups : NSLOT;
+    cudaStream_t streams[NSLOT];
+    if (e == cudaSuccess) e = slot_streams(streams);
     for (int s = 0; s < nslot && e == cudaSuccess; ++s) {
-        e = cudaStreamCreateWithFlags(&slots.st[s], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(slots.st[s], start, 0);
-        if (e == cudaSuccess) e = cudaMallocAsync(&slots.buf[s], al(gbytes) + al(ibytes) + al(obytes), slots.st[s]);
+        slots.st[s] = streams[s];
+        slots.n = s + 1;
+        e = cudaStreamWaitEvent(slots.st[s], start, 0);
+        if (e == cudaSuccess)
+            e = fadesim::lib_malloc_async(&slots.buf[s], al(gbytes) + al(ibytes) + al(obytes), slots.st[s]);
     }
     cudaEventDestroy(start);
     if (e != cudaSuccess) return fail_cuda("slot setup", e);

@@ -243,7 +243,7 @@ int fam_run(bool ir2s, const void *input_v, const void *G_v, int B, OuShape o, i
     const size_t rsum = (size_t)B * numX * numY * o.n * o.noy, csum = (size_t)B * numX * numY * o.m * o.nox;
     const size_t bytes = (ir2s ? 4 : 2) * plane_elems * sizeof(S) + (ir2s ? (rsum + csum) * sizeof(S) : 0) + 256;
     char *buf = nullptr;
-    cudaError_t e = cudaMallocAsync((void **)&buf, bytes, st);
+    cudaError_t e = lib_malloc_async((void **)&buf, bytes, st);
     if (e != cudaSuccess) return fail(FADESIM_E_CUDA, cudaGetErrorString(e));
     S *U = reinterpret_cast<S *>(buf), *D = U + plane_elems;
     S *U2 = ir2s ? D + plane_elems : nullptr, *D2 = ir2s ? U2 + plane_elems : nullptr;

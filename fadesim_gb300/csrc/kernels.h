@@ -29,6 +29,11 @@ struct SolveArgs {
 // Record msg as the message of fadesim_last_error() and return code.
 int report_error(int code, const char *msg);
 
+// Stream-ordered device allocation from the library's own memory pool on the
+// current device (created on first use, keeping freed memory for reuse, so
+// repeated calls do not map and unmap device memory); free with cudaFreeAsync.
+cudaError_t lib_malloc_async(void **p, size_t bytes, cudaStream_t st);
+
 // Block line relaxation, planes resident in shared memory (n, m <= 128).
 // Returns the LD (32/64/128) used, or 0 if the shape does not fit.
 int line_relax_ld(int n, int m);

@@ -118,6 +118,11 @@ int fadesim_ir_drop_gs_host(int dtype, const void *input, const void *G, int bat
                             int n_nonlinear_params, int ret_V, void *out, const fadesim_solve_opts *opts,
                             fadesim_solve_stats *stats, int group_x, void *stream);
 
+/* Return the device memory the library keeps for reuse (its stream-ordered scratch and staging
+ * buffers come from a per-device pool that keeps freed memory mapped between calls) to the
+ * system.  Call when no solve is in flight.  FADESIM_OK or FADESIM_E_CUDA. */
+int fadesim_release_memory(void);
+
 /* ---- the reference extension's other exports (split_arr_matmul.cu:1429-1437),
  * reproducing their iterates: same arguments and meaning, dtype (FADESIM_F32 /
  * FADESIM_F64) typing input, G and out; linear cells (nonlinear cells: ir_drop_gs).

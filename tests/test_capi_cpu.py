@@ -71,3 +71,9 @@ def test_superposition_refuses_nonlinear_cells():
     import pytest as _pt
     with _pt.raises(ValueError):
         splitarr.superposition_solver(splitarr.ArrayConfig(nonlinear_cell_enable=True))
+
+
+def test_release_memory_without_gpu():
+    """Nothing allocated yet: trimming the library's pools is a no-op."""
+    from fadesim_gb300 import _lib
+    assert _lib.load().fadesim_release_memory() == 0
