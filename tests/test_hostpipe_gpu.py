@@ -78,3 +78,15 @@ def test_host_argument_errors(acc):
         acc.ir_drop_gs_host(ti, tg, 1, 8, 8, 1, 1, tol=1e-8)
     empty = acc.ir_drop_gs_host(ti[:0], tg, 0, 8, 8, 1, 1)
     assert empty.shape == (0, 1, 8)
+
+
+def test_release_memory_between_calls(acc):
+    """The library's pool gives its memory back on request; later calls allocate again."""
+    from fadesim_gb300 import _lib
+    B, X, Y, n, m = 2, 3, 1, 64, 64
+    inp, G = case(11, B, X, Y, n, m)
+    ti, tg = torch.tensor(inp, dtype=torch.float32).pin_memory(), torch.tensor(G, dtype=torch.float32).pin_memory()
+    first = acc.ir_drop_gs_host(ti, tg, B, n, m, X, Y, g_wire=GW)
+    assert _lib.load().fadesim_release_memory() == 0
+    again = acc.ir_drop_gs_host(ti, tg, B, n, m, X, Y, g_wire=GW)
+    assert torch.equal(first, again)
