@@ -439,7 +439,7 @@ def run_ours(args):
         "gpu_launches": args.steps,
         "clocks": clk_summary,
     }
-    if rank == 0:
+    if world == 1:  # the host-core baseline is timed at N = 1 only (rank 0 is the only rank left here)
         line["cpu_baseline"] = cpu_baseline()
     print(json.dumps(line))
     if dist:
