@@ -149,6 +149,12 @@ def cpu_baseline(seconds=12.0, max_solves=4096):
                       "1e-6 V) over %d threads in %.1f s" % (done, threads, el)}
 
 
+def workload_name(tiles):
+    """The benchmarked workload, named the same way on both arms."""
+    return ("%d tiles x %d vectors of 128x128 per rank (ir_drop_gs layout B=%d, numX=%d, numY=1), 4-state cells, "
+            "2.93 ohm wires, Bernoulli 0.2 V inputs" % (tiles, N_VEC, N_VEC, tiles))
+
+
 def run_reference(args):
     from fadesim_gb300.ranks import rank_env
     if rank_env()[0] != 0:
@@ -164,8 +170,9 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "128x128 crossbar solves, 4-state cells, 2.93 ohm wires, Bernoulli 0.2 V inputs",
-                       "solver": "reference Au GS (V1 nodeBasedGS, C restatement) on host cores"},
+            "config": {"workload": workload_name(args.tiles),
+                       "solver": "reference Au GS (V1 nodeBasedGS, C restatement) on host cores, each step a "
+                                 "bounded sample of the workload (see cpu_baseline.sample)"},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -404,9 +411,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "%d tiles x %d vectors of 128x128 per rank (ir_drop_gs layout B=%d, numX=%d, "
-                               "numY=1), 4-state cells, 2.93 ohm wires, Bernoulli 0.2 V inputs"
-                               % (N_TILES, N_VEC, B, X),
+        "config": {"workload": workload_name(X),
                    "solver": "block line relaxation: FP32 tridiagonal line solves; residual in FP32, and in "
                              "float-float (FP64-class) arithmetic on the iteration expected to be the last, which "
                              "must pass the stop test; tol %.0e V (estimated max node error)" % args.tol,
