@@ -766,6 +766,11 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 const float delta = red[(par * 2 + 0) * CL_NW], vm = red[(par * 2 + 1) * CL_NW];
                 par ^= 1;
                 ++it;
+                if (!isfinite(delta) || !isfinite(vm)) {
+                    // the same cluster-wide values in every CTA: every CTA leaves here
+                    status = FADESIM_ST_NONFINITE;
+                    break;
+                }
                 const bool small = stop.update(delta, vm, tol);
                 omega = stop.omega;
                 if (small) {

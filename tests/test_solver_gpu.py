@@ -183,11 +183,17 @@ def test_line_solver_deterministic_and_stream(acc):
     assert torch.equal(a, b)
 
 
-def test_nonfinite_input_reports_status(acc):
-    B, X, Y, n, m = 1, 1, 1, 16, 16
+@pytest.mark.parametrize("n", [16, 256])  # single-CTA and cluster kernels
+def test_nonfinite_input_reports_status(acc, n):
+    B, X, Y, m = 2, 1, 1, n
     inp, G = make_case(3, B, X, Y, n, m, CFG1, 1.0)
     G[0, 3, 4] = np.nan
-    _, stats, _ = run(acc, inp, G, B, X, Y, n, m, method="line")
+    _, stats, iters = run(acc, inp, G, B, X, Y, n, m, method="line")
+    assert stats["status_or"] & 4
+    # the NaN stays in its lines (fmaxf skips it in the maxima): the rest converges as usual
+    # and the status flags the result, well before the iteration cap
+    assert iters.max() < 10
+    cur, stats, _ = run(acc, inp, G, B, X, Y, n, m, method="line", ret_V=False)
     assert stats["status_or"] & 4
 
 
