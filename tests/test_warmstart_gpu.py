@@ -142,8 +142,8 @@ def test_trained_network_saves_sweeps(ws, tmp_path):
     configuration, 64x64 tiles, Bernoulli 0.2 V inputs), then start the plain
     red-black SOR, at PimTorch's default relaxation factor 1.90, from the
     prediction: it must need fewer sweeps than from the ideal state, and the line
-    solve from the prediction must still land on the oracle (the solver stays the
-    judge)."""
+    solve from the prediction must still land on the oracle (the solver, not the
+    network, decides the error)."""
     from fadesim_gb300 import cpp_ir_drop_accelerate as acc
     n = 64
     Rs = torch.tensor([2e6, 1.6e6, 1.3e6, 1e6])
