@@ -1,0 +1,83 @@
+"""The shared-memory layouts the line kernels rely on, checked exhaustively on
+the CPU: the XOR swizzles (csrc/line_impl.cuh swz, csrc/cluster_impl.cuh cswz)
+permute each row, put every step of both walks on 32 distinct banks, and give
+the register addressing the passes use (node k of a wordline segment at its
+first node XOR k, of a bitline segment at Rb[k % V] + k * row length).  The
+formulas are restated here; a change in the kernels must be mirrored."""
+import pytest
+
+# (LD, NSEG, SEG, LPW, T, V) of line_impl.cuh's LineCfg
+LINE = [(128, 4, 32, 8, 512, 8), (64, 4, 16, 8, 256, 8), (32, 4, 8, 8, 128, 8)]
+
+
+def swz(LD, r, c):
+    if LD == 128:
+        x = (r & 7) | ((((c >> 5) ^ (r >> 5)) & 3) << 3)
+    elif LD == 64:
+        x = (r & 7) | ((((c >> 5) & 1) ^ ((r >> 4) & 1)) << 3) | (((r >> 5) & 1) << 4)
+    else:
+        x = r & 31
+    return r * LD + (c ^ x)
+
+
+@pytest.mark.parametrize("LD,NSEG,SEG,LPW,T,V", LINE)
+def test_line_layout(LD, NSEG, SEG, LPW, T, V):
+    for r in range(LD):
+        assert sorted(swz(LD, r, c) - r * LD for c in range(LD)) == list(range(LD))
+    for warp in range(T // 32):
+        for k in range(SEG):
+            row_walk, col_walk = set(), set()
+            for lane in range(32):
+                s, line = lane // LPW, warp * LPW + lane % LPW
+                row_walk.add(swz(LD, line, s * SEG + k) % 32)
+                col_walk.add(swz(LD, s * SEG + k, line) % 32)
+            assert len(row_walk) == 32 and len(col_walk) == 32, (warp, k)
+    for line in range(LD):
+        for s in range(NSEG):
+            p0 = s * SEG
+            Bw = swz(LD, line, p0)
+            Rb = [swz(LD, p0 + t, line) - t * LD for t in range(V)]
+            for k in range(SEG):
+                assert Bw ^ k == swz(LD, line, p0 + k)
+                assert Rb[k % V] + k * LD == swz(LD, p0 + k, line)
+
+
+def test_input_padding_spreads_the_bitline_walk():
+    """vpad: the bitline pass reads rows 16 s + k of NSEG segments at once."""
+    vpad = lambda p: p + (p >> 4)
+    for LD, NSEG, SEG, _, _, _ in LINE:
+        for k in range(SEG):
+            assert len({vpad(s * SEG + k) % 32 for s in range(NSEG)}) == NSEG
+
+
+# (LDM, C, RPC, NSEG_W, LPW_W, NSEG_B, LPW_B, V) of cluster_impl.cuh's CCfg; 512 threads, 32-node segments
+CLUSTER = [(256, 4, 64, 8, 4, 2, 16, 4), (512, 16, 32, 16, 2, 1, 32, 2)]
+
+
+def cswz(LDM, lr, c):
+    if LDM == 256:
+        x = (lr & 3) | (((c >> 5) & 3) << 2) | ((((c >> 7) ^ (lr >> 5)) & 1) << 4)
+    else:
+        x = (lr & 1) | (((c >> 5) & 15) << 1)
+    return lr * LDM + (c ^ x)
+
+
+@pytest.mark.parametrize("LDM,C,RPC,NSEG_W,LPW_W,NSEG_B,LPW_B,V", CLUSTER)
+def test_cluster_layout(LDM, C, RPC, NSEG_W, LPW_W, NSEG_B, LPW_B, V):
+    SEG, T = 32, 512
+    for lr in range(RPC):
+        assert sorted(cswz(LDM, lr, c) - lr * LDM for c in range(LDM)) == list(range(LDM))
+    for warp in range(T // 32):
+        for k in range(SEG):
+            word = {cswz(LDM, warp * LPW_W + lane % LPW_W, (lane // LPW_W) * SEG + k) % 32 for lane in range(32)}
+            bit = {cswz(LDM, (lane // LPW_B) * SEG + k, warp * LPW_B + lane % LPW_B) % 32 for lane in range(32)}
+            assert len(word) == 32 and len(bit) == 32, (warp, k)
+    for lr in range(RPC):
+        for s in range(NSEG_W):
+            Bw = cswz(LDM, lr, s * SEG)
+            assert all(Bw ^ k == cswz(LDM, lr, s * SEG + k) for k in range(SEG))
+    for col in range(LDM):
+        for s in range(NSEG_B):
+            p0 = s * SEG
+            Rb = [cswz(LDM, p0 + t, col) - t * LDM for t in range(V)]
+            assert all(Rb[k % V] + k * LDM == cswz(LDM, p0 + k, col) for k in range(SEG))
