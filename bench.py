@@ -466,7 +466,17 @@ def main():
                     help="time the device-resident solve only (no e2e, comparator or CPU baseline); for profiling")
     ap.add_argument("--size", type=int, default=128,
                     help="with --quick: tile size N (N x N tiles; 256 and 512 run on the cluster kernels)")
+    ap.add_argument("--only-large", type=int, default=0, metavar="TILES",
+                    help="run only the 512x512 sinh-cell figure on TILES tiles and print it (for profiling)")
     args = ap.parse_args()
+    if args.only_large:
+        import torch
+        from fadesim_gb300 import cpp_ir_drop_accelerate as acc
+        from fadesim_gb300.build import build
+        build()
+        acc.options.tol_v = args.tol
+        print(json.dumps(large_nonideal(torch, acc, n_tiles=args.only_large)))
+        return
     if args.size != 128:
         if not args.quick:
             ap.error("--size is a --quick (profiling) option; the metric is quoted on 128x128 tiles")
