@@ -18,8 +18,8 @@
 //   bitline residual needs one row above and below the band: those halo rows
 //   are read from the neighbouring CTAs before anyone updates them.
 // * Pivots of bitline columns: the recurrence p_r = diag_r - gw^2 / p_{r-1} is
-//   a product of 2x2 matrices; each CTA multiplies its rows' matrices (FP64,
-//   normalised), the products are exchanged once, and each CTA continues from
+//   a product of 2x2 matrices; each CTA multiplies its rows' matrices (float-
+//   float, normalised), the products are exchanged once, and each CTA continues from
 //   the state entering its band.
 // * The stop and precision decisions read every CTA's partial maxima after a
 //   cluster barrier and are therefore identical in all CTAs: every CTA of a

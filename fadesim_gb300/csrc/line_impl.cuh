@@ -16,7 +16,7 @@
 // neighbouring values (FP32, or precise -- float-float or FP64 -- on the
 // iterations an adaptive schedule or residual_period picks, and always for the
 // final convergence test) and T the line's tridiagonal matrix factored
-// once per tile (FP64 pivots rounded to FP32).  Forming T's diagonal in FP32
+// once per tile (float-float pivots rounded to FP32).  Forming T's diagonal in FP32
 // loses the cell term, so a direct (non-residual) FP32 line solve would stall
 // near 1e-5 V; in residual form that rounding only slows convergence.
 //
