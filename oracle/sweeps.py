@@ -141,7 +141,7 @@ def ir_drop_gs_nonlinear(input_v, G, batch_size, row_size, col_size, numX, numY,
 
 
 def ir_family(input_v, G, batch_size, row_size, col_size, numX, numY, iter_times, wire, mode, ou=None, loads=None,
-              beta=1.0, enable_break=False, break_threshold=0.0, ret_V=False):
+              beta=1.0, enable_break=False, break_threshold=0.0, ret_V=False, nonlinear=None):
     """The reference extension's IR2S and operation-unit (OU) solvers
     (split_arr_matmul.cu:336-1327), in the dtype of ``G``.
 
@@ -156,6 +156,15 @@ def ir_family(input_v, G, batch_size, row_size, col_size, numX, numY, iter_times
     r_wire * (first column + 1) and r_wire * (rows - last row) (ir2s_ou).
     Returns currents [B, numX * rows / ou_rows, numY * cols] (one row group
     without OUs), or cell voltages [B, numX, numY, rows, cols] with ret_V.
+
+    ``nonlinear`` = [R_on, R_off, a_on, b_on, a_off, b_off]: sinh cells as in
+    all five host functions (:455-475, 603-622, 727-746, 996-1016,
+    1241-1260).  Before every iteration the conductances are recomputed, in the
+    dtype of ``G``, from u - d of the buffers that iteration overwrites -- after
+    the ping-pong swap those hold the iterate before the newest one, so
+    iterations 0 and 1 both see the initial planes -- with |V| < 1e-5 set to
+    +-1e-5 (deal_v) and z from the linear conductances, negative z set to 0.
+    The currents are taken with the last conductances (get_current).
     """
     dt = np.asarray(G).dtype
     S = dt.type
@@ -187,7 +196,21 @@ def ir_family(input_v, G, batch_size, row_size, col_size, numX, numY, iter_times
         Rs = np.zeros((B, X, Y, n, noy), dt)
         Cs = np.zeros((B, X, Y, m, nox), dt)
     src = inp[:, :, None, :, None]                    # [B, X, 1, n, 1]
+    if nonlinear is not None:
+        R_on, R_off, a_on, b_on, a_off, b_off = (S(p) for p in nonlinear)
+        z = (one / g - R_on) / S(float(nonlinear[1]) - float(nonlinear[0]))
+        z = np.where(z < 0, S(0), z).astype(dt)
+        U_lag, D_lag = U.copy(), D.copy()            # the iterate before the newest
     for _ in range(iter_times):
+        if nonlinear is not None:
+            V = U_lag - D_lag
+            eps = S(1e-5)
+            V = np.where((V < eps) & (V > -eps), np.where(V > 0, eps, -eps), V).astype(dt)
+            Va = np.abs(V)
+            I_on = b_on * np.sinh(Va * a_on)
+            I_off = b_off * np.sinh(Va * a_off)
+            g = (one / ((one - z) * Va / I_on + z * Va / I_off)).astype(dt)
+            U_lag, D_lag = U.copy(), D.copy()
         U0, D0 = U.copy(), D.copy()
         if mode == "gs":
             for t in range(om):

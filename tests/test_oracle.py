@@ -196,3 +196,77 @@ def test_ir_family_consistency():
     for kw in (dict(ou=(n, m)), dict(loads=(2.93, 2.93))):
         r = sweeps.ir_family(inp, G, B, n, m, X, Y, 400, 2.93, "ir2s", **kw)
         assert np.abs(r - conv).max() <= 1e-13 * np.abs(conv).max()
+
+
+def _nl_case(seed, B=2, X=2, Y=2, n=8, m=6):
+    rng = np.random.default_rng(seed)
+    inp = rng.uniform(0, 0.2, (B, X, n))
+    inp[0, 0, 1] = 0.0                                   # a row at 0 V: cells under the deal_v clamp
+    G = 1 / rng.choice([1e5, 2e5, 5e5, 1e6], size=(X, n, Y * m))
+    return inp, G, nodal.sinh_params(1e5, 1e6, a=2.0)
+
+
+def test_nonlinear_sweeps_converge_to_nodal_fixed_point():
+    """The nonlinear sweep restatement (conductances from the iterate before the
+    newest) converges to the FP64 fixed point of the nonlinear nodal system."""
+    inp, G, params = _nl_case(3)
+    B, X, Y, n, m = 2, 2, 2, 8, 6
+    r = sweeps.ir_drop_gs_nonlinear(inp, G, B, n, m, X, Y, 400, GW, 1.5, params)
+    Gr = G.reshape(X, n, Y, m)
+    for b in range(B):
+        for x in range(X):
+            for y in range(Y):
+                u, d, _ = nodal.solve_nonlinear(Gr[x, :, y, :], GW, inp[b, x], params)
+                ref = nodal.nonlinear_currents(Gr[x, :, y, :], u, d, params)
+                got = r[b, x, y * m:(y + 1) * m]
+                assert np.abs(got - ref).max() <= 1e-9 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("iters", [1, 2, 5, 40])
+def test_nonlinear_family_matches_sweep_restatement(iters):
+    """The family's nonlinear bookkeeping (a lagged copy of the planes) against
+    the literal ping-pong restatement of ir_drop_gs: identical iterates for the
+    plain sweep, its whole-tile OU and its wire-valued loads."""
+    inp, G, params = _nl_case(4)
+    B, X, Y, n, m = 2, 2, 2, 8, 6
+    ref = sweeps.ir_drop_gs_nonlinear(inp, G, B, n, m, X, Y, iters, GW, 1.3, params)
+    for kw in (dict(), dict(ou=(n, m)), dict(loads=(GW, GW))):
+        r = sweeps.ir_family(inp, G, B, n, m, X, Y, iters, GW, "gs", beta=1.3, nonlinear=params, **kw)
+        assert np.abs(r - ref).max() <= 1e-13 * np.abs(ref).max(), kw
+
+
+def test_nonlinear_ir2s_family_fixed_point_and_linear_limit():
+    """Nonlinear IR2S converges to the nonlinear nodal solution (its loads equal
+    to the wire resistance make it the plain tile), the OU/load variants reduce
+    to it, and as a -> 0 (b = 1/(a R)) the cells turn linear."""
+    inp, G, params = _nl_case(5)
+    B, X, Y, n, m = 2, 2, 2, 8, 6
+    conv = sweeps.ir_family(inp, G, B, n, m, X, Y, 600, 2.93, "ir2s", nonlinear=params)
+    Gr = G.reshape(X, n, Y, m)
+    for b in range(B):
+        for x in range(X):
+            for y in range(Y):
+                u, d, _ = nodal.solve_nonlinear(Gr[x, :, y, :], GW, inp[b, x], params)
+                ref = nodal.nonlinear_currents(Gr[x, :, y, :], u, d, params)
+                assert np.abs(conv[b, x, y * m:(y + 1) * m] - ref).max() <= 1e-9 * np.abs(ref).max()
+    for kw in (dict(ou=(n, m)), dict(loads=(2.93, 2.93))):
+        r = sweeps.ir_family(inp, G, B, n, m, X, Y, 600, 2.93, "ir2s", nonlinear=params, **kw)
+        assert np.abs(r - conv).max() <= 1e-13 * np.abs(conv).max(), kw
+    lin = sweeps.ir_family(inp, G, B, n, m, X, Y, 30, 2.93, "ir2s")
+    a = 1e-4
+    weak = [1e5, 1e6, a, 1 / (a * 1e5), a, 1 / (a * 1e6)]
+    r = sweeps.ir_family(inp, G, B, n, m, X, Y, 30, 2.93, "ir2s", nonlinear=weak)
+    assert np.abs(r - lin).max() <= 1e-7 * np.abs(lin).max()
+
+
+def test_nonlinear_family_float32_tracks_float64():
+    """The FP32 form of the nonlinear family (arithmetic in the dtype of G, as
+    the reference's tensor ops) stays within FP32 rounding of the FP64 one."""
+    inp, G, params = _nl_case(6)
+    B, X, Y, n, m = 2, 2, 2, 8, 6
+    for mode, wire, kw in (("gs", GW, dict(ou=(4, 3), beta=1.2)), ("ir2s", 2.93, dict(loads=(5.0, 7.5)))):
+        r64 = sweeps.ir_family(inp, G, B, n, m, X, Y, 12, wire, mode, nonlinear=params, **kw)
+        r32 = sweeps.ir_family(inp.astype(np.float32), G.astype(np.float32), B, n, m, X, Y, 12, wire, mode,
+                               nonlinear=params, **kw)
+        assert r32.dtype == np.float32
+        assert np.abs(r32 - r64).max() <= 1e-5 * np.abs(r64).max(), mode
