@@ -251,15 +251,20 @@ int fam_run(bool ir2s, const void *input_v, const void *G_v, int B, OuShape o, i
     unsigned int *moved = reinterpret_cast<unsigned int *>(buf + bytes - 256);
     int rc = FADESIM_OK;
     fam_init_kernel<S><<<fam_grid(plane_elems), 256, 0, st>>>(input, U, D, B, numX, numY, o.n, o.m);
-    if (ir2s) {
-        cudaMemcpyAsync(U2, U, 2 * plane_elems * sizeof(S), cudaMemcpyDeviceToDevice, st);  // U2, D2 <- U, D
-        cudaMemsetAsync(Rs, 0, (rsum + csum) * sizeof(S), st);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && ir2s) {
+        e = cudaMemcpyAsync(U2, U, 2 * plane_elems * sizeof(S), cudaMemcpyDeviceToDevice, st);  // U2, D2 <- U, D
+        if (e == cudaSuccess) e = cudaMemsetAsync(Rs, 0, (rsum + csum) * sizeof(S), st);
     }
+    if (e != cudaSuccess) rc = fail(FADESIM_E_CUDA, cudaGetErrorString(e));
     const dim3 grid(B, numX, numY);
     const int threads = (int)min(1024, ((max(o.n * o.noy, o.m * o.nox) + 31) / 32) * 32);
-    for (int it = 0; it < iter_times && B > 0; ++it) {
+    for (int it = 0; rc == FADESIM_OK && it < iter_times && B > 0; ++it) {
         unsigned int *mv = enable_break ? moved : nullptr;
-        if (mv) cudaMemsetAsync(mv, 0, sizeof(unsigned int), st);
+        if (mv && (e = cudaMemsetAsync(mv, 0, sizeof(unsigned int), st)) != cudaSuccess) {
+            rc = fail(FADESIM_E_CUDA, cudaGetErrorString(e));
+            break;
+        }
         if (ir2s) {
             fam_ir2s_kernel<S><<<grid, threads, 0, st>>>(input, G, U, D, U2, D2, Rs, Cs, numX, numY, o, (S)wire,
                                                           (S)load_l, (S)load_d, (S)thr, mv);
@@ -279,8 +284,9 @@ int fam_run(bool ir2s, const void *input_v, const void *G_v, int B, OuShape o, i
         }
         if (mv) {
             unsigned int h = 0;
-            cudaMemcpyAsync(&h, mv, sizeof(h), cudaMemcpyDeviceToHost, st);
-            if ((e = cudaStreamSynchronize(st)) != cudaSuccess) {
+            e = cudaMemcpyAsync(&h, mv, sizeof(h), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) {
                 rc = fail(FADESIM_E_CUDA, cudaGetErrorString(e));
                 break;
             }
