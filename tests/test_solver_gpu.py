@@ -221,3 +221,36 @@ def test_precision_schedule_meets_tolerance(acc, tol, cells, n):
     # the every-iteration float-float schedule agrees with it to the same tolerance
     ref, _, _ = run(acc, inp, G, B, X, Y, n, n, dtype=torch.float64, method="line", tol_v=tol, residual_period=1)
     assert np.abs(got - ref).max() <= 2 * (tol + floor)
+
+
+@pytest.fixture(scope="module")
+def full_size():
+    """The throughput workload's full size: 4096 tiles of 128 x 128, 64 input
+    vectors each (262,144 solves), four-state 1-2 Mohm cells; two input sets."""
+    B, X, n = 64, 4096, 128
+    g = torch.Generator().manual_seed(11)
+    states = torch.randint(0, 4, (X, n, n), generator=g)
+    G = (1.0 / torch.tensor(CFG1, dtype=torch.float64))[states].float().cuda()
+    va = (torch.randint(0, 2, (B, X, n), generator=g) * 0.2).float().cuda()
+    vb = (torch.rand((B, X, n), generator=g) * 0.1).float().cuda()
+    return B, X, n, G, va, vb
+
+
+def test_full_size_linearity_and_tile_order(acc, full_size):
+    """At the full size, where the oracle cannot follow: every solve converges;
+    with linear cells the currents are linear in the inputs, I(a) + I(b) =
+    I(a + b) to the solver's tolerance; tiles are independent, so solving them
+    in another order returns the same currents in that order."""
+    B, X, n, G, va, vb = full_size
+
+    def solve(v, g):
+        out, st, _ = acc.ir_drop_gs_ex(v.contiguous(), g.contiguous(), B, n, n, X, 1, method="line", tol_v=1e-8)
+        assert st["solves"] == B * X and st["status_or"] == 1, st
+        return out.double()
+
+    Ia, Ib, Iab = solve(va, G), solve(vb, G), solve(va + vb, G)
+    scale = Iab.abs().max().item()
+    assert (Ia + Ib - Iab).abs().max().item() <= 1e-5 * scale
+    perm = torch.randperm(X, generator=torch.Generator().manual_seed(5)).cuda()
+    Ip = solve(va[:, perm], G[perm])
+    assert (Ip - Ia[:, perm]).abs().max().item() <= 1e-5 * Ia.abs().max().item()
