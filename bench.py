@@ -51,6 +51,22 @@ BYTES_PER_SOLVE = (ROWS * COLS * 4) / N_VEC + ROWS * 4 + COLS * 4
 SMEM_BYTES_PER_NODE_UPDATE = 4 * (2 + 1 + 1 + 1 + 0.5)
 SMEM_BYTES_PER_CLK_SM = 128  # shared-memory bandwidth per SM per clock (32 banks x 4 B)
 N_SMS = 152
+# algorithmic FP32 operations per node update of a line pass: the residual (cell
+# voltage, the two neighbour differences, their sum, the cell term: 7), the
+# Thomas forward step c r + c y (3), the backward step y + c x (an FMA: 2) and
+# the relaxed update omega x + own (an FMA: 2)
+FP32_FLOPS_PER_NODE_UPDATE = 14
+FP32_FLOPS_PER_CLK_SM = 256  # 128 FP32 lanes x 2 (FMA)
+
+
+def fp32_roofline(node_updates, kern_ms, sm_mhz):
+    """The line kernel against the FP32 pipe: algorithmic FP32 operations of its
+    node updates per second over the nominal FMA rate at the sampled clock."""
+    achieved = FP32_FLOPS_PER_NODE_UPDATE * node_updates / (kern_ms / 1e3) / 1e12
+    peak = FP32_FLOPS_PER_CLK_SM * N_SMS * sm_mhz * 1e6 / 1e12
+    return {"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "peak_kind": "nominal 128 FP32 FMA/clk/SM at the sampled clock",
+            "flops_per_node_update": FP32_FLOPS_PER_NODE_UPDATE}
 
 
 def peaks():
@@ -437,6 +453,7 @@ def run_ours(args):
                               "frac": smem_achieved / smem_peak, "peak_kind": "nominal 128 B/clk/SM at the sampled clock",
                               "bytes_per_node_update": SMEM_BYTES_PER_NODE_UPDATE,
                               "node_updates_per_launch": node_updates},
+                     "fp32": fp32_roofline(node_updates, kern_ms, clk_summary.get("sm_mhz") or 2070.0),
                      "note": "HBM carries only G, inputs and currents; the line passes run on shared-memory "
                              "planes and are bound by instruction issue (see profiles/)"},
         "e2e": {"value": e2e_value, "unit": UNIT,

@@ -19,3 +19,14 @@ def test_reference_arm_json_line():
     cb = line["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
     assert line["config"]["workload"].startswith("4096 tiles x 64 vectors of 128x128")
+
+
+def test_fp32_roofline_arithmetic():
+    """The FP32-pipe figure of the roofline: the bench's last measured launch
+    (1.73e10 node updates in 24.26 ms at 2070 MHz) is ~12% of the FMA rate."""
+    sys.path.insert(0, ROOT)
+    import bench
+    r = bench.fp32_roofline(1.7314545664e10, 24.26, 2070.0)
+    assert r["unit"] == "TFLOP/s" and abs(r["peak"] - 256 * 152 * 2070e6 / 1e12) < 1e-9
+    assert abs(r["achieved"] - 14 * 1.7314545664e10 / 24.26e-3 / 1e12) < 1e-9
+    assert 0.11 < r["frac"] < 0.13
