@@ -1,6 +1,9 @@
 """The closed-form pieces the kernels use, checked in numpy: the series for
 sinh(t)/t below t = 1 and the one-division form of the sinh cell's chord
-conductance (csrc/common.cuh)."""
+conductance (csrc/common.cuh); the error-free transforms of the precise
+residual and of the float-float pivots (csrc/line_common.cuh), restated in
+float32 arithmetic and checked against exact rationals.  The restatements
+mirror the device code; a change there must be mirrored here."""
 import math
 
 import numpy as np
@@ -41,3 +44,109 @@ def test_chord_conductance_one_division_form():
     V = x
     R = (1 - z) * V / (b_on * np.sinh(a_on * V)) + z * V / (b_off * np.sinh(a_off * V))
     np.testing.assert_allclose(one, 1 / R, rtol=1e-13)
+
+
+# ---- error-free transforms of the precise residual and the pivots
+# (csrc/line_common.cuh two_sum, lap_exact, ff_pivot_step), restated in float32
+# numpy arithmetic (IEEE round-to-nearest, as the kernels' __fadd_rn etc.) and
+# checked against exact rational arithmetic.
+from fractions import Fraction  # noqa: E402
+
+F = np.float32
+
+
+def rn32(q):
+    """Round an exact rational to the nearest float32, ties to even."""
+    if q == 0:
+        return F(0)
+    f = F(float(q))
+    best = None
+    for c in (np.nextafter(f, F(-np.inf)), f, np.nextafter(f, F(np.inf))):
+        d = abs(Fraction(float(c)) - q)
+        if best is None or d < best[0] or (d == best[0] and int(c.view(np.uint32)) % 2 == 0):
+            best = (d, c)
+    return best[1]
+
+
+def fma32(a, b, c):
+    return rn32(Fraction(float(a)) * Fraction(float(b)) + Fraction(float(c)))
+
+
+def two_sum(a, b):
+    s = F(a + b)
+    bb = F(s - a)
+    return s, F(F(a - F(s - bb)) + F(b - bb))
+
+
+def lap_exact(prev, cur, nxt, has_l, has_r):
+    sh, sl = two_sum(prev if has_l else F(0), nxt if has_r else F(0))
+    k = F(2) * cur if (has_l and has_r) else (cur if (has_l or has_r) else F(0))
+    th, tl = two_sum(sh, -k)
+    return th, F(tl + sl)
+
+
+def ff_pivot_step(base, gs, first, rh, rl):
+    dh, dl = two_sum(base, gs)
+    ph, pl = dh, dl
+    if not first:
+        sh, sl = two_sum(dh, -rh)
+        sl = F(sl + F(dl - rl))
+        ph = F(sh + sl)
+        pl = F(sl - F(ph - sh))
+    r = F(F(1) / ph)
+    e = fma32(-ph, r, F(1))
+    e = fma32(-pl, r, e)
+    return F(r + F(e * r)), r, F(e * r)
+
+
+def ulp32(x):
+    return float(np.spacing(np.abs(F(x))))
+
+
+def test_two_sum_is_error_free():
+    rng = np.random.default_rng(1)
+    a = (rng.standard_normal(4000) * 10.0 ** rng.integers(-8, 3, 4000)).astype(F)
+    b = (rng.standard_normal(4000) * 10.0 ** rng.integers(-8, 3, 4000)).astype(F)
+    for x, y in zip(a, b):
+        s, e = two_sum(x, y)
+        assert Fraction(float(s)) + Fraction(float(e)) == Fraction(float(x)) + Fraction(float(y))
+
+
+def test_line_part_exact_up_to_one_rounding_of_its_low_part():
+    """(prev - cur) + (nxt - cur) as hi + lo: the error is the rounding of lo
+    alone, for neighbouring node values (the cancellation the residual sees)."""
+    rng = np.random.default_rng(2)
+    for _ in range(3000):
+        cur = F(rng.uniform(-0.2, 0.2))
+        prev = F(cur + F(rng.standard_normal() * 10.0 ** rng.integers(-9, -2)))
+        nxt = F(cur + F(rng.standard_normal() * 10.0 ** rng.integers(-9, -2)))
+        has_l, has_r = bool(rng.integers(0, 4)), bool(rng.integers(0, 4))
+        hi, lo = lap_exact(prev, cur, nxt, has_l, has_r)
+        exact = ((Fraction(float(prev)) - Fraction(float(cur))) if has_l else 0) + \
+                ((Fraction(float(nxt)) - Fraction(float(cur))) if has_r else 0)
+        err = abs(Fraction(float(hi)) + Fraction(float(lo)) - exact)
+        assert err <= Fraction(ulp32(lo)) / 2
+
+
+def test_float_float_pivots_match_exact_recurrence():
+    """Chain multipliers 1/P_q of P_q = D_q - 1/P_(q-1), D_q = (1 or 2) + g/gw,
+    along 128-node wordlines and bitlines with 1 kohm - 1 Mohm cells and 2.93
+    ohm wires: correctly rounded against the exact rational recurrence (a
+    plain FP32 recurrence is hundreds of ulps off)."""
+    rng = np.random.default_rng(3)
+    L, gw = 128, 1 / 2.93
+    plain_worst = 0
+    for word in (True, False):
+        for _ in range(3):
+            gs = (1.0 / rng.choice([1e3, 2e4, 3e5, 1e6], L) / gw).astype(F)
+            rh = rl = F(0)
+            P = pf = None
+            for q in range(L):
+                base = F((2 if q + 1 < L else 1) if word else (2 if q > 0 else 1))
+                cf, rh, rl = ff_pivot_step(base, gs[q], q == 0, rh, rl)
+                D = Fraction(int(base)) + Fraction(float(gs[q]))
+                P = D if q == 0 else D - 1 / P
+                assert abs(Fraction(float(cf)) - 1 / P) <= Fraction(ulp32(cf)) / 2, (word, q)
+                pf = F(base + gs[q]) if q == 0 else F(F(base + gs[q]) - F(F(1) / pf))
+                plain_worst = max(plain_worst, abs(Fraction(float(F(F(1) / pf))) - 1 / P) / Fraction(ulp32(cf)))
+    assert plain_worst > 50
