@@ -150,3 +150,78 @@ def test_float_float_pivots_match_exact_recurrence():
                 pf = F(base + gs[q]) if q == 0 else F(F(base + gs[q]) - F(F(1) / pf))
                 plain_worst = max(plain_worst, abs(Fraction(float(F(F(1) / pf))) - 1 / P) / Fraction(ulp32(cf)))
     assert plain_worst > 50
+
+
+# cluster kernels (csrc/cluster_impl.cuh ff_norm, ff_mul_sub, ff_dot2, cl_pivots):
+# a bitline column spans C bands of RPC rows, one per CTA; each band's map
+# P -> D - 1/P is a product of [[D, -1], [1, 0]] in float-float, rescaled by a
+# power of two; the state entering a band composes the maps above it.
+def ff_norm(s, e):
+    h = F(s + e)
+    return h, F(e - F(h - s))
+
+
+def ff_mul_sub(x, y, z):
+    ph = F(x[0] * y[0])
+    pl = F(fma32(x[0], y[0], -ph) + F(F(x[0] * y[1]) + F(x[1] * y[0])))
+    sh, sl = two_sum(ph, -z[0])
+    return ff_norm(sh, F(sl + F(pl - z[1])))
+
+
+def ff_dot2(x, y, z, w):
+    ph, qh = F(x[0] * y[0]), F(z[0] * w[0])
+    pl = F(fma32(x[0], y[0], -ph) + F(F(x[0] * y[1]) + F(x[1] * y[0])))
+    ql = F(fma32(z[0], w[0], -qh) + F(F(z[0] * w[1]) + F(z[1] * w[0])))
+    sh, sl = two_sum(ph, qh)
+    return ff_norm(sh, F(sl + F(pl + ql)))
+
+
+def inv_binade(v):
+    _, e = np.frexp(np.float64(v))
+    return F(2.0 ** (1 - e))
+
+
+def band_pivots(gs, C, RPC):
+    scale = lambda x, k: (F(x[0] * k), F(x[1] * k))
+    mobs = []
+    for r in range(C):
+        a, b, c, d = (F(1), F(0)), (F(0), F(0)), (F(0), F(0)), (F(1), F(0))
+        for lr in range(RPC):
+            q = r * RPC + lr
+            D = two_sum(F(2 if q > 0 else 1), gs[q])
+            a, b, c, d = ff_mul_sub(D, a, c), ff_mul_sub(D, b, d), a, b
+        k = inv_binade(max(abs(a[0]), abs(b[0]), abs(c[0]), abs(d[0])))
+        mobs.append([scale(v, k) for v in (a, b, c, d)])
+    out = []
+    for rank in range(C):
+        num, den = (F(1), F(0)), (F(0), F(0))
+        for a, b, c, d in mobs[:rank]:
+            nn, dd = ff_dot2(a, num, b, den), ff_dot2(c, num, d, den)
+            k = inv_binade(max(abs(nn[0]), abs(dd[0])))
+            num, den = scale(nn, k), scale(dd, k)
+        rh = rl = F(0)
+        if rank > 0 and num[0] != 0:
+            rh = F(den[0] / num[0])
+            rl = F(F(fma32(-num[0], rh, den[0]) + F(den[1] - F(rh * num[1]))) / num[0])
+        for lr in range(RPC):
+            q = rank * RPC + lr
+            cf, rh, rl = ff_pivot_step(F(2 if q > 0 else 1), gs[q], q == 0, rh, rl)
+            out.append(cf)
+    return out
+
+
+def test_cluster_band_pivots_match_exact_recurrence():
+    """Bitline multipliers of the 256-row (4 bands of 64) and 512-row (16 bands
+    of 32) cluster layouts, through the band products: correctly rounded against
+    the exact recurrence, for mixed and for all-1-kohm columns."""
+    rng = np.random.default_rng(4)
+    gw = 1 / 2.93
+    for L, C, RPC in ((256, 4, 64), (512, 16, 32)):
+        for cells in ([1e3, 2e4, 3e5, 1e6], [1e3], [1e6]):
+            gs = (1.0 / rng.choice(cells, L) / gw).astype(F)
+            cfs = band_pivots(gs, C, RPC)
+            P = None
+            for q in range(L):
+                D = Fraction(2 if q > 0 else 1) + Fraction(float(gs[q]))
+                P = D if q == 0 else D - 1 / P
+                assert abs(Fraction(float(cfs[q])) - 1 / P) <= Fraction(ulp32(cfs[q])) / 2, (L, cells, q)
