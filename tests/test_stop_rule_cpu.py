@@ -6,8 +6,9 @@ What is checked is the rule's promise, separately from FP32 rounding: when it
 says stop, the iterate is within the tolerance (plus its floor, 4 FP32 ulps of
 the largest deviation) of the nodal solution, for weak and strong cells,
 several sizes and both tolerances the benchmarks use, with the rate and
-relaxation factor carried from one input vector of a tile to the next.  The
-restatement mirrors the device code; a change there must be mirrored here.
+relaxation factor carried from one input vector of a tile to the next.  Also
+the identity behind the fused current epilogue.  The restatement mirrors the
+device code; a change there must be mirrored here.
 """
 import math
 
@@ -137,3 +138,26 @@ def test_stop_rule_keeps_its_promise(n, cells, vmax, tol):
     # weak cells: a few block iterations, as the kernel's counts on the GPU
     if cells is CFG1:
         assert max(iters) <= 4
+
+
+def test_ground_link_currents_after_an_unrelaxed_bitline_pass():
+    """The current epilogue's identity (csrc/line_impl.cuh outputs): after a
+    bitline pass at omega 1 every bitline equation holds, so summed down a
+    column the wire terms telescope and the column current sum_i g (u - d)
+    equals gw d_(n-1) -- from any wordline plane, converged or not.  Over-
+    relaxed passes break it, which is why the kernel sums the cells then."""
+    rng = np.random.default_rng(9)
+    n, m = 40, 24
+    g = 1.0 / rng.choice(STRONG, (n, m))
+    u = rng.uniform(0, 1, (n, m))
+    d_old = rng.uniform(0, 0.1, (n, m))
+    bl_diag = (np.where(np.arange(n) > 0, GW, 0.0)[:, None] + GW + g).T
+    bl_low = np.where(np.arange(n) > 0, -GW, 0.0)[None, :].repeat(m, 0)
+    bl_up = np.full((m, n), -GW)
+    d_star = thomas(bl_low, bl_diag, bl_up, (g * u).T).T
+    for w, holds in ((1.0, True), (1.5, False)):
+        d = d_old + w * (d_star - d_old)
+        summed = (g * (u - d)).sum(axis=0)
+        link = GW * d[-1]
+        gap = np.abs(summed - link).max() / np.abs(summed).max()
+        assert (gap < 1e-12) == holds, (w, gap)
