@@ -225,3 +225,53 @@ def test_cluster_band_pivots_match_exact_recurrence():
                 D = Fraction(2 if q > 0 else 1) + Fraction(float(gs[q]))
                 P = D if q == 0 else D - 1 / P
                 assert abs(Fraction(float(cfs[q])) - 1 / P) <= Fraction(ulp32(cfs[q])) / 2, (L, cells, q)
+
+
+def line_residual(RES, word, prev, cur, nxt, gs, o, vin):
+    """line_residual_s (csrc/line_common.cuh) for an interior node, RES 0 (FP32),
+    2 (float-float) and 3 (exact line part, FP32 cell term), in gw units."""
+    if RES == 2:
+        sh, sl = two_sum(o, -vin if word else vin)
+        th, tl = two_sum(sh, -cur)
+        lh, lap_lo = lap_exact(prev, cur, nxt, True, True)
+        ph = F(gs * th)
+        pl = fma32(gs, th, -ph)
+        rh, rl = two_sum(lh, ph)
+        return F(rh + F(F(rl + F(lap_lo + pl)) + F(gs * F(tl + sl))))
+    src = F(F(o - vin) - cur) if word else F(F(o + vin) - cur)
+    if RES == 3:
+        lh, lap_lo = lap_exact(prev, cur, nxt, True, True)
+        return F(lh + fma32(gs, src, lap_lo))
+    return fma32(gs, src, F(F(prev - cur) + F(nxt - cur)))
+
+
+def test_residual_forms_near_convergence():
+    """Near convergence the residual is ~1e-10 V while its terms are ~1e-4: the
+    float-float form (RES 2) stays within a few units of 2^-46 of the terms,
+    orders of magnitude under the FP32 form (RES 0); the semi-precise form
+    (RES 3) is held to one FP32 rounding of the cell term, which the kernels
+    allow only where that rounding stays far under the tolerance."""
+    rng = np.random.default_rng(5)
+    q = lambda v: Fraction(float(v))
+    err0, err2 = [], []
+    for _ in range(1500):
+        word = bool(rng.integers(0, 2))
+        vin = F(rng.choice([0.0, 0.2, 1.0]))
+        cur = F(-rng.uniform(0, 0.05)) if word else F(rng.uniform(0, 0.05))
+        o = F(rng.uniform(0, 0.05)) if word else F(-rng.uniform(0, 0.05))
+        gs = F(2.93 / rng.choice([1e3, 2e4, 3e5, 1e6]))
+        nxt = F(cur + F(rng.standard_normal() * 1e-4))
+        srcv = (float(o) - float(vin) - float(cur)) if word else (float(o) + float(vin) - float(cur))
+        prev = F(2 * float(cur) - float(nxt) - float(gs) * srcv + rng.standard_normal() * 1e-10)
+        src = (q(o) - q(vin) - q(cur)) if word else (q(o) + q(vin) - q(cur))
+        exact = (q(prev) - q(cur)) + (q(nxt) - q(cur)) + q(gs) * src
+        mag = max(abs(float(prev)), abs(float(cur)), abs(float(nxt)), abs(float(o)) + abs(float(vin)))
+        r2 = line_residual(2, word, prev, cur, nxt, gs, o, vin)
+        e2 = abs(q(r2) - exact)
+        assert e2 <= Fraction(ulp32(r2)) / 2 + Fraction(mag) * Fraction(2) ** -46
+        r3 = line_residual(3, word, prev, cur, nxt, gs, o, vin)
+        assert abs(q(r3) - exact) <= Fraction(ulp32(r3)) + 4 * q(gs) * Fraction(mag + 1.0) * Fraction(2) ** -23
+        r0 = line_residual(0, word, prev, cur, nxt, gs, o, vin)
+        err0.append(float(abs(q(r0) - exact)))
+        err2.append(float(e2))
+    assert np.median(err0) > 1000 * np.median(err2)
