@@ -2,8 +2,9 @@
 the CPU: the XOR swizzles (csrc/line_impl.cuh swz, csrc/cluster_impl.cuh cswz)
 permute each row, put every step of both walks on 32 distinct banks, and give
 the register addressing the passes use (node k of a wordline segment at its
-first node XOR k, of a bitline segment at Rb[k % V] + k * row length).  The
-formulas are restated here; a change in the kernels must be mirrored."""
+first node XOR k, of a bitline segment at Rb[k % V] + k * row length); and the
+red-black comparator's thread-to-node map.  The formulas are restated here; a
+change in the kernels must be mirrored."""
 import pytest
 
 # (LD, NSEG, SEG, LPW, T, V) of line_impl.cuh's LineCfg
@@ -81,3 +82,41 @@ def test_cluster_layout(LDM, C, RPC, NSEG_W, LPW_W, NSEG_B, LPW_B, V):
             p0 = s * SEG
             Rb = [cswz(LDM, p0 + t, col) - t * LDM for t in range(V)]
             assert all(Rb[k % V] + k * LDM == cswz(LDM, p0 + k, col) for k in range(SEG))
+
+
+def test_red_black_sweep_covers_each_colour_once():
+    """csrc/rbsor.cu: thread t owns column t % 128 at rows t / 128 + 8k and, in
+    half-sweep c, relaxes its cells' wordline node when (row0 + col) & 1 == c,
+    else their bitline node.  For every shape up to 128 x 128 each half-sweep
+    updates every node of colour c exactly once (wordline (i+j)&1, bitline
+    (i+j+1)&1), and every value it reads -- the line neighbours and the
+    partner in the other plane -- has the other colour, so the update is a true
+    red-black Gauss-Seidel step."""
+    import numpy as np
+    T, MAXL, STEP = 1024, 128, 8
+    t = np.arange(T)
+    col, row0 = t % MAXL, t // MAXL
+    for n in (2, 3, 5, 8, 9, 16, 31, 64, 77, 100, 127, 128):
+        for m in (2, 3, 5, 8, 9, 16, 31, 64, 77, 100, 127, 128):
+            for c in (0, 1):
+                hitU = np.zeros((n, m), int)
+                hitD = np.zeros((n, m), int)
+                for tt in range(T):
+                    j = col[tt]
+                    if j >= m:
+                        continue
+                    isU = ((row0[tt] + j) & 1) == c
+                    rows = np.arange(row0[tt], n, STEP)
+                    (hitU if isU else hitD)[rows, j] += 1
+                    # reads: line neighbours in the same plane, the partner in the other
+                    for i in rows:
+                        own = (i + j) & 1 if isU else (i + j + 1) & 1
+                        assert own == c
+                        nbrs = [(i, j - 1), (i, j + 1)] if isU else [(i - 1, j), (i + 1, j)]
+                        for a, b in nbrs:
+                            if 0 <= a < n and 0 <= b < m:
+                                assert (((a + b) & 1) if isU else ((a + b + 1) & 1)) != c
+                        assert (((i + j + 1) & 1) if isU else ((i + j) & 1)) != c
+                ii, jj = np.meshgrid(np.arange(n), np.arange(m), indexing="ij")
+                assert np.array_equal(hitU, (((ii + jj) & 1) == c).astype(int)), (n, m, c)
+                assert np.array_equal(hitD, (((ii + jj + 1) & 1) == c).astype(int)), (n, m, c)
