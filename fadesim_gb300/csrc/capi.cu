@@ -10,6 +10,7 @@
 #include <string>
 
 #include "kernels.h"
+#include "trace.h"
 
 using namespace fadesim;
 
@@ -249,6 +250,7 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
                                      const double *nonlinear_params, int n_nonlinear_params, int ret_V, void *out,
                                      const fadesim_solve_opts *opts, fadesim_solve_stats *stats,
                                      int *per_solve_iters, void *stream) {
+    TraceRange trace("fadesim_ir_drop_gs_ex");
     g_err.clear();
     if (dtype != FADESIM_F32 && dtype != FADESIM_F64) return fail(FADESIM_E_ARG, "dtype must be f32 or f64");
     if (batch_size == 0 && row_size >= 2 && col_size >= 2) {

@@ -19,6 +19,7 @@
 #include <string>
 
 #include "kernels.h"
+#include "trace.h"
 
 namespace {
 
@@ -78,6 +79,7 @@ extern "C" int fadesim_ir_drop_gs_host(int dtype, const void *input, const void 
                                        const double *nonlinear_params, int n_nonlinear_params, int ret_V, void *out,
                                        const fadesim_solve_opts *opts, fadesim_solve_stats *stats, int group_x,
                                        void *stream) {
+    fadesim::TraceRange trace("fadesim_ir_drop_gs_host");
     if (dtype != FADESIM_F32 && dtype != FADESIM_F64)
         return fadesim::report_error(FADESIM_E_ARG, "dtype must be FADESIM_F32 or FADESIM_F64");
     if (batch_size < 0 || numX < 0 || numY < 0 || row_size < 2 || col_size < 2)

@@ -23,6 +23,7 @@
 // that moved more than it after every iteration (the reference's two .item()
 // reductions, :297-306).
 #include "kernels.h"
+#include "trace.h"
 
 namespace fadesim {
 
@@ -323,6 +324,7 @@ int fam_dispatch(int dtype, bool ir2s, const void *input, const void *G, int B, 
                  int iter_times, double wire, double load_l, double load_d, double beta, int enable_break, double thr,
                  int ret_V, void *out, void *stream) {
     if (B == 0) return FADESIM_OK;
+    TraceRange trace(ir2s ? "fadesim_ir2s_family" : "fadesim_ir_gs_ou_family");
     cudaStream_t st = (cudaStream_t)stream;
     return dtype == FADESIM_F64
                ? fam_run<double>(ir2s, input, G, B, o, numX, numY, iter_times, wire, load_l, load_d, beta, enable_break,
