@@ -197,6 +197,17 @@ def test_nonfinite_input_reports_status(acc, n):
     assert stats["status_or"] & 4
 
 
+@pytest.mark.parametrize("method,n,cap", [("line", 64, 1), ("line", 256, 2), ("rbsor", 64, 5)])
+def test_iteration_cap_reports_status(acc, method, n, cap):
+    """Forced non-convergence: a cap far below what the tolerance needs ends
+    every solve with the cap status, never the converged one, at the cap."""
+    B, X, Y = 3, 2, 1
+    inp, G = make_case(4, B, X, Y, n, n, STRONG, 1.0)
+    _, stats, iters = run(acc, inp, G, B, X, Y, n, n, method=method, max_iters=cap, tol_v=1e-8, ret_V=False)
+    assert stats["status_or"] & 2 and not stats["status_or"] & 1, stats
+    assert iters.min() == cap and iters.max() == cap
+
+
 @pytest.mark.parametrize("tol", [5e-7, 1e-8])
 @pytest.mark.parametrize("cells,n", [("cfg1", 128), ("cfg1", 64), ("strong", 64), ("cfg1", 256), ("strong", 256),
                                      ("cfg1", 512)])
