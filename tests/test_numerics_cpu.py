@@ -275,3 +275,33 @@ def test_residual_forms_near_convergence():
         err0.append(float(abs(q(r0) - exact)))
         err2.append(float(e2))
     assert np.median(err0) > 1000 * np.median(err2)
+
+
+def widen_f64(bits):
+    """csrc/line_common.cuh widen_f64 on uint32 float bit patterns -> float64."""
+    b = bits.astype(np.uint64)
+    mag = b & np.uint64(0x7FFFFFFF)
+    sign = b & np.uint64(0x80000000)
+    normal = sign | ((mag >> np.uint64(3)) + np.uint64(896 << 20))
+    special = sign | np.uint64(0x7FF00000) | ((mag & np.uint64(0x007FFFFF)) >> np.uint64(3)) | \
+        np.where(mag > np.uint64(0x7F800000), np.uint64(0x00080000), np.uint64(0))
+    hi = np.where(mag == 0, b, np.where(mag >= np.uint64(0x7F800000), special, normal))
+    lo = (b & np.uint64(7)) << np.uint64(29)
+    return ((hi << np.uint64(32)) | lo).view(np.float64)
+
+
+def test_widen_to_fp64_on_the_integer_pipe():
+    """The FP64 residual's float -> double conversion by bit manipulation: exact
+    for normal numbers, signed zeros and infinities, NaN stays NaN; over every
+    exponent and random mantissas and signs."""
+    rng = np.random.default_rng(6)
+    exps = np.repeat(np.arange(1, 255, dtype=np.uint32), 2000)
+    bits = (rng.integers(0, 2, exps.size, dtype=np.uint32) << np.uint32(31)) | (exps << np.uint32(23)) | \
+        rng.integers(0, 1 << 23, exps.size, dtype=np.uint32)
+    bits = np.concatenate([bits, np.array([0, 0x80000000, 0x7F800000, 0xFF800000, 0x00800000, 0x7F7FFFFF],
+                                          np.uint32)])
+    got = widen_f64(bits)
+    ref = bits.view(np.float32).astype(np.float64)
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+    nan = widen_f64(np.array([0x7FC00000, 0xFFC00001, 0x7F800001], np.uint32))
+    assert np.isnan(nan).all()
