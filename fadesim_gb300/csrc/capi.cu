@@ -54,7 +54,11 @@ cudaError_t lib_pool(cudaMemPool_t *pool) {
         // keep what the pool has mapped between calls (fadesim_release_memory trims it)
         unsigned long long keep = ~0ull;
         e = cudaMemPoolSetAttribute(g_pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
-        if (e != cudaSuccess) return e;
+        if (e != cudaSuccess) {
+            cudaMemPoolDestroy(g_pools[dev]);  // nothing was allocated from it yet
+            g_pools[dev] = nullptr;
+            return e;
+        }
     }
     *pool = g_pools[dev];
     return cudaSuccess;
