@@ -1,4 +1,5 @@
-"""The C-ABI library loads and exports every function include/*.h declares (no GPU needed)."""
+"""The C-ABI library loads and exports every function include/*.h declares,
+and the ctypes bindings match the header's signatures (no GPU needed)."""
 import ctypes
 import glob
 import os
@@ -77,3 +78,42 @@ def test_release_memory_without_gpu():
     """Nothing allocated yet: trimming the library's pools is a no-op."""
     from fadesim_gb300 import _lib
     assert _lib.load().fadesim_release_memory() == 0
+
+
+def _declarations():
+    """name -> [parameter kind] of every function include/*.h declares, kinds
+    'ptr' or (class, bytes) for scalars."""
+    scalars = {"int": ("int", 4), "unsigned int": ("int", 4), "double": ("float", 8), "float": ("float", 4),
+               "long long": ("int", 8), "unsigned long long": ("int", 8), "int64_t": ("int", 8),
+               "size_t": ("int", 8)}
+    out = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"\b(fadesim_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src):
+            params = [p.strip() for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+            kinds = []
+            for p in params:
+                if "*" in p:
+                    kinds.append("ptr")
+                    continue
+                words = [w for w in p.split() if w != "const"][:-1]  # drop the parameter name
+                kinds.append(scalars[" ".join(words)])
+            out[m.group(1)] = kinds
+    return out
+
+
+def _kind(t):
+    if t is ctypes.c_void_p or hasattr(t, "_type_") and isinstance(t._type_, type):
+        return "ptr"
+    cls = "float" if t in (ctypes.c_float, ctypes.c_double) else "int"
+    return (cls, ctypes.sizeof(t))
+
+
+def test_ctypes_bindings_match_the_header():
+    """Every binding in the ctypes table has the header's parameter count and
+    kinds (pointer, integer or floating point of the same width)."""
+    from fadesim_gb300 import _lib
+    decl = _declarations()
+    for name, args in _lib.EXPORTS.items():
+        assert name in decl, name
+        assert [_kind(t) for t in args] == decl[name], name
