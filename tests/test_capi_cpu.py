@@ -117,3 +117,17 @@ def test_ctypes_bindings_match_the_header():
     for name, args in _lib.EXPORTS.items():
         assert name in decl, name
         assert [_kind(t) for t in args] == decl[name], name
+
+
+def test_warm_start_bindings_match_the_header():
+    from fadesim_gb300 import warmstart
+    m = {"v": ctypes.c_void_p, "p": ctypes.c_void_p, "i": ctypes.c_int, "l": ctypes.c_longlong, "f": ctypes.c_float}
+    decl = _declarations()
+    for name, sig in warmstart._SIGS.items():
+        assert name in decl, name
+        assert [_kind(m[c]) for c in sig] == decl[name], name
+
+
+def test_every_declared_function_has_a_binding():
+    from fadesim_gb300 import _lib, warmstart
+    assert set(_declarations()) == set(_lib.EXPORTS) | set(warmstart._SIGS)
