@@ -19,12 +19,12 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("tol_v", ctypes.c_double), ("max_iters", ctypes.c_int),
                 ("residual_period", ctypes.c_int), ("omega", ctypes.c_double), ("vectors_per_cta", ctypes.c_int),
                 ("residual_kind", ctypes.c_int), ("read_noise_sigma", ctypes.c_double),
-                ("noise_seed", ctypes.c_ulonglong)]
+                ("noise_seed", ctypes.c_ulonglong), ("kernel_ld", ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):
     _fields_ = [("solves", ctypes.c_int64), ("iters_sum", ctypes.c_int64), ("iters_max", ctypes.c_int),
-                ("status_or", ctypes.c_int)]
+                ("status_or", ctypes.c_int), ("warm_rejected", ctypes.c_int64)]
 
 
 _lib = None
@@ -55,13 +55,17 @@ EXPORTS = {
     "fadesim_map_conductance_ref_f32": [_vp] + [_i] * 10 + [ctypes.c_float, ctypes.c_float, _vp, _vp],
     "fadesim_adc_shift_add_ex_f32": [_vp] + [_i] * 7 + [ctypes.c_float] * 3 + [_i] * 5 + [ctypes.c_float, _vp, _i,
                                                                                          _vp, _vp],
-    "fadesim_ir2s": [_i, _vp, _vp] + [_i] * 6 + [_d, _i, _d, _i, _vp, _vp],
-    "fadesim_ir2s_ou_local": [_i, _vp, _vp] + [_i] * 6 + [_d, _d, _d, _i, _d, _vp, _vp],
-    "fadesim_ir2s_ou": [_i, _vp, _vp] + [_i] * 8 + [_d, _i, _d, _vp, _vp],
-    "fadesim_ir_gs_ou_local": [_i, _vp, _vp] + [_i] * 6 + [_d, _d, _d, _d, _i, _d, _vp, _vp],
-    "fadesim_ir_gs_ou": [_i, _vp, _vp] + [_i] * 8 + [_d, _d, _i, _d, _vp, _vp],
+    "fadesim_vary_conductance_f32": [_vp, _vp, ctypes.c_longlong, _d, ctypes.c_ulonglong, ctypes.c_ulonglong, _vp,
+                                     _vp],
+    "fadesim_ir2s": [_i, _vp, _vp] + [_i] * 6 + [_d, _i, _d, _i, _vp, _i, _i, _vp, _vp],
+    "fadesim_ir2s_ou_local": [_i, _vp, _vp] + [_i] * 6 + [_d, _d, _d, _i, _d, _i, _vp, _i, _vp, _vp],
+    "fadesim_ir2s_ou": [_i, _vp, _vp] + [_i] * 8 + [_d, _i, _d, _i, _vp, _i, _vp, _vp],
+    "fadesim_ir_gs_ou_local": [_i, _vp, _vp] + [_i] * 6 + [_d, _d, _d, _d, _i, _d, _i, _vp, _i, _vp, _vp],
+    "fadesim_ir_gs_ou": [_i, _vp, _vp] + [_i] * 8 + [_d, _d, _i, _d, _i, _vp, _i, _vp, _vp],
     "fadesim_noalloc_scratch_bytes": [],
     "fadesim_noalloc_last_error": [],
+    "fadesim_noalloc_last_status": [ctypes.POINTER(SolveStats), _vp],
+    "fadesim_smem_read_probe": [_vp, _i, _i, _vp],
 }
 
 

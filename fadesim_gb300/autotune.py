@@ -1,10 +1,19 @@
 """Project autotuner for the solver's launch parameters.
 
-For a tile shape it times a small set of candidate settings on a seeded sample
-of the caller's own tiles -- work split (vectors per CTA), precise-residual
-period, and for the point-SOR comparator the relaxation factor -- keeps the
-fastest that converges, and caches the winner in a JSON file keyed by GPU name,
-shape and method.  ``lookup`` returns the cached keyword arguments for
+For a tile shape it times a set of candidate settings on a sample of the
+caller's own tiles and keeps the fastest one whose solves all converge:
+
+* kernel shape -- the tile on one CTA (single-CTA layouts 32 / 64 / 128) or on
+  a thread-block cluster (4 CTAs of 64-row bands, 256; 16 CTAs of 32-row bands,
+  512): the layout that fits the tile and the next larger one;
+* work split -- input vectors per work item (CTAs claim items from the call's
+  queue);
+* precise-residual period -- adaptive (0) or every iteration (1);
+* for the point-SOR comparator, the relaxation factor.
+
+The line passes have no unroll axis: a thread's line segment is unrolled by
+construction.  Winners are cached in a JSON file keyed by GPU name, shape and
+method; ``lookup`` returns the cached keyword arguments for
 ``cpp_ir_drop_accelerate.ir_drop_gs_ex`` (empty when nothing is cached).
 """
 import json
@@ -54,10 +63,23 @@ def _store(n, m, method, kw, ms):
         os.replace(tmp, CACHE)
 
 
-def candidates(method):
+LAYOUTS = (32, 64, 128, 256, 512)
+
+
+def layouts(n, m):
+    """Kernel layouts worth timing for an n x m tile: the smallest that holds it
+    and the next larger one (a tile on one CTA against a tile on a cluster at
+    the 128 / 256 boundary)."""
+    L = max(n, m)
+    fit = [ld for ld in LAYOUTS if ld >= L]
+    return fit[:2]
+
+
+def candidates(method, n=128, m=128):
     if method == "rbsor":
         return [dict(omega=w) for w in (1.96, 1.97, 1.975, 1.98, 1.985)]
-    return [dict(vectors_per_cta=v, residual_period=k) for v in (0, 8, 32) for k in (0, 1)]
+    return [dict(kernel_ld=ld, vectors_per_cta=v, residual_period=k) for ld in layouts(n, m) for v in (0, 8, 32)
+            for k in (0, 1)]
 
 
 def tune(G, vin, g_wire=1 / 2.93, method="line", reps=3):
@@ -66,7 +88,7 @@ def tune(G, vin, g_wire=1 / 2.93, method="line", reps=3):
     T, n, m = G.shape
     B = vin.shape[0]
     best = None
-    for kw in candidates(method):
+    for kw in candidates(method, n, m):
         _, st, _ = _acc.ir_drop_gs_ex(vin, G, B, n, m, T, 1, g_wire=g_wire, method=method, **kw)
         if st["status_or"] != 1:
             continue

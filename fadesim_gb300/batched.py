@@ -1,12 +1,15 @@
 """Batches of crossbar tiles of uneven size, solved as one GPU job.
 
 A layer (or any workload) can hold tiles of several sizes, each with its own
-input vectors.  Tiles are grouped by shape; every group is one launch of the
-solver that fits it (shared-memory tile-per-CTA kernel up to 128 x 128,
-cluster-per-tile kernel up to 512 x 512), and the groups run concurrently on
-forked streams.  ``TileBatch.capture()`` records the whole job as one CUDA graph
-for replay (inputs updated in place between replays).  Per-shape launch
-parameters come from ``fadesim_gb300.autotune`` when a tuned entry exists.
+input vectors.  Tiles are grouped by shape; every group is one launch of a
+persistent solver kernel -- shared-memory tile-per-CTA up to 128 x 128,
+cluster-per-tile up to 512 x 512, or the layout the autotuner picked -- whose
+CTAs (clusters) claim (tile, vector chunk) items from the call's device-side
+queue, and the groups run concurrently on forked streams.
+``TileBatch.capture()`` records the whole job as one CUDA graph for replay
+(inputs updated in place between replays).  ``TileBatch.tune()`` runs the
+project's autotuner (``fadesim_gb300.autotune``) on a sample of every group;
+per-shape launch parameters come from its cache.
 """
 import torch
 
@@ -76,6 +79,18 @@ class TileBatch:
         for s in self.streams:
             main.wait_stream(s)
         return out if stats else None
+
+    def tune(self, sample_tiles=304, reps=2):
+        """Autotune every group's launch parameters (kernel layout, vectors per
+        work item, precise-residual period) on its first ``sample_tiles`` tiles
+        and cache the winners; later runs use them when ``tuned``.  Returns
+        {shape: (kwargs, ms)}."""
+        out = {}
+        for g in self.groups:
+            k = min(g.T, sample_tiles)
+            out["%dx%d" % (g.n, g.m)] = autotune.tune(g.G[:k].contiguous(), g.vin[:, :k].contiguous(),
+                                                      g_wire=self.g_wire, method=self.method, reps=reps)
+        return out
 
     def capture(self):
         """Record run() as a CUDA graph (warm-up launch first, as graph capture needs)."""

@@ -15,10 +15,18 @@ pair is solved to ``options.tol_v`` (1e-8 V) of the nodal solution, so results
 match the reference's converged solver.  ``options.method = "sweeps"`` (or
 ``FADESIM_METHOD=sweeps`` in the environment) reproduces the reference's own
 sweep order for exactly ``iter_times`` sweeps instead.
+
+Solve status.  The reference returns whatever its sweeps reached.  Here every
+solve also reports whether it met the tolerance, hit the iteration cap, or met
+non-finite values; ``ir_drop_gs`` reads that status back after each call and,
+with ``options.check_status`` "warn" (the default, or ``FADESIM_CHECK_STATUS``),
+issues a ``SolveStatusWarning`` for a capped or non-finite solve, with "raise"
+raises ``SolveStatusError``, with "off" skips the read (no host synchronisation).
 """
 import ctypes
 import math
 import os
+import warnings
 from dataclasses import dataclass
 
 import torch
@@ -41,6 +49,8 @@ class SolverOptions:
     residual: str = "ff"         # precise residual: "ff" (float-float on the FP32 pipe) or "fp64"
     read_noise_sigma: float = 0.0  # > 0: Gaussian read noise, sigma relative to each cell current
     noise_seed: int = 0
+    check_status: str = os.environ.get("FADESIM_CHECK_STATUS", "warn")  # "warn", "raise" or "off"
+    kernel_ld: int = 0           # 0: layout by tile size; 32/64/128 tile per CTA, 256/512 tile per cluster
 
     def to_c(self, method=None):
         m = method if method is not None else self.method
@@ -50,10 +60,54 @@ class SolverOptions:
             raise ValueError("residual must be 'fp64' or 'ff'")
         return _lib.SolveOpts(_METHODS[m], float(self.tol_v), int(self.max_iters), int(self.residual_period),
                               float(self.omega), int(self.vectors_per_cta), 1 if self.residual == "fp64" else 0,
-                              float(self.read_noise_sigma), int(self.noise_seed) & (2 ** 64 - 1))
+                              float(self.read_noise_sigma), int(self.noise_seed) & (2 ** 64 - 1),
+                              int(self.kernel_ld))
 
 
 options = SolverOptions()
+
+
+class SolveStatusWarning(RuntimeWarning):
+    """A solve stopped at its iteration cap or met non-finite values."""
+
+
+class SolveStatusError(RuntimeError):
+    """Raised instead of SolveStatusWarning under check_status = "raise"."""
+
+
+def status_message(status_or, solves, method):
+    """What the OR of the per-solve status bits says went wrong, or None.  An
+    iteration cap is a failure for the converging methods only: the sweep
+    method runs exactly iter_times sweeps, as the reference does."""
+    problems = []
+    if status_or & _lib.ST_NONFINITE:
+        problems.append("non-finite values (NaN or inf in the inputs or the iterate)")
+    if (status_or & _lib.ST_MAXITER) and method != "sweeps":
+        problems.append("the iteration cap before reaching the tolerance")
+    if not problems:
+        return None
+    return "IR-drop solve: at least one of %d solves ended with %s" % (solves, " and ".join(problems))
+
+
+def resolved_method(method, row_size, col_size):
+    """The method "auto" runs: the line relaxation up to 512 x 512, else the sweep order."""
+    if method == "auto":
+        return "line" if max(row_size, col_size) <= 512 else "sweeps"
+    return method
+
+
+def check_solve_status(stats, method, policy):
+    """Apply the check_status policy to a stats dict (solves, status_or, ...)."""
+    if policy == "off" or stats is None:
+        return
+    if policy not in ("warn", "raise"):
+        raise ValueError("check_status must be 'warn', 'raise' or 'off'")
+    msg = status_message(int(stats["status_or"]), int(stats["solves"]), method)
+    if msg is None:
+        return
+    if policy == "raise":
+        raise SolveStatusError(msg)
+    warnings.warn(msg, SolveStatusWarning, stacklevel=3)
 
 
 def _check_input(t, name):
@@ -118,19 +172,24 @@ def ir_drop_gs(input, G, batch_size, row_size, col_size, numX, numY, iter_times,
 
     input [batch, numX, rows] and G [numX, rows, numY*cols], contiguous CUDA,
     float32 or float64; returns bitline currents [batch, numX, numY*cols], or
-    the cell voltages [batch, numX, numY, rows, cols] when ``ret_V``.
+    the cell voltages [batch, numX, numY, rows, cols] when ``ret_V``.  The
+    solves' status is checked per ``options.check_status``.
     """
-    out, _, _ = _solve(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, beta, enable_break,
-                       break_threshould, nonlinear_cell_enable, nonlinear_params, ret_V, options.to_c(), False,
-                       False)
+    check = options.check_status != "off"
+    out, st, _ = _solve(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, beta,
+                        enable_break, break_threshould, nonlinear_cell_enable, nonlinear_params, ret_V,
+                        options.to_c(), check, False)
+    if check:
+        check_solve_status(dict(solves=int(st.solves), status_or=int(st.status_or)),
+                           resolved_method(options.method, row_size, col_size), options.check_status)
     return out
 
 
 def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_times=600, g_wire=1 / 2.93, beta=1.9,
                   enable_break=False, break_threshould=1e-7, nonlinear_cell_enable=False, nonlinear_params=(),
                   ret_V=False, method=None, tol_v=None, max_iters=None, residual_period=None, omega=None,
-                  vectors_per_cta=None, residual=None, read_noise_sigma=None, noise_seed=None, return_stats=True,
-                  return_iters=False, out=None):
+                  vectors_per_cta=None, residual=None, read_noise_sigma=None, noise_seed=None, kernel_ld=None,
+                  return_stats=True, return_iters=False, out=None):
     """``ir_drop_gs`` with explicit solver options (``ret_V=2`` returns both node
     planes, [batch, numX, numY, 2, rows, cols]).  Returns (out, stats, iters):
     stats is a dict (solves, iters_sum, iters_max, status_or) and iters an int32
@@ -139,7 +198,7 @@ def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_tim
     o = SolverOptions(**{k: v for k, v in vars(options).items()})
     for k, v in dict(tol_v=tol_v, max_iters=max_iters, residual_period=residual_period, omega=omega,
                      vectors_per_cta=vectors_per_cta, residual=residual, read_noise_sigma=read_noise_sigma,
-                     noise_seed=noise_seed).items():
+                     noise_seed=noise_seed, kernel_ld=kernel_ld).items():
         if v is not None:
             setattr(o, k, v)
     out, st, it = _solve(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, beta,
@@ -148,7 +207,7 @@ def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_tim
     stats = None
     if st is not None:
         stats = dict(solves=int(st.solves), iters_sum=int(st.iters_sum), iters_max=int(st.iters_max),
-                     status_or=int(st.status_or))
+                     status_or=int(st.status_or), warm_rejected=int(st.warm_rejected))
     return out, stats, it
 
 
@@ -205,13 +264,15 @@ def ir_drop_gs_host(input, G, batch_size, row_size, col_size, numX, numY, iter_t
     _lib.check(rc)
     if return_stats:
         return out, dict(solves=int(stats.solves), iters_sum=int(stats.iters_sum), iters_max=int(stats.iters_max),
-                         status_or=int(stats.status_or))
+                         status_or=int(stats.status_or), warm_rejected=int(stats.warm_rejected))
     return out
 
 
 def _family(cname, input, G, batch_size, row_size, col_size, numX, numY, out_rows, ret_V, nonlinear_cell_enable,
-            *cargs):
-    """Shared checks and launch of the IR2S / OU exports (their own iterates)."""
+            nonlinear_params, *cargs):
+    """Shared checks and launch of the IR2S / OU exports (their own iterates):
+    cargs are the C entry's arguments up to the break threshold; the sinh-cell
+    arguments (and ret_V, for ir2s) follow them."""
     _check_input(input, "input")
     _check_input(G, "G")
     if row_size < 2:
@@ -220,29 +281,33 @@ def _family(cname, input, G, batch_size, row_size, col_size, numX, numY, out_row
         raise RuntimeError("col_size should be >=2")
     if input.dtype not in (torch.float32, torch.float64) or G.dtype != input.dtype:
         raise RuntimeError("input and G must both be float32 or both float64")
-    if nonlinear_cell_enable:
-        raise NotImplementedError("%s with nonlinear cells is not implemented in this build; ir_drop_gs handles "
-                                  "them" % cname)
     lib = _lib.load()
     shape = (batch_size, numX, numY, row_size, col_size) if ret_V else (batch_size, out_rows, numY * col_size)
     out = torch.empty(shape, dtype=input.dtype, device=input.device)
     dtype = _lib.F64 if input.dtype == torch.float64 else _lib.F32
+    params = [float(v) for v in (nonlinear_params or [])] if nonlinear_cell_enable else []
+    cparams = (ctypes.c_double * len(params))(*params) if params else None
+    nl = (int(bool(nonlinear_cell_enable)), cparams, len(params))
+    tail = (int(bool(ret_V)),) if cname == "ir2s" else ()
     with torch.cuda.device(input.device):
         stream = torch.cuda.current_stream(input.device).cuda_stream
-        rc = getattr(lib, "fadesim_" + cname)(dtype, input.data_ptr(), G.data_ptr(), *cargs, out.data_ptr(), stream)
+        rc = getattr(lib, "fadesim_" + cname)(dtype, input.data_ptr(), G.data_ptr(), *cargs, *nl, *tail,
+                                              out.data_ptr(), stream)
     _lib.check(rc)
     return out
 
 
 # The reference module's other exports (split_arr_matmul.cu:1429-1437): the IR2S
-# iteration and the operation-unit (OU) variants, reproducing their iterates.
+# iteration and the operation-unit (OU) variants, reproducing their iterates,
+# with linear or sinh cells (nonlinear_params = [R_on, R_off, a_on, b_on, a_off,
+# b_off], commonConst.py:207).
 def ir2s(input, G, batch_size, row_size, col_size, numX, numY, iter_times, r_wire, enable_break, break_threshould,
          nonlinear_cell_enable=False, nonlinear_params=(), ret_V=False):
     """ir2s (split_arr_matmul.cu:419-545): the IR-drop-to-source iteration with
     the wire resistance r_wire (also the source and ground loads)."""
     return _family("ir2s", input, G, batch_size, row_size, col_size, numX, numY, numX, ret_V,
-                   nonlinear_cell_enable, batch_size, row_size, col_size, numX, numY, iter_times, float(r_wire),
-                   int(bool(enable_break)), float(break_threshould), int(bool(ret_V)))
+                   nonlinear_cell_enable, nonlinear_params, batch_size, row_size, col_size, numX, numY, iter_times,
+                   float(r_wire), int(bool(enable_break)), float(break_threshould))
 
 
 def ir2s_ou_local(input, G, batch_size, row_size, col_size, numX, numY, iter_times, r_wire, r_load_left,
@@ -250,8 +315,9 @@ def ir2s_ou_local(input, G, batch_size, row_size, col_size, numX, numY, iter_tim
     """ir2s_ou_local (split_arr_matmul.cu:565-680): ir2s of one OU-sized array
     with source and ground load resistances."""
     return _family("ir2s_ou_local", input, G, batch_size, row_size, col_size, numX, numY, numX, False,
-                   nonlinear_cell_enable, batch_size, row_size, col_size, numX, numY, iter_times, float(r_wire),
-                   float(r_load_left), float(r_load_down), int(bool(enable_break)), float(break_threshould))
+                   nonlinear_cell_enable, nonlinear_params, batch_size, row_size, col_size, numX, numY, iter_times,
+                   float(r_wire), float(r_load_left), float(r_load_down), int(bool(enable_break)),
+                   float(break_threshould))
 
 
 def ir2s_ou(input, G, batch_size, row_size, col_size, ou_row_size, ou_col_size, numX, numY, iter_times, r_wire,
@@ -260,9 +326,9 @@ def ir2s_ou(input, G, batch_size, row_size, col_size, ou_row_size, ou_col_size, 
     through the lumped wire outside it; currents per OU row group
     [batch, numX * rows/ou_row_size, numY * cols]."""
     return _family("ir2s_ou", input, G, batch_size, row_size, col_size, numX, numY,
-                   numX * (row_size // max(1, ou_row_size)), False, nonlinear_cell_enable, batch_size, row_size,
-                   col_size, ou_row_size, ou_col_size, numX, numY, iter_times, float(r_wire), int(bool(enable_break)),
-                   float(break_threshould))
+                   numX * (row_size // max(1, ou_row_size)), False, nonlinear_cell_enable, nonlinear_params,
+                   batch_size, row_size, col_size, ou_row_size, ou_col_size, numX, numY, iter_times, float(r_wire),
+                   int(bool(enable_break)), float(break_threshould))
 
 
 def ir_gs_ou_local(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, g_load_left,
@@ -271,8 +337,8 @@ def ir_gs_ou_local(input, G, batch_size, row_size, col_size, numX, numY, iter_ti
     """ir_gs_ou_local (split_arr_matmul.cu:690-813): the ir_drop_gs sweep of one
     OU-sized array with source and ground load conductances."""
     return _family("ir_gs_ou_local", input, G, batch_size, row_size, col_size, numX, numY, numX, False,
-                   nonlinear_cell_enable, batch_size, row_size, col_size, numX, numY, iter_times, float(g_wire),
-                   float(g_load_left), float(g_load_down), float(beta), int(bool(enable_break)),
+                   nonlinear_cell_enable, nonlinear_params, batch_size, row_size, col_size, numX, numY, iter_times,
+                   float(g_wire), float(g_load_left), float(g_load_down), float(beta), int(bool(enable_break)),
                    float(break_threshould))
 
 
@@ -282,9 +348,9 @@ def ir_gs_ou(input, G, batch_size, row_size, col_size, ou_row_size, ou_col_size,
     array at once; currents per OU row group [batch, numX * rows/ou_row_size,
     numY * cols]."""
     return _family("ir_gs_ou", input, G, batch_size, row_size, col_size, numX, numY,
-                   numX * (row_size // max(1, ou_row_size)), False, nonlinear_cell_enable, batch_size, row_size,
-                   col_size, ou_row_size, ou_col_size, numX, numY, iter_times, float(g_wire), float(beta),
-                   int(bool(enable_break)), float(break_threshould))
+                   numX * (row_size // max(1, ou_row_size)), False, nonlinear_cell_enable, nonlinear_params,
+                   batch_size, row_size, col_size, ou_row_size, ou_col_size, numX, numY, iter_times, float(g_wire),
+                   float(beta), int(bool(enable_break)), float(break_threshould))
 
 
 def ir_drop_gs_warm(input, G, batch_size, row_size, col_size, numX, numY, init, g_wire=1 / 2.93, tol_v=None,
@@ -316,4 +382,4 @@ def ir_drop_gs_warm(input, G, batch_size, row_size, col_size, numX, numY, init, 
                                          torch.cuda.current_stream(input.device).cuda_stream)
     _lib.check(rc)
     return out, dict(solves=int(st.solves), iters_sum=int(st.iters_sum), iters_max=int(st.iters_max),
-                     status_or=int(st.status_or)), iters
+                     status_or=int(st.status_or), warm_rejected=int(st.warm_rejected)), iters

@@ -133,6 +133,7 @@ int finish_stats(DevStats *dst, fadesim_solve_stats *stats, cudaStream_t st) {
     stats->iters_sum = (int64_t)h.iters_sum;
     stats->iters_max = h.iters_max;
     stats->status_or = h.status_or;
+    stats->warm_rejected = (int64_t)h.warm_rejected;
     return FADESIM_OK;
 }
 
@@ -150,6 +151,15 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
         ld = line_relax_ld(a.n, a.m);
         cld = ld ? 0 : cluster_relax_ld(a.n, a.m);
         if (!ld && !cld) return fail(FADESIM_E_UNSUPPORTED, "line relaxation in this build handles rows, cols <= 512");
+        const int want = opts ? opts->kernel_ld : 0;  // a forced layout (the autotuner's shape axis)
+        if (want) {
+            if (want != 32 && want != 64 && want != 128 && want != 256 && want != 512)
+                return fail(FADESIM_E_ARG, "kernel_ld must be 0, 32, 64, 128, 256 or 512");
+            if (L > want) return fail(FADESIM_E_ARG, "kernel_ld is smaller than the tile");
+            ld = want <= 128 ? want : 0;
+            cld = want > 128 ? want : 0;
+            if (a.init && cld) return fail(FADESIM_E_UNSUPPORTED, "warm starts run on the single-CTA layouts");
+        }
         a.ctl.max_iters = (opts && opts->max_iters > 0) ? opts->max_iters : 400;
         a.ctl.omega = (opts && opts->omega > 0) ? (float)opts->omega : 0.f;
         if (ld) {
@@ -173,14 +183,34 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
             scratch_floats = cluster_relax_scratch_floats_per_cta(cld) * grid;
         }
     } else {
-        if (L > 128) return fail(FADESIM_E_UNSUPPORTED, "red-black SOR in this build handles rows, cols <= 128");
+        if (L > 512) return fail(FADESIM_E_UNSUPPORTED, "red-black SOR in this build handles rows, cols <= 512");
         a.ctl.max_iters = (opts && opts->max_iters > 0) ? opts->max_iters : 20000;
         a.ctl.omega = (opts && opts->omega > 0) ? (float)opts->omega
                                                 : (float)(2.0 / (1.0 + sin(M_PI / (2.0 * L + 1.0))));
-        CUDA_TRY(rbsor_prepare(dtype));
-        grid = sms;
-        plan_items(a, grid, opts ? opts->vectors_per_cta : 0);
-        if ((long long)grid > a.nitems) grid = (int)a.nitems;
+        cld = rbsor_cluster_ld(a.n, a.m);
+        const int want = opts ? opts->kernel_ld : 0;  // a forced layout: 128 single-CTA, 256 / 512 clusters
+        if (want) {
+            if (want != 128 && want != 256 && want != 512)
+                return fail(FADESIM_E_ARG, "kernel_ld must be 0, 128, 256 or 512 for red-black SOR");
+            if (L > want) return fail(FADESIM_E_ARG, "kernel_ld is smaller than the tile");
+            cld = want > 128 ? want : 0;
+            if (a.init && cld) return fail(FADESIM_E_UNSUPPORTED, "warm starts run on the single-CTA layouts");
+        }
+        if (!cld) {
+            CUDA_TRY(rbsor_prepare(dtype));
+            grid = sms;
+            plan_items(a, grid, opts ? opts->vectors_per_cta : 0);
+            if ((long long)grid > a.nitems) grid = (int)a.nitems;
+        } else {
+            int clusters = 0;
+            CUDA_TRY(rbsor_cluster_occupancy(cld, dtype, &clusters));
+            if (clusters < 1)
+                return fail(FADESIM_E_UNSUPPORTED, "this device cannot co-schedule the cluster the tile size needs");
+            plan_items(a, clusters, opts ? opts->vectors_per_cta : 0);
+            if ((long long)clusters > a.nitems) clusters = (int)a.nitems;
+            grid = clusters * rbsor_cluster_size(cld);
+            scratch_floats = rbsor_cluster_scratch_floats_per_cta(cld) * grid;
+        }
     }
     Scratch scr;
     scr.st = st;
@@ -194,6 +224,8 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
         CUDA_TRY(launch_line_relax(a, ld, dtype, grid, st));
     } else if (method == FADESIM_METHOD_LINE) {
         CUDA_TRY(launch_cluster_relax(a, cld, dtype, grid, st));
+    } else if (cld) {
+        CUDA_TRY(launch_rbsor_cluster(a, cld, dtype, grid, st));
     } else {
         CUDA_TRY(launch_rbsor(a, dtype, grid, st));
     }
@@ -258,7 +290,7 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
     g_err.clear();
     if (dtype != FADESIM_F32 && dtype != FADESIM_F64) return fail(FADESIM_E_ARG, "dtype must be f32 or f64");
     if (batch_size == 0 && row_size >= 2 && col_size >= 2) {
-        if (stats) *stats = fadesim_solve_stats{0, 0, 0, 0};
+        if (stats) *stats = fadesim_solve_stats{0, 0, 0, 0, 0};
         return FADESIM_OK;  // nothing to solve; empty tensors may carry null pointers
     }
     if (!input || !G || !out) return fail(FADESIM_E_ARG, "input, G and out must be device pointers");
@@ -273,7 +305,7 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
         if (!(q[1] > q[0]) || !(q[2] > 0) || !(q[3] > 0) || !(q[4] > 0) || !(q[5] > 0))
             return fail(FADESIM_E_ARG, "nonlinear_params need R_off > R_on and positive a, b");
     }
-    if (stats) *stats = fadesim_solve_stats{0, 0, 0, 0};
+    if (stats) *stats = fadesim_solve_stats{0, 0, 0, 0, 0};
     if (batch_size == 0) return FADESIM_OK;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     SolveArgs a{};
@@ -311,8 +343,36 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
     if (method == FADESIM_METHOD_AUTO)
         method = (line_relax_ld(row_size, col_size) || cluster_relax_ld(row_size, col_size)) ? FADESIM_METHOD_LINE
                                                                                            : FADESIM_METHOD_SWEEPS;
+    if (nonlinear_cell_enable && method == FADESIM_METHOD_SWEEPS) {
+        // the reference's own sweeps with per-sweep re-linearised cells
+        if (iter_times < 0) return fail(FADESIM_E_ARG, "iter_times must be >= 0");
+        if (ret_V == 2) return fail(FADESIM_E_UNSUPPORTED, "ret_V = 2 is not available for the sweep method");
+        if (row_size > 1024 || col_size > 1024) return fail(FADESIM_E_ARG, "row_size and col_size must be <= 1024");
+        if (a.ctl.noise_sigma > 0) return fail(FADESIM_E_UNSUPPORTED, "read noise applies to the line method's currents");
+        int done = 0;
+        const int rc = family_gs_nonlinear(dtype, input, G, batch_size, row_size, col_size, numX, numY, iter_times,
+                                           g_wire, beta, enable_break, break_threshould, nonlinear_params,
+                                           ret_V ? 1 : 0, out, &done, st);
+        if (rc != FADESIM_OK) return rc;
+        if (per_solve_iters) {
+            const size_t nsol = (size_t)batch_size * numX * numY;
+            std::string tmp(nsol * sizeof(int), '\0');
+            int *h = reinterpret_cast<int *>(&tmp[0]);
+            for (size_t k = 0; k < nsol; ++k) h[k] = done;
+            CUDA_TRY(cudaMemcpyAsync(per_solve_iters, h, nsol * sizeof(int), cudaMemcpyHostToDevice, st));
+            CUDA_TRY(cudaStreamSynchronize(st));
+        }
+        if (stats) {
+            stats->solves = (int64_t)batch_size * numX * numY;
+            stats->iters_sum = stats->solves * done;
+            stats->iters_max = done;
+            stats->status_or = (enable_break && done < iter_times) ? FADESIM_ST_CONVERGED : FADESIM_ST_MAXITER;
+            CUDA_TRY(cudaStreamSynchronize(st));
+        }
+        return FADESIM_OK;
+    }
     if (nonlinear_cell_enable && method != FADESIM_METHOD_LINE)
-        return fail(FADESIM_E_UNSUPPORTED, "nonlinear cells are solved by the line method (rows, cols <= 512)");
+        return fail(FADESIM_E_UNSUPPORTED, "nonlinear cells are solved by the line method or the sweep order");
     if (a.ctl.noise_sigma > 0 && (method != FADESIM_METHOD_LINE || ret_V))
         return fail(FADESIM_E_UNSUPPORTED, "read noise applies to the line method's currents");
     switch (method) {

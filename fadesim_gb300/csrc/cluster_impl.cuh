@@ -608,7 +608,25 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
     float rate_hint = 0.f;  // first-step rate of the previous vector of this tile (cluster-uniform)
     float omega_prev = 0.f; // final relaxation factor of that vector (cluster-uniform)
     float gs_max = 0.f;     // largest g / gw of the tile (cluster-uniform, linear cells)
-    for (long long item = cid; item < a.nitems; item += ncl) {
+    // work queue: rank 0 of every cluster claims the cluster's next (tile,
+    // vector chunk) item from the call's counter and the cluster reads it after
+    // a cluster barrier (rank 0 claims again only after the item's own cluster
+    // barriers, which every CTA reaches after reading the claim)
+    __shared__ long long s_item;
+    long long next_static = cid;
+    auto claim = [&]() -> long long {
+        if (rank == 0 && tid == 0) {
+            if (a.stats) {
+                s_item = (long long)atomicAdd(&a.stats->queue_head, 1ull);
+            } else {
+                s_item = next_static;
+                next_static += ncl;
+            }
+        }
+        cluster.sync();
+        return *cluster.map_shared_rank(&s_item, 0);
+    };
+    for (long long item = claim(); item < a.nitems; item = claim()) {
         const long long tile = item / a.nchunks;
         const int chunk = (int)(item % a.nchunks);
         const int x = (int)(tile / a.numY), y = (int)(tile % a.numY);

@@ -13,6 +13,8 @@ struct DevStats {
     unsigned long long iters_sum;
     int iters_max;
     int status_or;
+    unsigned long long queue_head;  // next work item of the call's queue (persistent kernels claim items)
+    unsigned long long warm_rejected;  // solves whose warm start was discarded
 };
 
 // Solver controls shared by the converging kernels.
@@ -102,6 +104,11 @@ __device__ __forceinline__ float nl_gs(float cell, float V, const SolveCtl &c, f
 __device__ __forceinline__ float nl_g(float cell, float V, const SolveCtl &c, float gw) {
     return c.nl_single_a ? (cell * gw) * sinhc(c.nl_a_on * fabsf(V)) : nl_geff(cell, V, c);
 }
+
+// Second counter of the cycle-to-cycle variation draws (normal_from(seed, cell,
+// kVariationStream)); the read noise uses (seed, solve, cell of a tile < 2^18),
+// so the two streams never share a counter pair.
+constexpr unsigned long long kVariationStream = 0x7661726961ull;
 
 // Standard normal from a counter (splitmix64 hash, Box-Muller): the same value
 // for the same (seed, a, b) on every run and every device.

@@ -161,6 +161,7 @@ extern "C" int fadesim_ir_drop_gs_host(int dtype, const void *input, const void 
             stats->iters_sum += gs.iters_sum;
             if (gs.iters_max > stats->iters_max) stats->iters_max = gs.iters_max;
             stats->status_or |= gs.status_or;
+            stats->warm_rejected += gs.warm_rejected;
         }
         e = cudaMemcpy2DAsync(hout + (size_t)x0 * out_x * es, (size_t)numX * out_x * es, dout,
                               (size_t)gx * out_x * es, (size_t)gx * out_x * es, (size_t)batch_size,

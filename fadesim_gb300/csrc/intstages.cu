@@ -14,6 +14,7 @@
 // reference's order (__fmul_rn / __fadd_rn / __fdiv_rn keep the compiler from
 // fusing them); scalar operands arrive already rounded to float32, as torch
 // rounds a Python scalar combined with a float32 tensor.
+#include <math.h>
 #include <stdint.h>
 
 #include "kernels.h"
@@ -217,12 +218,39 @@ __global__ void adc_shift_add_kernel(const float *__restrict__ I, int ref_cols, 
     }
 }
 
+// Cycle-to-cycle variation of a conductance map: out = G / f with f the
+// host-drawn divisor (the reference's exp(sigma N(0,1)) from its CPU generator,
+// conductance_variation.py:6-13; one correctly rounded division, as torch's),
+// or, without divisors, f = exp(sigma z) with z standard normal from a counter
+// hash of (seed, offset + k): the same numbers on every run and device, drawn
+// where the map lives (R becomes R exp(sigma z), the lognormal spread).
+__global__ void vary_conductance_kernel(const float *__restrict__ G, const float *__restrict__ div, long long n,
+                                        float sigma, unsigned long long seed, unsigned long long offset,
+                                        float *__restrict__ out) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const float f = div ? div[e]
+                            : expf(sigma * fadesim::normal_from(seed, offset + (unsigned long long)e,
+                                                                fadesim::kVariationStream));
+        out[e] = __fdiv_rn(G[e], f);
+    }
+}
+
 int grid_for(long long total) {
     long long g = (total + 255) / 256;
     return (int)(g > 16384 ? 16384 : (g < 1 ? 1 : g));
 }
 
 }  // namespace
+
+extern "C" int fadesim_vary_conductance_f32(const float *G, const float *divisor, long long n, double sigma,
+                                            unsigned long long seed, unsigned long long offset, float *out,
+                                            void *stream) {
+    if (!G || !out || n < 0 || !isfinite(sigma) || sigma < 0) return FADESIM_E_ARG;
+    if (n == 0) return FADESIM_OK;
+    vary_conductance_kernel<<<grid_for(n), 256, 0, (cudaStream_t)stream>>>(G, divisor, n, (float)sigma, seed, offset,
+                                                                          out);
+    return cudaGetLastError() == cudaSuccess ? FADESIM_OK : FADESIM_E_CUDA;
+}
 
 extern "C" int fadesim_quantize_f32(const float *x, long long n, int s, int32_t *q, void *stream) {
     if (!x || !q || n < 0) return FADESIM_E_ARG;

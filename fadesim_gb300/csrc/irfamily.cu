@@ -22,6 +22,16 @@
 // operand order.  With a break threshold the host reads the count of nodes
 // that moved more than it after every iteration (the reference's two .item()
 // reductions, :297-306).
+//
+// Sinh cells (nonlinear_cell_enable, :455-475, 603-622, 727-746, 996-1016,
+// 1241-1260): before every iteration each solve's conductances are recomputed
+// cell by cell, in the I/O type, from u - d of the iterate before the newest
+// one (what the reference's ping-pong buffers hold when it recomputes them;
+// iterations 0 and 1 both see the initial planes), |V| < 1e-5 set to +-1e-5
+// (deal_v, :142-166), R(V) = (1-z) |V| / (b_on sinh(a_on |V|)) + z |V| /
+// (b_off sinh(a_off |V|)) with z = (1/g - R_on) / (R_off - R_on) from the linear
+// conductance, negative z set to 0 (:176-196).  The conductances then live in
+// one plane per solve, and the currents use the last of them (get_current).
 #include "kernels.h"
 #include "trace.h"
 
@@ -56,14 +66,15 @@ __global__ void fam_init_kernel(const S *__restrict__ input, S *__restrict__ U, 
 template <typename S>
 __global__ void fam_gs_sweep_kernel(const S *__restrict__ input, const S *__restrict__ G, S *__restrict__ U,
                                     S *__restrict__ D, int numX, int numY, OuShape o, S g_wire, S gll, S gdl, S beta,
-                                    S thr, unsigned int *moved) {
+                                    S thr, unsigned int *moved, int gsol) {
     const int b = blockIdx.x, x = blockIdx.y, y = blockIdx.z;
     const int n = o.n, m = o.m;
     const size_t plane = (((size_t)b * numX + x) * numY + y) * n * m;
     S *u = U + plane;
     S *d = D + plane;
-    const size_t ldG = (size_t)numY * m;
-    const S *g = G + (size_t)x * n * ldG + (size_t)y * m;  // g[i*ldG + j]
+    // g[i*ldG + j]: the tile's map, or this solve's own plane (sinh cells)
+    const size_t ldG = gsol ? (size_t)m : (size_t)numY * m;
+    const S *g = gsol ? G + plane : G + (size_t)x * n * ldG + (size_t)y * m;
     unsigned int cnt = 0;
     // wordline segments: one thread per (row, OU column)
     for (int w = threadIdx.x; w < n * o.noy; w += blockDim.x) {
@@ -148,15 +159,15 @@ template <typename S>
 __global__ void fam_ir2s_kernel(const S *__restrict__ input, const S *__restrict__ G, const S *__restrict__ Up,
                                 const S *__restrict__ Dp, S *__restrict__ Un, S *__restrict__ Dn, S *__restrict__ Rsum,
                                 S *__restrict__ Csum, int numX, int numY, OuShape o, S r_wire, S rll, S rdl, S thr,
-                                unsigned int *moved) {
+                                unsigned int *moved, int gsol) {
     const int b = blockIdx.x, x = blockIdx.y, y = blockIdx.z;
     const int n = o.n, m = o.m;
     const size_t sol = ((size_t)b * numX + x) * numY + y;
     const size_t plane = sol * n * m;
     const S *up = Up + plane, *dp = Dp + plane;
     S *un = Un + plane, *dn = Dn + plane;
-    const size_t ldG = (size_t)numY * m;
-    const S *g = G + (size_t)x * n * ldG + (size_t)y * m;
+    const size_t ldG = gsol ? (size_t)m : (size_t)numY * m;
+    const S *g = gsol ? G + plane : G + (size_t)x * n * ldG + (size_t)y * m;
     unsigned int cnt = 0;
     for (int w = threadIdx.x; w < n * o.noy; w += blockDim.x) {
         const int row = w / o.noy, sy = w % o.noy, s = sy * o.om;
@@ -203,7 +214,7 @@ __global__ void fam_ir2s_kernel(const S *__restrict__ input, const S *__restrict
 // the OU's rows (ascending) of (u - d) g; one group = a whole column.
 template <typename S>
 __global__ void fam_current_kernel(const S *__restrict__ U, const S *__restrict__ D, const S *__restrict__ G,
-                                   S *__restrict__ out, int B, int numX, int numY, OuShape o) {
+                                   S *__restrict__ out, int B, int numX, int numY, OuShape o, int gsol) {
     const int n = o.n, m = o.m;
     const size_t total = (size_t)B * numX * o.nox * numY * m;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
@@ -213,11 +224,55 @@ __global__ void fam_current_kernel(const S *__restrict__ U, const S *__restrict_
         const size_t bx = e / ((size_t)m * numY * o.nox);  // b*numX + x
         const int x = (int)(bx % numX);
         const size_t plane = (bx * numY + y) * n * m;
-        const S *g = G + (size_t)x * n * numY * m + (size_t)y * m + col;
+        const size_t ldG = gsol ? (size_t)m : (size_t)numY * m;
+        const S *g = gsol ? G + plane + col : G + (size_t)x * n * numY * m + (size_t)y * m + col;
         S acc = 0;
         for (int i = sx * o.on; i < (sx + 1) * o.on; ++i)
-            acc += (U[plane + (size_t)i * m + col] - D[plane + (size_t)i * m + col]) * g[(size_t)i * numY * m];
+            acc += (U[plane + (size_t)i * m + col] - D[plane + (size_t)i * m + col]) * g[(size_t)i * ldG];
         out[e] = acc;
+    }
+}
+
+// Sinh-cell parameters in the I/O type.
+template <typename S>
+struct FamNl {
+    S R_on, dR, a_on, b_on, a_off, b_off;
+};
+
+// z = (1/g - R_on) / (R_off - R_on), negative z set to 0, per cell of the maps
+// [numX, n, numY*m] (get_nonlinear_ratio_z, :176-182).
+template <typename S>
+__global__ void fam_nl_z_kernel(const S *__restrict__ G, S *__restrict__ z, size_t total, FamNl<S> p) {
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const S r = (S)1 / G[e];
+        const S v = (r - p.R_on) / p.dR;
+        z[e] = v < (S)0 ? (S)0 : v;
+    }
+}
+
+// Before an iteration: every solve's conductances from the lagged planes
+// (deal_v, then 1 / R(V), :142-196), and the lag advanced to the current
+// planes.  Gn, U, D, LU, LD are [B, numX, numY, n, m]; z is [numX, n, numY*m].
+template <typename S>
+__global__ void fam_nl_refresh_kernel(const S *__restrict__ z, const S *__restrict__ U, const S *__restrict__ D,
+                                      S *__restrict__ LU, S *__restrict__ LD, S *__restrict__ Gn, int B, int numX,
+                                      int numY, int n, int m, FamNl<S> p) {
+    const size_t total = (size_t)B * numX * numY * n * m;
+    const S eps = (S)1e-5;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(e % m);
+        const int i = (int)((e / m) % n);
+        const int y = (int)((e / ((size_t)m * n)) % numY);
+        const int x = (int)((e / ((size_t)m * n * numY)) % numX);
+        S V = LU[e] - LD[e];
+        if (V < eps && V > -eps) V = V > (S)0 ? eps : -eps;
+        const S Va = V < (S)0 ? -V : V;
+        const S zz = z[((size_t)x * n + i) * numY * m + (size_t)y * m + j];
+        const S I_on = p.b_on * sinh(Va * p.a_on);
+        const S I_off = p.b_off * sinh(Va * p.a_off);
+        Gn[e] = (S)1 / (((S)1 - zz) * Va / I_on + zz * Va / I_off);
+        LU[e] = U[e];
+        LD[e] = D[e];
     }
 }
 
@@ -232,23 +287,45 @@ int fam_grid(size_t total) {
     return (int)(g > 16384 ? 16384 : (g < 1 ? 1 : g));
 }
 
-// Host driver shared by the five entry points.
+// Host driver shared by the five entry points.  nl: the sinh-cell parameters
+// [R_on, R_off, a_on, b_on, a_off, b_off], or null for linear cells.
 template <typename S>
 int fam_run(bool ir2s, const void *input_v, const void *G_v, int B, OuShape o, int numX, int numY, int iter_times,
             double wire, double load_l, double load_d, double beta, int enable_break, double thr, int ret_V,
-            void *out_v, cudaStream_t st) {
+            const double *nl, void *out_v, cudaStream_t st, int *done_out = nullptr) {
     const S *input = static_cast<const S *>(input_v);
     const S *G = static_cast<const S *>(G_v);
     S *out = static_cast<S *>(out_v);
     const size_t plane_elems = (size_t)B * numX * numY * o.n * o.m;
+    const size_t map_elems = (size_t)numX * o.n * numY * o.m;
     const size_t rsum = (size_t)B * numX * numY * o.n * o.noy, csum = (size_t)B * numX * numY * o.m * o.nox;
-    const size_t bytes = (ir2s ? 4 : 2) * plane_elems * sizeof(S) + (ir2s ? (rsum + csum) * sizeof(S) : 0) + 256;
+    // planes U, D (+ U2, D2 for IR2S), the IR2S line sums, and for sinh cells
+    // the cell positions z, the per-solve conductances and the lagged planes
+    const size_t elems = (ir2s ? 4 : 2) * plane_elems + (ir2s ? rsum + csum : 0) +
+                         (nl ? map_elems + 3 * plane_elems : 0);
+    const size_t bytes = elems * sizeof(S) + 256;
     char *buf = nullptr;
     cudaError_t e = lib_malloc_async((void **)&buf, bytes, st);
     if (e != cudaSuccess) return fail(FADESIM_E_CUDA, cudaGetErrorString(e));
     S *U = reinterpret_cast<S *>(buf), *D = U + plane_elems;
-    S *U2 = ir2s ? D + plane_elems : nullptr, *D2 = ir2s ? U2 + plane_elems : nullptr;
-    S *Rs = ir2s ? D2 + plane_elems : nullptr, *Cs = ir2s ? Rs + rsum : nullptr;
+    S *next = D + plane_elems;
+    S *U2 = nullptr, *D2 = nullptr, *Rs = nullptr, *Cs = nullptr;
+    if (ir2s) {
+        U2 = next;
+        D2 = U2 + plane_elems;
+        Rs = D2 + plane_elems;
+        Cs = Rs + rsum;
+        next = Cs + csum;
+    }
+    S *Z = nullptr, *Gn = nullptr, *LU = nullptr, *LD = nullptr;
+    FamNl<S> p{};
+    if (nl) {
+        Z = next;
+        Gn = Z + map_elems;
+        LU = Gn + plane_elems;
+        LD = LU + plane_elems;
+        p = FamNl<S>{(S)nl[0], (S)(nl[1] - nl[0]), (S)nl[2], (S)nl[3], (S)nl[4], (S)nl[5]};
+    }
     unsigned int *moved = reinterpret_cast<unsigned int *>(buf + bytes - 256);
     int rc = FADESIM_OK;
     fam_init_kernel<S><<<fam_grid(plane_elems), 256, 0, st>>>(input, U, D, B, numX, numY, o.n, o.m);
@@ -257,7 +334,18 @@ int fam_run(bool ir2s, const void *input_v, const void *G_v, int B, OuShape o, i
         e = cudaMemcpyAsync(U2, U, 2 * plane_elems * sizeof(S), cudaMemcpyDeviceToDevice, st);  // U2, D2 <- U, D
         if (e == cudaSuccess) e = cudaMemsetAsync(Rs, 0, (rsum + csum) * sizeof(S), st);
     }
+    if (e == cudaSuccess && nl) {
+        e = cudaMemcpyAsync(LU, U, plane_elems * sizeof(S), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(LD, D, plane_elems * sizeof(S), cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess) {
+            fam_nl_z_kernel<S><<<fam_grid(map_elems), 256, 0, st>>>(G, Z, map_elems, p);
+            e = cudaGetLastError();
+        }
+    }
     if (e != cudaSuccess) rc = fail(FADESIM_E_CUDA, cudaGetErrorString(e));
+    const S *Gi = nl ? Gn : G;  // what the iterations read
+    const int gsol = nl ? 1 : 0;
+    int done = 0;
     const dim3 grid(B, numX, numY);
     const int threads = (int)min(1024, ((max(o.n * o.noy, o.m * o.nox) + 31) / 32) * 32);
     for (int it = 0; rc == FADESIM_OK && it < iter_times && B > 0; ++it) {
@@ -266,9 +354,17 @@ int fam_run(bool ir2s, const void *input_v, const void *G_v, int B, OuShape o, i
             rc = fail(FADESIM_E_CUDA, cudaGetErrorString(e));
             break;
         }
+        if (nl) {
+            fam_nl_refresh_kernel<S><<<fam_grid(plane_elems), 256, 0, st>>>(Z, U, D, LU, LD, Gn, B, numX, numY, o.n,
+                                                                             o.m, p);
+            if ((e = cudaGetLastError()) != cudaSuccess) {
+                rc = fail(FADESIM_E_CUDA, cudaGetErrorString(e));
+                break;
+            }
+        }
         if (ir2s) {
-            fam_ir2s_kernel<S><<<grid, threads, 0, st>>>(input, G, U, D, U2, D2, Rs, Cs, numX, numY, o, (S)wire,
-                                                          (S)load_l, (S)load_d, (S)thr, mv);
+            fam_ir2s_kernel<S><<<grid, threads, 0, st>>>(input, Gi, U, D, U2, D2, Rs, Cs, numX, numY, o, (S)wire,
+                                                          (S)load_l, (S)load_d, (S)thr, mv, gsol);
             S *t = U;
             U = U2;
             U2 = t;
@@ -276,13 +372,14 @@ int fam_run(bool ir2s, const void *input_v, const void *G_v, int B, OuShape o, i
             D = D2;
             D2 = t;
         } else {
-            fam_gs_sweep_kernel<S><<<grid, threads, 0, st>>>(input, G, U, D, numX, numY, o, (S)wire, (S)load_l,
-                                                              (S)load_d, (S)beta, (S)thr, mv);
+            fam_gs_sweep_kernel<S><<<grid, threads, 0, st>>>(input, Gi, U, D, numX, numY, o, (S)wire, (S)load_l,
+                                                              (S)load_d, (S)beta, (S)thr, mv, gsol);
         }
         if ((e = cudaGetLastError()) != cudaSuccess) {
             rc = fail(FADESIM_E_CUDA, cudaGetErrorString(e));
             break;
         }
+        ++done;
         if (mv) {
             unsigned int h = 0;
             e = cudaMemcpyAsync(&h, mv, sizeof(h), cudaMemcpyDeviceToHost, st);
@@ -295,14 +392,18 @@ int fam_run(bool ir2s, const void *input_v, const void *G_v, int B, OuShape o, i
         }
     }
     if (rc == FADESIM_OK) {
+        // the currents use the last conductances the iterations used (the linear
+        // map when no iteration ran)
+        const bool last_nl = nl && done > 0;
         if (ret_V)
             fam_voltage_kernel<S><<<fam_grid(plane_elems), 256, 0, st>>>(U, D, out, plane_elems);
         else
-            fam_current_kernel<S><<<fam_grid((size_t)B * numX * o.nox * numY * o.m), 256, 0, st>>>(U, D, G, out, B,
-                                                                                                 numX, numY, o);
+            fam_current_kernel<S><<<fam_grid((size_t)B * numX * o.nox * numY * o.m), 256, 0, st>>>(
+                U, D, last_nl ? Gn : G, out, B, numX, numY, o, last_nl ? 1 : 0);
         if ((e = cudaGetLastError()) != cudaSuccess) rc = fail(FADESIM_E_CUDA, cudaGetErrorString(e));
     }
     cudaFreeAsync(buf, st);
+    if (done_out) *done_out = done;
     return rc;
 }
 
@@ -320,20 +421,56 @@ int fam_check(int dtype, const void *input, const void *G, void *out, int B, int
     return FADESIM_OK;
 }
 
+// Sinh-cell parameters of a family call: null for linear cells, an argument
+// error (code in *rc) for an unusable set.  Checks as fadesim_ir_drop_gs_ex.
+const double *fam_nl(int enable, const double *params, int n_params, int *rc) {
+    *rc = FADESIM_OK;
+    if (!enable) return nullptr;
+    if (!params || n_params < 6) {
+        *rc = fail(FADESIM_E_ARG, "nonlinear_params must hold [R_on, R_off, a_on, b_on, a_off, b_off]");
+        return nullptr;
+    }
+    const double *q = params;
+    if (!(q[1] > q[0]) || !(q[0] > 0) || !(q[2] > 0) || !(q[3] > 0) || !(q[4] > 0) || !(q[5] > 0)) {
+        *rc = fail(FADESIM_E_ARG, "nonlinear_params need R_off > R_on > 0 and positive a, b");
+        return nullptr;
+    }
+    return params;
+}
+
 int fam_dispatch(int dtype, bool ir2s, const void *input, const void *G, int B, OuShape o, int numX, int numY,
                  int iter_times, double wire, double load_l, double load_d, double beta, int enable_break, double thr,
-                 int ret_V, void *out, void *stream) {
+                 int ret_V, const double *nl, void *out, void *stream) {
     if (B == 0) return FADESIM_OK;
     TraceRange trace(ir2s ? "fadesim_ir2s_family" : "fadesim_ir_gs_ou_family");
     cudaStream_t st = (cudaStream_t)stream;
     return dtype == FADESIM_F64
                ? fam_run<double>(ir2s, input, G, B, o, numX, numY, iter_times, wire, load_l, load_d, beta, enable_break,
-                                 thr, ret_V, out, st)
+                                 thr, ret_V, nl, out, st)
                : fam_run<float>(ir2s, input, G, B, o, numX, numY, iter_times, wire, load_l, load_d, beta, enable_break,
-                                thr, ret_V, out, st);
+                                thr, ret_V, nl, out, st);
 }
 
 }  // namespace
+
+// ir_drop_gs's own sweep order with sinh cells (split_arr_matmul.cu:204-333
+// with nonlinear_cell_enable): the family's sweep with both loads g_wire, which
+// is that sweep (:275, 290) -- same update order, same lagged conductances.
+int family_gs_nonlinear(int dtype, const void *input, const void *G, int B, int n, int m, int numX, int numY,
+                        int iter_times, double g_wire, double beta, int enable_break, double thr, const double *nl,
+                        int ret_V, void *out, int *done, cudaStream_t st) {
+    int rc = fam_check(dtype, input, G, out, B, n, m, n, m, numX, numY, iter_times, g_wire);
+    if (rc) return rc;
+    OuShape o{n, m, n, m, 1, 1, 0};
+    *done = 0;
+    if (B == 0) return FADESIM_OK;
+    TraceRange trace("fadesim_ir_drop_gs_sweeps_nonlinear");
+    return dtype == FADESIM_F64
+               ? fam_run<double>(false, input, G, B, o, numX, numY, iter_times, g_wire, g_wire, g_wire, beta,
+                                 enable_break, thr, ret_V, nl, out, st, done)
+               : fam_run<float>(false, input, G, B, o, numX, numY, iter_times, g_wire, g_wire, g_wire, beta,
+                                enable_break, thr, ret_V, nl, out, st, done);
+}
 
 }  // namespace fadesim
 
@@ -342,59 +479,76 @@ using namespace fadesim;
 extern "C" int fadesim_ir_gs_ou_local(int dtype, const void *input, const void *G, int batch_size, int row_size,
                                       int col_size, int numX, int numY, int iter_times, double g_wire,
                                       double g_load_left, double g_load_down, double beta, int enable_break,
-                                      double break_threshould, void *out, void *stream) {
+                                      double break_threshould, int nonlinear_cell_enable,
+                                      const double *nonlinear_params, int n_nonlinear_params, void *out,
+                                      void *stream) {
     int rc = fam_check(dtype, input, G, out, batch_size, row_size, col_size, row_size, col_size, numX, numY,
                        iter_times, g_wire);
     if (rc) return rc;
     if (!(g_load_left > 0) || !(g_load_down > 0)) return fail(FADESIM_E_ARG, "load conductances must be positive");
+    const double *nl = fam_nl(nonlinear_cell_enable, nonlinear_params, n_nonlinear_params, &rc);
+    if (rc) return rc;
     OuShape o{row_size, col_size, row_size, col_size, 1, 1, 0};
     return fam_dispatch(dtype, false, input, G, batch_size, o, numX, numY, iter_times, g_wire, g_load_left,
-                        g_load_down, beta, enable_break, break_threshould, 0, out, stream);
+                        g_load_down, beta, enable_break, break_threshould, 0, nl, out, stream);
 }
 
 extern "C" int fadesim_ir_gs_ou(int dtype, const void *input, const void *G, int batch_size, int row_size,
                                 int col_size, int ou_row_size, int ou_col_size, int numX, int numY, int iter_times,
-                                double g_wire, double beta, int enable_break, double break_threshould, void *out,
-                                void *stream) {
+                                double g_wire, double beta, int enable_break, double break_threshould,
+                                int nonlinear_cell_enable, const double *nonlinear_params, int n_nonlinear_params,
+                                void *out, void *stream) {
     int rc = fam_check(dtype, input, G, out, batch_size, row_size, col_size, ou_row_size, ou_col_size, numX, numY,
                        iter_times, g_wire);
     if (rc) return rc;
+    const double *nl = fam_nl(nonlinear_cell_enable, nonlinear_params, n_nonlinear_params, &rc);
+    if (rc) return rc;
     OuShape o{row_size, col_size, ou_row_size, ou_col_size, row_size / ou_row_size, col_size / ou_col_size, 1};
     return fam_dispatch(dtype, false, input, G, batch_size, o, numX, numY, iter_times, g_wire, g_wire, g_wire, beta,
-                        enable_break, break_threshould, 0, out, stream);
+                        enable_break, break_threshould, 0, nl, out, stream);
 }
 
 extern "C" int fadesim_ir2s(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
                             int numX, int numY, int iter_times, double r_wire, int enable_break,
-                            double break_threshould, int ret_V, void *out, void *stream) {
+                            double break_threshould, int nonlinear_cell_enable, const double *nonlinear_params,
+                            int n_nonlinear_params, int ret_V, void *out, void *stream) {
     int rc = fam_check(dtype, input, G, out, batch_size, row_size, col_size, row_size, col_size, numX, numY,
                        iter_times, r_wire);
     if (rc) return rc;
+    const double *nl = fam_nl(nonlinear_cell_enable, nonlinear_params, n_nonlinear_params, &rc);
+    if (rc) return rc;
     OuShape o{row_size, col_size, row_size, col_size, 1, 1, 0};
     return fam_dispatch(dtype, true, input, G, batch_size, o, numX, numY, iter_times, r_wire, r_wire, r_wire, 1.0,
-                        enable_break, break_threshould, ret_V ? 1 : 0, out, stream);
+                        enable_break, break_threshould, ret_V ? 1 : 0, nl, out, stream);
 }
 
 extern "C" int fadesim_ir2s_ou_local(int dtype, const void *input, const void *G, int batch_size, int row_size,
                                      int col_size, int numX, int numY, int iter_times, double r_wire,
                                      double r_load_left, double r_load_down, int enable_break,
-                                     double break_threshould, void *out, void *stream) {
+                                     double break_threshould, int nonlinear_cell_enable,
+                                     const double *nonlinear_params, int n_nonlinear_params, void *out,
+                                     void *stream) {
     int rc = fam_check(dtype, input, G, out, batch_size, row_size, col_size, row_size, col_size, numX, numY,
                        iter_times, r_wire);
     if (rc) return rc;
     if (!(r_load_left >= 0) || !(r_load_down >= 0)) return fail(FADESIM_E_ARG, "load resistances must be >= 0");
+    const double *nl = fam_nl(nonlinear_cell_enable, nonlinear_params, n_nonlinear_params, &rc);
+    if (rc) return rc;
     OuShape o{row_size, col_size, row_size, col_size, 1, 1, 0};
     return fam_dispatch(dtype, true, input, G, batch_size, o, numX, numY, iter_times, r_wire, r_load_left,
-                        r_load_down, 1.0, enable_break, break_threshould, 0, out, stream);
+                        r_load_down, 1.0, enable_break, break_threshould, 0, nl, out, stream);
 }
 
 extern "C" int fadesim_ir2s_ou(int dtype, const void *input, const void *G, int batch_size, int row_size,
                                int col_size, int ou_row_size, int ou_col_size, int numX, int numY, int iter_times,
-                               double r_wire, int enable_break, double break_threshould, void *out, void *stream) {
+                               double r_wire, int enable_break, double break_threshould, int nonlinear_cell_enable,
+                               const double *nonlinear_params, int n_nonlinear_params, void *out, void *stream) {
     int rc = fam_check(dtype, input, G, out, batch_size, row_size, col_size, ou_row_size, ou_col_size, numX, numY,
                        iter_times, r_wire);
     if (rc) return rc;
+    const double *nl = fam_nl(nonlinear_cell_enable, nonlinear_params, n_nonlinear_params, &rc);
+    if (rc) return rc;
     OuShape o{row_size, col_size, ou_row_size, ou_col_size, row_size / ou_row_size, col_size / ou_col_size, 1};
     return fam_dispatch(dtype, true, input, G, batch_size, o, numX, numY, iter_times, r_wire, r_wire, r_wire, 1.0,
-                        enable_break, break_threshould, 0, out, stream);
+                        enable_break, break_threshould, 0, nl, out, stream);
 }

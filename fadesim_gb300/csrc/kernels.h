@@ -58,10 +58,36 @@ size_t rbsor_smem(int n, int m);
 cudaError_t rbsor_prepare(int dtype);
 cudaError_t launch_rbsor(const SolveArgs &a, int dtype, int grid, cudaStream_t st);
 
+// Plain red-black point SOR for 128 < rows, cols <= 512 on thread-block clusters
+// (4 CTAs up to 256, 16 CTAs up to 512), bands of rows per CTA, halo rows read
+// through distributed shared memory.  Returns 256/512, or 0 if not handled.
+int rbsor_cluster_ld(int n, int m);
+int rbsor_cluster_size(int ld);
+size_t rbsor_cluster_scratch_floats_per_cta(int ld);  // the low parts of both planes of one band
+cudaError_t rbsor_cluster_occupancy(int ld, int dtype, int *clusters);
+cudaError_t launch_rbsor_cluster(const SolveArgs &a, int ld, int dtype, int grid, cudaStream_t st);
+
 // The reference's sweep order (split_arr_matmul.cu:27-119), one sweep per launch.
 cudaError_t launch_sweep(const SolveArgs &a, int dtype, void *U, void *D, double gw, double beta,
                          double thr, unsigned int *moved, cudaStream_t st);
 cudaError_t launch_sweep_init(const SolveArgs &a, int dtype, void *U, void *D, cudaStream_t st);
 cudaError_t launch_sweep_output(const SolveArgs &a, int dtype, const void *U, const void *D, cudaStream_t st);
+
+// The same sweep order with sinh cells (nl = [R_on, R_off, a_on, b_on, a_off, b_off]),
+// conductances recomputed before every sweep from the iterate before the newest
+// (irfamily.cu); *done = sweeps run.  Returns FADESIM_OK or a FADESIM_E_* code.
+int family_gs_nonlinear(int dtype, const void *input, const void *G, int B, int n, int m, int numX, int numY,
+                        int iter_times, double g_wire, double beta, int enable_break, double thr, const double *nl,
+                        int ret_V, void *out, int *done, cudaStream_t st);
+
+// Tensor-core 3x3 convolution of the warm-start network (warmnet_tc.cu): TMA
+// loads, tcgen05.mma into TMEM.  conv3x3_tc_supported: Cin a multiple of 32,
+// Cout a multiple of 16 up to 128, W a power of two up to 128, H x W a multiple
+// of 128, 16-byte aligned buffers.  err: device flag set when a bounded wait
+// expires (conv_tc_error_flag: the library's own, per device).
+bool conv3x3_tc_supported(const void *X, const void *Wt, const void *Y, int H, int W, int Cin, int Cout);
+cudaError_t conv3x3_fwd_tc(const void *X, const void *Wt, const float *bias, const void *skip, void *Y, int N, int H,
+                           int W, int Cin, int Cout, int flags, int *err, cudaStream_t st);
+int *conv_tc_error_flag();
 
 }  // namespace fadesim

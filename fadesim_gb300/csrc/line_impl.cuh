@@ -373,17 +373,35 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
     float rate_hint = 0.f;                   // final rate of the previous vector of this tile
     float omega_prev = 0.f;                  // final relaxation factor of that vector
     float gs_max = 0.f;                      // largest g / gw of the tile (linear cells)
-    __shared__ unsigned long long st_solves, st_iters;  // this CTA's counters (thread 0)
+    __shared__ unsigned long long st_solves, st_iters, st_rej;  // this CTA's counters (thread 0)
     __shared__ int st_max, st_or;
     if (tid == 0) {
         st_solves = 0;
         st_iters = 0;
+        st_rej = 0;
         st_max = 0;
         st_or = 0;
         nonfinite_flag = 0;
     }
 
-    for (long long item = blockIdx.x; item < a.nitems; item += gridDim.x) {
+    // work queue: every CTA claims its next (tile, vector chunk) item from the
+    // call's counter, so CTAs that finish early take more items
+    __shared__ long long s_item;
+    long long next_static = blockIdx.x;
+    auto claim = [&]() -> long long {
+        __syncthreads();  // every thread has read the previous claim
+        if (tid == 0) {
+            if (a.stats) {
+                s_item = (long long)atomicAdd(&a.stats->queue_head, 1ull);
+            } else {
+                s_item = next_static;
+                next_static += gridDim.x;
+            }
+        }
+        __syncthreads();
+        return s_item;
+    };
+    for (long long item = claim(); item < a.nitems; item = claim()) {
         const long long tile = item / a.nchunks;
         const int chunk = (int)(item % a.nchunks);
         const int x = (int)(tile / a.numY), y = (int)(tile % a.numY);
@@ -561,6 +579,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 st_iters += it;
                 st_max = max(st_max, it);
                 st_or |= status;
+                if (status & FADESIM_ST_WARM_REJECTED) st_rej += 1;
             }
         }
     }
@@ -570,6 +589,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
         atomicAdd(&a.stats->iters_sum, st_iters);
         atomicMax(&a.stats->iters_max, st_max);
         atomicOr(&a.stats->status_or, st_or);
+        if (st_rej) atomicAdd(&a.stats->warm_rejected, st_rej);
     }
 }
 

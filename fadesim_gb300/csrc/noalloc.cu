@@ -13,13 +13,20 @@
 // Rules of use:
 // * The first call on each device looks up the array's device address with
 //   cudaGetSymbolAddress (that device current); make that first call before
-//   any stream capture.
+//   any stream capture.  The address is kept for the process: do not use this
+//   entry across a cudaDeviceReset (the module, and the array with it, may be
+//   reloaded elsewhere).
+// * The solve stops at tol 1e-8 V (estimated max node error) or after 400 line
+//   iterations; fadesim_noalloc_last_status reads the finished call's counters
+//   (solves, iterations, status bits) back from the array without allocating.
 // * All calls share the array and it keeps the last call's contents: calls
 //   that overlap on the GPU (other streams, other host threads) race on it.
 //   The counters are cleared at the start of every call; the pivots are
 //   rewritten before use.
 // * Tiles up to 128 x 128 only (the shared-memory-resident line kernel); the
 //   grid is capped by how many CTA pivot slots fit in the array.
+#include <math.h>
+
 #include <mutex>
 #include <string>
 
@@ -75,7 +82,8 @@ extern "C" int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G
                             "(its fixed scratch serves the 128x128 shared-memory line solver)");
     if (batch_size < 0 || numX < 1 || numY < 1)
         return noalloc_fail(FADESIM_E_ARG, "fadesim_ir_drop_gs_noalloc_f32: batch_size >= 0, numX >= 1, numY >= 1");
-    if (!(g_wire > 0)) return noalloc_fail(FADESIM_E_ARG, "fadesim_ir_drop_gs_noalloc_f32: g_wire must be positive");
+    if (!(g_wire > 0) || !isfinite(g_wire))
+        return noalloc_fail(FADESIM_E_ARG, "fadesim_ir_drop_gs_noalloc_f32: g_wire must be positive and finite");
     if (batch_size == 0) return FADESIM_OK;
     if (!input || !G || !out) return noalloc_fail(FADESIM_E_ARG, "fadesim_ir_drop_gs_noalloc_f32: null pointer");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
@@ -95,8 +103,13 @@ extern "C" int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G
     int per_sm = 0, dev = 0, sms = 0;
     if ((e = line_relax_occupancy(ld, FADESIM_F32, &per_sm)) != cudaSuccess)
         return noalloc_fail(FADESIM_E_CUDA, cudaGetErrorString(e));
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (per_sm < 1)
+        return noalloc_fail(FADESIM_E_CUDA, "fadesim_ir_drop_gs_noalloc_f32: line relaxation kernel does not fit on "
+                                            "this device");
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+        return noalloc_fail(FADESIM_E_CUDA, std::string("device query: ") + cudaGetErrorString(e));
+    if (sms < 1) return noalloc_fail(FADESIM_E_CUDA, "fadesim_ir_drop_gs_noalloc_f32: device reports no SMs");
 
     SolveArgs a{};
     a.input = input;
@@ -115,7 +128,7 @@ extern "C" int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G
     a.ctl.residual_period = 0;  // adaptive, as the default of the allocating entry
     a.ctl.omega = 0.f;
     a.ctl.residual_ff = 1;
-    long long grid = (long long)(per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+    long long grid = (long long)per_sm * sms;
     if (grid > max_ctas) grid = max_ctas;
     // whole tiles per work item when tiles are plentiful, else split vectors
     const long long tiles = (long long)numX * numY;
@@ -133,5 +146,24 @@ extern "C" int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G
         return noalloc_fail(FADESIM_E_CUDA, cudaGetErrorString(e));
     if ((e = launch_line_relax(a, ld, FADESIM_F32, (int)grid, st)) != cudaSuccess)
         return noalloc_fail(FADESIM_E_CUDA, cudaGetErrorString(e));
+    return FADESIM_OK;
+}
+
+extern "C" int fadesim_noalloc_last_status(fadesim_solve_stats *stats, void *stream) {
+    using namespace fadesim;
+    g_noalloc_err.clear();
+    if (!stats) return noalloc_fail(FADESIM_E_ARG, "fadesim_noalloc_last_status: stats must not be NULL");
+    *stats = fadesim_solve_stats{0, 0, 0, 0, 0};
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    DevStats h{};
+    cudaError_t e = cudaMemcpyFromSymbolAsync(&h, g_noalloc_scratch, sizeof(DevStats), 0, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess)
+        return noalloc_fail(FADESIM_E_CUDA, std::string("fadesim_noalloc_last_status: ") + cudaGetErrorString(e));
+    stats->solves = (int64_t)h.solves;
+    stats->iters_sum = (int64_t)h.iters_sum;
+    stats->iters_max = h.iters_max;
+    stats->status_or = h.status_or;
+    stats->warm_rejected = (int64_t)h.warm_rejected;
     return FADESIM_OK;
 }

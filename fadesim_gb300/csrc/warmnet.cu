@@ -5,7 +5,10 @@
 // Layouts: activations NHWC bf16, channels a multiple of 16 (zero padded);
 // weights [Cout][3][3][Cin] bf16 with Cout a multiple of 8; "same" zero
 // padding.  The convolution is an implicit GEMM, M = pixels, N = Cout,
-// K = 9 * Cin, issued as mma.sync.m16n8k16 (bf16 x bf16 -> f32).  The input
+// K = 9 * Cin.  Where the shape allows (the warm-start network's layers) it
+// runs on the tcgen05 / TMA kernel of warmnet_tc.cu; elsewhere, and on request
+// (flags 8), on the kernel here, issued as mma.sync.m16n8k16 (bf16 x bf16 ->
+// f32).  The input
 // gradient is the forward kernel run on dY with the weights transposed and
 // flipped (W'[ci][8 - tap][co] = W[co][tap][ci]); the weight gradient is a GEMM
 // over pixels split across CTAs and reduced with FP32 atomics.
@@ -308,6 +311,12 @@ int gridn(long long n) {
 extern "C" int fadesim_conv3x3_fwd_bf16(const void *X, const void *W, const float *bias, const void *skip, void *Y,
                                         int N, int H, int Wd, int Cin, int Cout, int flags, void *stream) {
     if (!X || !W || !Y || Cin % 16 || Cout % 8 || Cout > 128 || Cout < 8 || ((flags & 2) && !skip)) return FADESIM_E_ARG;
+    if (!(flags & 8) && fadesim::conv3x3_tc_supported(X, W, Y, H, Wd, Cin, Cout)) {
+        // the tensor-core (tcgen05 / TMA) kernel for the network's shapes
+        const cudaError_t e = fadesim::conv3x3_fwd_tc(X, W, bias, skip, Y, N, H, Wd, Cin, Cout, flags & 7,
+                                                      fadesim::conv_tc_error_flag(), (cudaStream_t)stream);
+        return e == cudaSuccess ? FADESIM_OK : FADESIM_E_CUDA;
+    }
     const long long P = (long long)N * H * Wd;
     const dim3 grid((unsigned)((P + CF_M - 1) / CF_M));
     const __nv_bfloat16 *x = (const __nv_bfloat16 *)X, *w = (const __nv_bfloat16 *)W, *sk = (const __nv_bfloat16 *)skip;

@@ -1,0 +1,374 @@
+// 3x3 convolution of the warm-start network on the 5th-generation tensor cores
+// (sm_103a): TMA tile loads, tcgen05.mma with the accumulator in tensor memory
+// (TMEM), BF16 operands, FP32 accumulation.
+//
+// Implicit GEMM, one CTA per 128-pixel output tile: M = 128 pixels (TMEM lanes),
+// N = Cout (TMEM columns), K = 9 taps x Cin in chunks of 32 channels.
+// * A (pixels x 32 channels of one tap): one 4-D TMA box (32 channels, W
+//   columns, 128 / W rows, 1 image) of the NHWC input at (c, dx, h0 + dy, n):
+//   the "same" padding comes from the TMA's zero fill of out-of-range
+//   coordinates (the channel coordinate, the only one with an alignment rule,
+//   is always a multiple of 32).  Rows of 64 bytes, 64-byte swizzle: the
+//   K-major operand layout of the MMA, 8-row groups 512 bytes apart.
+// * B (Cout x 32 channels of one tap): a 2-D TMA box of the weights viewed as
+//   [Cout][9 Cin], same layout.
+// * A six-stage ring of (A, B) buffers with full / empty mbarriers: thread 0
+//   (warp 0) issues the TMA loads, thread 32 (warp 1) the MMAs -- two
+//   K = 16 instructions per stage, the second with the descriptors advanced
+//   by 32 bytes -- and releases each stage with tcgen05.commit.
+// * Epilogue: the four warps read their 32 TMEM lanes (tcgen05.ld 32x32b, 16
+//   columns at a time), add the bias, apply ReLU and the skip connection, and
+//   store BF16 (or FP32) NHWC rows.
+// Every mbarrier wait is bounded (about a second of clock64); on expiry the
+// kernel records an error code, stops issuing, and still frees its TMEM.
+//
+// Shapes: Cin a multiple of 32, Cout a multiple of 16 up to 128, W a power of
+// two up to 128, H x W a multiple of 128 (the warm-start network's levels,
+// 128 x 128 down to 16 x 16).  Other shapes use the mma.sync kernel in
+// warmnet.cu.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "kernels.h"
+
+namespace fadesim {
+
+namespace {
+
+constexpr int TC_M = 128;          // pixels per tile = TMEM lanes
+constexpr int TC_KC = 32;          // channels per K chunk (64-byte rows)
+constexpr int TC_STAGES = 6;
+constexpr int TC_A_BYTES = TC_M * TC_KC * 2;   // 8 KB
+constexpr int TC_B_BYTES = 128 * TC_KC * 2;    // 8 KB (Cout <= 128)
+constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /* alignment */ + 256 /* barriers */;
+constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Wait until the barrier's phase with the given parity has completed, for at
+// most TC_WAIT_CYCLES; false on expiry.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (true) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory operand descriptor of a K-major tile with 64-byte rows and the
+// 64-byte swizzle: start address, stride between 8-row groups (512 B), the
+// descriptor version of this architecture, layout type 4 (64-byte swizzle).
+// The leading-dimension offset is unused for a swizzled K-major operand whose
+// K extent is one swizzle row.
+__device__ __forceinline__ uint64_t desc_sw64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(512 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)4 << 61;
+    return d;
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N and M.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(128, 1)
+    conv3x3_fwd_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW,
+                          const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ skip, void *__restrict__ Y,
+                          int H, int W, int Cin, int Cout, int flags, int *err) {
+    extern __shared__ unsigned char tc_smem_raw[];
+    // stage buffers 1024-byte aligned in the shared window (the swizzle pattern
+    // is a function of the shared-memory address)
+    unsigned char *base = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + TC_STAGES * TC_STAGE_BYTES);
+    uint64_t *empty = full + TC_STAGES;
+    uint64_t *done = empty + TC_STAGES;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const long long p0 = (long long)blockIdx.x * TC_M;  // first output pixel
+    const long long HW = (long long)H * W;
+    const int n = (int)(p0 / HW);
+    const int h0 = (int)((p0 % HW) / W);
+    const int kchunks = Cin / TC_KC, kiters = 9 * kchunks;
+    const uint32_t ncols = Cout <= 32 ? 32 : (Cout <= 64 ? 64 : 128);
+
+    if (tid == 0) {
+        s_fail = 0;
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(ncols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (tid == 0) {
+        // producer: TMA loads of A and B for every K step
+        const uint32_t tx = (uint32_t)(TC_A_BYTES + Cout * TC_KC * 2);
+        for (int it = 0; it < kiters; ++it) {
+            const int s = it % TC_STAGES;
+            const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
+            if (!mbar_wait(&empty[s], ph ^ 1u)) {
+                atomicExch(&s_fail, 1);
+                break;
+            }
+            const int tap = it / kchunks, c0 = (it % kchunks) * TC_KC;
+            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            unsigned char *sa = base + s * TC_STAGE_BYTES;
+            mbar_expect_tx(&full[s], tx);
+            tma_load_4d(sa, &tmX, c0, dx, h0 + dy, n, &full[s]);
+            tma_load_2d(sa + TC_A_BYTES, &tmW, tap * Cin + c0, 0, &full[s]);
+        }
+    } else if (tid == 32) {
+        // MMA issuer: two K = 16 steps per stage into the TMEM accumulator
+        const uint32_t idesc = idesc_bf16(TC_M, Cout);
+        bool ok = true;
+        for (int it = 0; it < kiters; ++it) {
+            const int s = it % TC_STAGES;
+            const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
+            if (!mbar_wait(&full[s], ph)) {
+                atomicExch(&s_fail, 2);
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_u32(base + s * TC_STAGE_BYTES);
+            const uint32_t sb = sa + TC_A_BYTES;
+#pragma unroll
+            for (int k = 0; k < TC_KC / 16; ++k)
+                umma_bf16(tmem, desc_sw64(sa + 32 * k), desc_sw64(sb + 32 * k), idesc, (it | k) ? 1u : 0u);
+            umma_commit(&empty[s]);  // the stage is free once these MMAs have read it
+        }
+        if (ok) umma_commit(done);  // the accumulator is final once every MMA has completed
+    }
+    __syncwarp();
+    // epilogue: warp w owns TMEM lanes 32w .. 32w + 31 (pixels p0 + 32w + lane)
+    const bool ready = __all_sync(0xffffffffu, mbar_wait(done, 0));
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ready && lane == 0) atomicExch(&s_fail, 3);
+    if (ready) {
+        const long long p = p0 + warp * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int j0 = 0; j0 < Cout; j0 += 16) {
+            float v[16];
+            tmem_ld16(lane_base + (uint32_t)j0, v);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                float t = v[i] + (bias ? bias[j0 + i] : 0.f);
+                if (flags & 1) t = fmaxf(t, 0.f);
+                v[i] = t;
+            }
+            if (flags & 2) {
+                const uint4 *sk = reinterpret_cast<const uint4 *>(skip + p * Cout + j0);
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const uint4 w4 = sk[q];
+                    const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&w4);
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const float2 f = __bfloat1622float2(h2[e]);
+                        v[q * 8 + 2 * e] += f.x;
+                        v[q * 8 + 2 * e + 1] += f.y;
+                    }
+                }
+            }
+            if (flags & 4) {
+                float4 *o = reinterpret_cast<float4 *>(reinterpret_cast<float *>(Y) + p * Cout + j0);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+            } else {
+                uint4 pk[2];
+                __nv_bfloat162 *h2 = reinterpret_cast<__nv_bfloat162 *>(pk);
+#pragma unroll
+                for (int e = 0; e < 8; ++e) h2[e] = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
+                uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(Y) + p * Cout + j0);
+                o[0] = pk[0];
+                o[1] = pk[1];
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+    }
+    if (tid == 0 && s_fail && err) atomicExch(err, s_fail);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+// Set by a tensor-core convolution whose bounded wait expired (1: a stage never
+// freed, 2: a stage never filled, 3: the accumulator never completed).
+__device__ int g_conv_tc_err;
+
+}  // namespace
+
+int *conv_tc_error_flag() {
+    static int *addr[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+    if (!addr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_conv_tc_err) != cudaSuccess) return nullptr;
+        addr[dev] = static_cast<int *>(p);
+    }
+    return addr[dev];
+}
+
+bool conv3x3_tc_supported(const void *X, const void *Wt, const void *Y, int H, int W, int Cin, int Cout) {
+    if (Cin < TC_KC || Cin % TC_KC || Cout < 16 || Cout > 128 || Cout % 16) return false;
+    if (W < 1 || W > TC_M || (TC_M % W) || ((long long)H * W) % TC_M) return false;
+    if ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(Wt) | reinterpret_cast<uintptr_t>(Y)) & 15)
+        return false;
+    return encode_fn() != nullptr;
+}
+
+// The tensor-core forward convolution; assumes conv3x3_tc_supported.  err: a
+// device int the kernel sets when one of its waits expires (may be null).
+cudaError_t conv3x3_fwd_tc(const void *X, const void *Wt, const float *bias, const void *skip, void *Y, int N, int H,
+                           int W, int Cin, int Cout, int flags, int *err, cudaStream_t st) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    CUtensorMap mx, mw;
+    const cuuint64_t xdim[4] = {(cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+    const cuuint64_t xstr[3] = {(cuuint64_t)Cin * 2, (cuuint64_t)W * Cin * 2, (cuuint64_t)H * W * Cin * 2};
+    const cuuint32_t xbox[4] = {(cuuint32_t)TC_KC, (cuuint32_t)W, (cuuint32_t)(TC_M / W), 1};
+    const cuuint32_t ones[4] = {1, 1, 1, 1};
+    if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(X), xdim, xstr, xbox, ones,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const cuuint64_t wdim[2] = {(cuuint64_t)9 * Cin, (cuuint64_t)Cout};
+    const cuuint64_t wstr[1] = {(cuuint64_t)9 * Cin * 2};
+    const cuuint32_t wbox[2] = {(cuuint32_t)TC_KC, (cuuint32_t)Cout};
+    if (enc(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(Wt), wdim, wstr, wbox, ones,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+    if (e != cudaSuccess) return e;
+    const long long tiles = (long long)N * H * W / TC_M;
+    if (tiles < 1) return cudaSuccess;
+    conv3x3_fwd_tc_kernel<<<(unsigned)tiles, 128, TC_SMEM, st>>>(mx, mw, bias,
+                                                                 static_cast<const __nv_bfloat16 *>(skip), Y, H, W,
+                                                                 Cin, Cout, flags, err);
+    return cudaGetLastError();
+}
+
+}  // namespace fadesim
+
+extern "C" int fadesim_conv_tc_status(void *stream) {
+    int h = 0;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (cudaMemcpyFromSymbolAsync(&h, fadesim::g_conv_tc_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return FADESIM_E_CUDA;
+    if (h) {
+        const int zero = 0;
+        cudaMemcpyToSymbolAsync(fadesim::g_conv_tc_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st);
+        cudaStreamSynchronize(st);
+    }
+    return h;
+}

@@ -14,7 +14,9 @@ of ``libfadesim_gb300.so`` and are bit-exact with the reference's float32
 arithmetic given the same currents; the currents come from the IR-drop solve
 (``cpp_ir_drop_accelerate.ir_drop_gs`` unless a ``solver`` is passed).  The
 solves of one (weight slice, array) pair cover all input-bit cycles at once:
-the input bits are stacked on the batch.
+the input bits are stacked on the batch -- unless the cells vary from cycle to
+cycle (``sigma != 0``), when every (input bit, slice, array) solve gets its own
+draw of the variation, in the reference's order and from its generator.
 
 Array and device parameters come from an object with ``phyArrParams``'s
 attribute names, so the reference's own ``commonConst.phyArrParams`` can be
@@ -28,6 +30,7 @@ import torch
 
 from . import _lib
 from . import cpp_ir_drop_accelerate as _acc
+from . import variation as _variation
 
 
 @dataclass
@@ -92,15 +95,19 @@ def quantize(x, bit_width, pn):
 
 def default_solver(cfg, tol_v=None):
     """The IR-drop solve of the drop-in module with the array's parameters
-    (tol_v None: the module-wide option)."""
+    (tol_v None: the module-wide option); the solves' status is checked per
+    the module's ``options.check_status``, as ``ir_drop_gs`` does."""
     def solve(v, G, B, rows, cols, numX, numY, out):
-        return _acc.ir_drop_gs_ex(v, G, B, rows, cols, numX, numY, iter_times=cfg.ir_drop_iter_time,
-                                  g_wire=1 / cfg.r_wire, beta=cfg.ir_drop_GS_method_beta_scale,
-                                  enable_break=cfg.ir_drop_less_than_thresholdBreak_enable,
-                                  break_threshould=cfg.ir_drop_less_than_threshold,
-                                  nonlinear_cell_enable=cfg.nonlinear_cell_enable,
-                                  nonlinear_params=cfg.nonlinear_params, tol_v=tol_v, return_stats=False,
-                                  out=out)[0]
+        policy = _acc.options.check_status
+        r, st, _ = _acc.ir_drop_gs_ex(v, G, B, rows, cols, numX, numY, iter_times=cfg.ir_drop_iter_time,
+                                      g_wire=1 / cfg.r_wire, beta=cfg.ir_drop_GS_method_beta_scale,
+                                      enable_break=cfg.ir_drop_less_than_thresholdBreak_enable,
+                                      break_threshould=cfg.ir_drop_less_than_threshold,
+                                      nonlinear_cell_enable=cfg.nonlinear_cell_enable,
+                                      nonlinear_params=cfg.nonlinear_params, tol_v=tol_v,
+                                      return_stats=policy != "off", out=out)
+        _acc.check_solve_status(st, _acc.resolved_method(_acc.options.method, rows, cols), policy)
+        return r
     return solve
 
 
@@ -158,17 +165,24 @@ def _check_modes(arr, in_mode, dacBits, cfg):
         raise Exception("[Error] Complement code input mode, but dac is not 1 bit. dacbits = {}".format(dacBits))
     if getattr(cfg, "useOUSize", False) or getattr(cfg, "useBNN", False):
         raise NotImplementedError("OU and BNN modes are not implemented")
-    if getattr(cfg, "sigma", 0) != 0:
-        raise NotImplementedError("conductance variation: use fadesim_gb300.variation on the maps")
 
 
 def _split_matmul_core(xq, geom, M, insize, has_ones, ones_q, s1, w, inputBits, dacBits, adcBits, weightBits, arr,
-                       neg_pulse, cfg, solver, bias=None, L=0):
+                       neg_pulse, cfg, solver, bias=None, L=0, rand_gen=None):
     """The bit-serial, bit-sliced product of splitArr_matmul_nn from quantised
     inputs: xq is an int32 NCHW image (geom = N, C, H, W, kh, kw, sh, sw, ph,
     pw, dh, dw; a linear layer is the 1x1 case) whose unfold has M rows and
     insize columns (plus a ones column if has_ones); w [insize(+1), outsize]
-    float weights.  Returns float32 [M, outsize], or [M/L, outsize, L] if L."""
+    float weights.  Returns float32 [M, outsize], or [M/L, outsize, L] if L.
+
+    With ``cfg.sigma != 0`` every solve gets its own conductance variation, as
+    in the reference's ``matmul`` (splitArrayArithmetic.py:758-760 PN, :788
+    Ref): one draw of exp(sigma N(0,1)) per cell of the padded map for every
+    (input bit, weight slice, array) call, in the reference's loop order --
+    input bit outer, slice inner, the positive array before the negative one
+    (:1197-1217, :1247-1251) -- from ``rand_gen`` (default
+    ``variation.variations.rand_gen_network``).  The input bits then cannot
+    share one solve per map, so each bit's vectors are solved on their own."""
     lib = _lib.load()
     if weightBits % cfg.cellBits != 0:
         raise Exception("[Error] cellbit is not factor of weight_bit")
@@ -193,20 +207,43 @@ def _split_matmul_core(xq, geom, M, insize, has_ones, ones_q, s1, w, inputBits, 
     I = torch.empty((nslices, narr, nbits * M, numX, numY * cb), dtype=torch.float32, device=dev)
     G = torch.empty((numX, rows, numY * cb), dtype=torch.float32, device=dev)
     plus = 2 ** (weightBits - 1)
-    for j in range(nslices):
-        for a in range(narr):
-            if ref:
-                _lib.check(lib.fadesim_map_conductance_ref_f32(wq.data_ptr(), K, outsize, rows, cols, numX, numY,
-                                                               j * cfg.cellBits, cfg.cellBits, plus,
-                                                               2 ** weightBits - 1, cfg.cellDeltaConduct,
-                                                               cfg.cellMinConduct, G.data_ptr(), st))
-            else:
-                _lib.check(lib.fadesim_map_conductance_f32(wq.data_ptr(), K, outsize, rows, cols, numX, numY,
-                                                           j * cfg.cellBits, cfg.cellBits, a, cfg.cellDeltaConduct,
+
+    def map_slice(j, a, G):
+        if ref:
+            _lib.check(lib.fadesim_map_conductance_ref_f32(wq.data_ptr(), K, outsize, rows, cols, numX, numY,
+                                                           j * cfg.cellBits, cfg.cellBits, plus,
+                                                           2 ** weightBits - 1, cfg.cellDeltaConduct,
                                                            cfg.cellMinConduct, G.data_ptr(), st))
-            r = solver(v, G, nbits * M, rows, cb, numX, numY, I[j, a])
-            if r is not None and r.data_ptr() != I[j, a].data_ptr():
-                I[j, a].copy_(r.reshape(I[j, a].shape))
+        else:
+            _lib.check(lib.fadesim_map_conductance_f32(wq.data_ptr(), K, outsize, rows, cols, numX, numY,
+                                                       j * cfg.cellBits, cfg.cellBits, a, cfg.cellDeltaConduct,
+                                                       cfg.cellMinConduct, G.data_ptr(), st))
+
+    def solve_into(vv, GG, nb, dst):
+        r = solver(vv, GG, nb, rows, cb, numX, numY, dst)
+        if r is not None and r.data_ptr() != dst.data_ptr():
+            dst.copy_(r.reshape(dst.shape))
+
+    sigma = float(getattr(cfg, "sigma", 0) or 0)
+    if sigma == 0:
+        for j in range(nslices):
+            for a in range(narr):
+                map_slice(j, a, G)
+                solve_into(v, G, nbits * M, I[j, a])
+    else:
+        gen = rand_gen if rand_gen is not None else _variation.variations.rand_gen_network
+        maps = torch.empty((nslices, narr) + tuple(G.shape), dtype=torch.float32, device=dev)
+        for j in range(nslices):
+            for a in range(narr):
+                map_slice(j, a, maps[j, a])
+        div = torch.empty(G.shape, dtype=torch.float32, device=dev)
+        for i in range(nbits):
+            for j in range(nslices):
+                for a in range(narr):
+                    div.copy_(_variation.variation_divisor(tuple(G.shape), sigma, gen))
+                    _lib.check(lib.fadesim_vary_conductance_f32(maps[j, a].data_ptr(), div.data_ptr(), G.numel(),
+                                                                0.0, 0, 0, G.data_ptr(), st))
+                    solve_into(v[i * M:(i + 1) * M], G, M, I[j, a, i * M:(i + 1) * M])
     shape = (M // L, outsize, L) if L else (M, outsize)
     out = torch.empty(shape, dtype=torch.float32, device=dev)
     scale = rows * (2 ** dacBits - 1) * (2 ** cfg.cellBits - 1) / (2 ** adcBits - 1)
@@ -222,12 +259,14 @@ def _split_matmul_core(xq, geom, M, insize, has_ones, ones_q, s1, w, inputBits, 
 
 
 def splitArr_matmul_nn(input, w, inputBits, dacBits, adcBits, outputBits, weightBits, arrType="PN",
-                       float_type=torch.float32, cfg=None, solver=None):
+                       float_type=torch.float32, cfg=None, solver=None, rand_gen=None):
     """Same arguments as the reference; ``arrType`` is "PN" / "Ref" or an enum
     with that name; ``cfg`` is a phyArrParams-like object (default
     ``ArrayConfig()``; its ``inputVmode`` selects complement-code or
-    negative-pulse inputs); ``solver(v, G, B, rows, cols, numX, numY, out)`` may
-    replace the IR-drop solve."""
+    negative-pulse inputs, its ``sigma`` the conductance variation);
+    ``solver(v, G, B, rows, cols, numX, numY, out)`` may replace the IR-drop
+    solve; ``rand_gen`` is the variation's generator (default
+    ``variation.variations.rand_gen_network``, the reference's)."""
     cfg = cfg if cfg is not None else ArrayConfig()
     arr = _mode_name(arrType, "PN")
     in_mode = _mode_name(getattr(cfg, "inputVmode", None), "complement_code")
@@ -241,7 +280,7 @@ def splitArr_matmul_nn(input, w, inputBits, dacBits, adcBits, outputBits, weight
         xq, s1 = quantize(x, inputBits, pn=False)
         geom = (B, insize, 1, 1, 1, 1, 1, 1, 0, 0, 1, 1)
         return _split_matmul_core(xq, geom, B, insize, False, 0, s1, w, inputBits, dacBits, adcBits, weightBits, arr,
-                                  in_mode == "neg_pulse", cfg, solver)
+                                  in_mode == "neg_pulse", cfg, solver, rand_gen=rand_gen)
 
 
 def _covered(n, k, s, p, d, on):
@@ -257,7 +296,7 @@ def _covered(n, k, s, p, d, on):
 
 
 def conv2d_split(input, weight, bias, stride=1, padding=0, dilation=1, inputBits=8, dacBits=1, adcBits=10,
-                 outputBits=10, weightBits=8, arrType="PN", use_fp_bias=True, cfg=None, solver=None):
+                 outputBits=10, weightBits=8, arrType="PN", use_fp_bias=True, cfg=None, solver=None, rand_gen=None):
     """Conv2d_sp's evaluation (fixedPoint/nn/modules/conv_split.py:89-136):
     unfold, splitArr_matmul_nn against the weights reshaped [Cout, C*kh*kw] and
     transposed, float32 bias (or a bias row in the array driven by ones when
@@ -300,7 +339,7 @@ def conv2d_split(input, weight, bias, stride=1, padding=0, dilation=1, inputBits
         L = OH * OW
         out = _split_matmul_core(xq, geom, N * L, C * kh * kw, ones, ones_q, s1, wm.contiguous(), inputBits, dacBits,
                                  adcBits, weightBits, arr, in_mode == "neg_pulse", cfg, solver,
-                                 bias=bias if (bias is not None and use_fp_bias) else None, L=L)
+                                 bias=bias if (bias is not None and use_fp_bias) else None, L=L, rand_gen=rand_gen)
         return out.reshape(N, Cout, OH, OW)
 
 

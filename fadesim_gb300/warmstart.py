@@ -5,19 +5,22 @@ and its wordline voltages to predicted node-voltage deviations from the ideal
 state (wordline u - vin, bitline d); the line solver starts from that
 prediction and iterates to the same tolerance as from zero, and rejects the
 prediction when its first correction is as large as the solution.  Every
-layer runs in the project's CUDA kernels (``csrc/warmnet.cu``: tensor-core
-implicit-GEMM 3x3 convolutions, input and weight gradients, pooling,
-upsampling, ReLU, MSE, Adam); torch tensors only hold the buffers.
+layer runs in the project's CUDA kernels (``csrc/warmnet_tc.cu``: 3x3
+convolutions and their input gradients as implicit GEMMs on the tcgen05
+tensor cores, fed by TMA, accumulating in tensor memory; ``csrc/warmnet.cu``:
+weight gradients, the convolutions of levels too small for the 128-pixel
+tile, pooling, upsampling, ReLU, MSE, Adam); torch tensors only hold the
+buffers.
 
 Architecture (NHWC, "same" 3x3 convolutions, 4 levels):
-  e1 = relu(conv(x, 16->32))            @ S      (x: 2 used input channels, 14 zero)
+  e1 = relu(conv(x, 32->32))            @ S      (x: 2 used input channels, 30 zero)
   e2 = relu(conv(pool(e1), 32->64))     @ S/2
   e3 = relu(conv(pool(e2), 64->96))     @ S/4
   e4 = relu(conv(pool(e3), 96->128))    @ S/8
   d3 = relu(conv(up(e4), 128->96)) + e3 @ S/4
   d2 = relu(conv(up(d3), 96->64)) + e2  @ S/2
   d1 = relu(conv(up(d2), 64->32)) + e1  @ S
-  y  = conv(d1, 32->16)                 @ S      (2 output channels used, FP32)
+  y  = conv(d1, 32->32)                 @ S      (2 output channels used, FP32)
 Inputs: channel 0 = G / max(G) of the tile, channel 1 = vin_i / max(vin) on row
 i.  Targets: deviations / (0.05 max(vin)).
 """
@@ -29,8 +32,8 @@ import torch
 from . import _lib
 
 CH = [32, 64, 96, 128]
-CIN = 16   # padded input channels
-COUT = 16  # padded output channels (2 used)
+CIN = 32   # padded input channels (2 used): every layer's Cin a multiple of 32, for the tensor-core kernel
+COUT = 32  # padded output channels (2 used)
 TARGET_SCALE = 0.05
 
 _SIGS = {
@@ -43,6 +46,7 @@ _SIGS = {
     "fadesim_add_bf16": "vvvlv",
     "fadesim_mse_f32": "pppvliiv",
     "fadesim_adam_f32": "pvppplffffiv",
+    "fadesim_conv_tc_status": "v",
 }
 
 
@@ -96,10 +100,11 @@ class Conv:
         self.mb, self.vb = torch.zeros_like(self.b), torch.zeros_like(self.b)
         self.flip = torch.empty((cin, 3, 3, cout), dtype=torch.bfloat16, device=device)
 
-    def fwd(self, x, relu, skip=None, f32=False):
+    def fwd(self, x, relu, skip=None, f32=False, legacy=False):
+        """legacy: run the mma.sync kernel even where the tensor-core kernel applies."""
         N, H, W, _ = x.shape
         y = torch.empty((N, H, W, self.cout), dtype=torch.float32 if f32 else torch.bfloat16, device=x.device)
-        flags = (1 if relu else 0) | (2 if skip is not None else 0) | (4 if f32 else 0)
+        flags = (1 if relu else 0) | (2 if skip is not None else 0) | (4 if f32 else 0) | (8 if legacy else 0)
         _chk(_k().fadesim_conv3x3_fwd_bf16(_p(x), _p(self.wb), _p(self.b), _p(skip), _p(y), N, H, W, self.cin,
                                            self.cout, flags, _st()), "conv fwd")
         return y
@@ -186,7 +191,7 @@ class WarmStartNet:
     # ---- data ----------------------------------------------------------------
     @staticmethod
     def make_inputs(G, vin):
-        """G [N, n, m] (any float), vin [N, n] -> bf16 NHWC input [N, n, m, 16] and the
+        """G [N, n, m] (any float), vin [N, n] -> bf16 NHWC input [N, n, m, CIN] and the
         per-instance target scale [N]."""
         N, n, m = G.shape
         x = torch.zeros((N, n, m, CIN), dtype=torch.float32, device=G.device)
@@ -223,7 +228,7 @@ class WarmStartNet:
         return y
 
     def backward(self, dy):
-        """dy: bf16 gradient at the output [N, S, S, 16]; accumulates parameter gradients."""
+        """dy: bf16 gradient at the output [N, S, S, COUT]; accumulates parameter gradients."""
         c, L = self.cache, self.layers
         dd1 = L["out"].bwd(dy, c["d1"])
         du1 = L["d1"].bwd(_relu_bwd(dd1, c["a1"]), c["u1"])

@@ -7,7 +7,8 @@ own throughput, and for both solvers the iterations (line) or sweeps (red-black
 SOR) from the ideal state and from the prediction, the fallback (rejection) rate
 and the end-to-end solves/s including inference.
 
-  python -m fadesim_gb300.warmstart_eval [--size 128] [--steps 600] [--infer 8192]
+  python -m fadesim_gb300.warmstart_eval [--size 128] [--train 200000] [--infer 8192] [--cells weak|strong]
+  python -m fadesim_gb300.warmstart_eval --conv      (one convolution on both kernels, TFLOP/s)
 """
 import argparse
 import json
@@ -19,6 +20,8 @@ from . import cpp_ir_drop_accelerate as acc
 from . import warmstart as ws
 
 R_STATES = (2e6, 1.6e6, 1.3e6, 1e6)
+# 2-bit cells between 1 kohm and 1 Mohm, linear in conductance (the MLP layers' arrays)
+G_STRONG = tuple(1e-6 + k * (1e-3 - 1e-6) / 3 for k in range(4))
 
 
 def _timed(fn):
@@ -31,14 +34,21 @@ def _timed(fn):
     return r, e0.elapsed_time(e1) / 1e3
 
 
-def train_and_evaluate(size=128, steps=600, batch=32, infer=8192, lr=1e-3, g_wire=1 / 2.93, seed=0,
-                       sor_omegas=(1.90, 1.96), sor_sample=256):
+def train_and_evaluate(size=128, train_instances=200000, batch=64, infer=8192, lr=1e-3, g_wire=1 / 2.93, seed=0,
+                       cells="weak", sor_omegas=(1.96, 1.98), sor_sample=304):
+    """Train on ``train_instances`` solver-generated tiles of the given cells
+    ("weak": four states 1-2 Mohm; "strong": 2-bit 1 kohm - 1 Mohm) with
+    Bernoulli 0.2 V inputs, then on a fresh batch of ``infer`` tiles report the
+    prediction error, the network's throughput, and for the line solver and the
+    plain red-black SOR the iterations / sweeps from the ideal state and from
+    the prediction, the fallback rate (predictions the line solver discarded)
+    and solves/s with and without the warm start, inference included."""
     n = size
-    Rs = torch.tensor(R_STATES)
+    gvals = torch.tensor(G_STRONG if cells == "strong" else [1.0 / r for r in R_STATES])
     gen = torch.Generator().manual_seed(seed)
 
     def draw(N):
-        G = (1.0 / Rs[torch.randint(0, len(R_STATES), (N, n, n), generator=gen)]).float().cuda()
+        G = gvals[torch.randint(0, len(gvals), (N, n, n), generator=gen)].float().cuda()
         vin = (torch.randint(0, 2, (N, n), generator=gen).float() * 0.2).cuda()
         return G, vin
 
@@ -51,6 +61,7 @@ def train_and_evaluate(size=128, steps=600, batch=32, infer=8192, lr=1e-3, g_wir
         return p
 
     net = ws.WarmStartNet(seed=seed)
+    steps = max(1, train_instances // batch)
     t0 = time.perf_counter()
     losses = []
     for _ in range(steps):
@@ -60,6 +71,7 @@ def train_and_evaluate(size=128, steps=600, batch=32, infer=8192, lr=1e-3, g_wir
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     G, vin = draw(infer)
+    net.predict_planes(G[:batch], vin[:batch])  # warm-up
     pred, t_inf = _timed(lambda: net.predict_planes(G, vin))
     true = solve_planes(G, vin)
     rel = float((pred - true).norm() / true.norm())
@@ -67,15 +79,17 @@ def train_and_evaluate(size=128, steps=600, batch=32, infer=8192, lr=1e-3, g_wir
     init = pred[None, :, None].contiguous()
     (_, cold, _), t_cold = _timed(lambda: acc.ir_drop_gs_ex(ti, G, 1, n, n, infer, 1, g_wire=g_wire, method="line"))
     (_, warm, _), t_warm = _timed(lambda: acc.ir_drop_gs_warm(ti, G, 1, n, n, infer, 1, init, g_wire=g_wire))
-    rejected = int(warm["status_or"] & 8)
+    line = {"iters_mean_cold": cold["iters_sum"] / cold["solves"], "iters_mean_warm": warm["iters_sum"] / warm["solves"],
+            "iters_saved_frac": 1 - warm["iters_sum"] / cold["iters_sum"],
+            "fallback_rate": warm["warm_rejected"] / warm["solves"],
+            "solves_per_s_cold": infer / t_cold, "solves_per_s_warm_excl_inference": infer / t_warm,
+            "solves_per_s_warm_incl_inference": infer / (t_warm + t_inf)}
+    line["net_gain_incl_inference"] = line["solves_per_s_warm_incl_inference"] / line["solves_per_s_cold"]
     out = {
-        "tile": "%dx%d" % (n, n), "train_instances": steps * batch, "train_s": train_s,
+        "tile": "%dx%d" % (n, n), "cells": cells, "train_instances": steps * batch, "train_s": train_s,
         "loss_first": float(losses[0]), "loss_last": float(losses[-1]),
         "infer_batch": infer, "infer_instances_per_s": infer / t_inf, "prediction_rel_err": rel,
-        "line": {"iters_mean_cold": cold["iters_sum"] / cold["solves"], "iters_mean_warm": warm["iters_sum"] / warm["solves"],
-                 "solves_per_s_cold": infer / t_cold, "solves_per_s_warm_incl_inference": infer / (t_warm + t_inf),
-                 "any_rejected": bool(rejected)},
-        "rbsor": {},
+        "line": line, "rbsor": {},
     }
     k = min(sor_sample, infer)
     tis = vin[None, :k].contiguous()
@@ -86,21 +100,53 @@ def train_and_evaluate(size=128, steps=600, batch=32, infer=8192, lr=1e-3, g_wir
                                                          omega=w))
         (_, wm, _), tw = _timed(lambda: acc.ir_drop_gs_warm(tis, Gs, 1, n, n, k, 1, inits, g_wire=g_wire,
                                                             method="rbsor", omega=w))
-        out["rbsor"]["omega_%.2f" % w] = {
-            "sweeps_mean_cold": c["iters_sum"] / c["solves"], "sweeps_mean_warm": wm["iters_sum"] / wm["solves"],
-            "sweeps_saved_frac": 1 - wm["iters_sum"] / c["iters_sum"], "solves_per_s_cold": k / tc,
-            "solves_per_s_warm_incl_inference": k / (tw + t_inf * k / infer)}
+        r = {"sweeps_mean_cold": c["iters_sum"] / c["solves"], "sweeps_mean_warm": wm["iters_sum"] / wm["solves"],
+             "sweeps_saved_frac": 1 - wm["iters_sum"] / c["iters_sum"], "solves_per_s_cold": k / tc,
+             "solves_per_s_warm_incl_inference": k / (tw + t_inf * k / infer)}
+        r["net_gain_incl_inference"] = r["solves_per_s_warm_incl_inference"] / r["solves_per_s_cold"]
+        out["rbsor"]["omega_%.2f" % w] = r
     return out
+
+
+def conv_throughput(N=64, H=128, W=128, cin=64, cout=32, reps=10, legacy=False):
+    """Time one 3x3 convolution of the network (default: the d1 layer, 64 -> 32
+    channels at 128 x 128, batch 64) on the tensor-core kernel (tcgen05 / TMA)
+    or, with ``legacy``, the mma.sync kernel.  Returns ms per launch and
+    TFLOP/s (2 * 9 * Cin * Cout flops per output pixel)."""
+    g = torch.Generator().manual_seed(1)
+    x = torch.randn((N, H, W, cin), generator=g).to(torch.bfloat16).cuda()
+    conv = ws.Conv(cin, cout, g, "cuda")
+    for _ in range(2):
+        conv.fwd(x, relu=True, legacy=legacy)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        conv.fwd(x, relu=True, legacy=legacy)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    flops = 2.0 * 9 * cin * cout * N * H * W
+    return {"kernel": "mma.sync" if legacy else "tcgen05+TMA", "shape": "N%d %dx%d %d->%d" % (N, H, W, cin, cout),
+            "ms": ms, "tflops": flops / (ms / 1e3) / 1e12}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--size", type=int, default=128)
-    ap.add_argument("--steps", type=int, default=600)
-    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--train", type=int, default=200000, help="training instances")
+    ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--infer", type=int, default=8192)
+    ap.add_argument("--cells", default="weak", choices=["weak", "strong"])
+    ap.add_argument("--conv", action="store_true",
+                    help="only time one network convolution on both kernels (for profiling)")
     a = ap.parse_args()
-    print(json.dumps(train_and_evaluate(a.size, a.steps, a.batch, a.infer)))
+    if a.conv:
+        from .build import build
+        build()
+        print(json.dumps([conv_throughput(), conv_throughput(legacy=True)]))
+        return
+    print(json.dumps(train_and_evaluate(a.size, a.train, a.batch, a.infer, cells=a.cells)))
 
 
 if __name__ == "__main__":

@@ -37,7 +37,8 @@ extern "C" {
 #define FADESIM_METHOD_AUTO 0      /* line relaxation up to 512 x 512, else the sweep order */
 #define FADESIM_METHOD_LINE 1      /* block line relaxation, residual form, to tolerance (<= 512 x 512;
                                       > 128 on 4- or 16-CTA clusters) */
-#define FADESIM_METHOD_RBSOR 2     /* plain red-black point SOR, residual form, to tolerance */
+#define FADESIM_METHOD_RBSOR 2     /* plain red-black point SOR, residual form, to tolerance (<= 512 x 512;
+                                      > 128 on 4- or 16-CTA clusters) */
 #define FADESIM_METHOD_SWEEPS 3    /* the reference's sweep order for exactly iter_times sweeps */
 
 /* per-solve status bits (fadesim_solve_stats.status_or, per_solve_status) */
@@ -61,6 +62,9 @@ typedef struct fadesim_solve_opts {
     double read_noise_sigma;        /* > 0: each cell current gets N(0, (sigma * I_cell)^2) in the returned
                                        bitline currents (line method); not a reference feature */
     unsigned long long noise_seed;  /* counter-based: same seed, same noise */
+    int kernel_ld;         /* kernel layout, 0 = by tile size; else the line (or red-black) kernel of that
+                              size: 32 / 64 / 128 one tile per CTA, 256 / 512 one tile per 4- / 16-CTA
+                              cluster (>= rows and cols; red-black SOR: 128, 256, 512) */
 } fadesim_solve_opts;
 
 typedef struct fadesim_solve_stats {
@@ -68,6 +72,7 @@ typedef struct fadesim_solve_stats {
     int64_t iters_sum;     /* sum over solves of iterations (line) or sweeps (rbsor, sweeps) */
     int iters_max;
     int status_or;         /* OR of per-solve status bits */
+    int64_t warm_rejected; /* solves whose warm start was discarded (FADESIM_ST_WARM_REJECTED) */
 } fadesim_solve_stats;
 
 /* Drop-in for the reference's ir_drop_gs (split_arr_matmul.cu:204-220, bound
@@ -125,33 +130,43 @@ int fadesim_release_memory(void);
 
 /* ---- the reference extension's other exports (split_arr_matmul.cu:1429-1437),
  * reproducing their iterates: same arguments and meaning, dtype (FADESIM_F32 /
- * FADESIM_F64) typing input, G and out; linear cells (nonlinear cells: ir_drop_gs).
- * ou_* functions split every rows x cols tile into ou_row_size x ou_col_size
- * operation units solved at once, each through the lumped wire outside it, and
- * return currents per OU row group [batch, numX * rows / ou_row_size, numY * cols];
- * the others return [batch, numX, numY * cols] (ir2s with ret_V: cell voltages
+ * FADESIM_F64) typing input, G and out.  nonlinear_cell_enable != 0 selects the
+ * reference's sinh cells, nonlinear_params = [R_on, R_off, a_on, b_on, a_off, b_off]
+ * (commonConst.py:207): before every iteration each solve's conductances are
+ * recomputed from u - d of the iterate before the newest, |V| < 1e-5 clamped to
+ * +-1e-5, as the reference's host loops do (:455-475, 603-622, 727-746, 996-1016,
+ * 1241-1260).  ou_* functions split every rows x cols tile into ou_row_size x
+ * ou_col_size operation units solved at once, each through the lumped wire
+ * outside it, and return currents per OU row group
+ * [batch, numX * rows / ou_row_size, numY * cols]; the others return
+ * [batch, numX, numY * cols] (ir2s with ret_V: cell voltages
  * [batch, numX, numY, rows, cols]). ---- */
 
 /* ir2s (split_arr_matmul.cu:419-545): IR-drop-to-source iteration, r_wire the wire and load resistance. */
 int fadesim_ir2s(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size, int numX,
-                 int numY, int iter_times, double r_wire, int enable_break, double break_threshould, int ret_V,
+                 int numY, int iter_times, double r_wire, int enable_break, double break_threshould,
+                 int nonlinear_cell_enable, const double *nonlinear_params, int n_nonlinear_params, int ret_V,
                  void *out, void *stream);
 /* ir2s_ou_local (:565-680): ir2s with source and ground load resistances. */
 int fadesim_ir2s_ou_local(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
                           int numX, int numY, int iter_times, double r_wire, double r_load_left, double r_load_down,
-                          int enable_break, double break_threshould, void *out, void *stream);
+                          int enable_break, double break_threshould, int nonlinear_cell_enable,
+                          const double *nonlinear_params, int n_nonlinear_params, void *out, void *stream);
 /* ir2s_ou (:953-1084): ir2s on every OU at once. */
 int fadesim_ir2s_ou(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
                     int ou_row_size, int ou_col_size, int numX, int numY, int iter_times, double r_wire,
-                    int enable_break, double break_threshould, void *out, void *stream);
+                    int enable_break, double break_threshould, int nonlinear_cell_enable,
+                    const double *nonlinear_params, int n_nonlinear_params, void *out, void *stream);
 /* ir_gs_ou_local (:690-813): the ir_drop_gs sweep with source and ground load conductances. */
 int fadesim_ir_gs_ou_local(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
                            int numX, int numY, int iter_times, double g_wire, double g_load_left, double g_load_down,
-                           double beta, int enable_break, double break_threshould, void *out, void *stream);
+                           double beta, int enable_break, double break_threshould, int nonlinear_cell_enable,
+                           const double *nonlinear_params, int n_nonlinear_params, void *out, void *stream);
 /* ir_gs_ou (:1197-1310): the sweep on every OU at once. */
 int fadesim_ir_gs_ou(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
                      int ou_row_size, int ou_col_size, int numX, int numY, int iter_times, double g_wire, double beta,
-                     int enable_break, double break_threshould, void *out, void *stream);
+                     int enable_break, double break_threshould, int nonlinear_cell_enable,
+                     const double *nonlinear_params, int n_nonlinear_params, void *out, void *stream);
 
 /* ---- integer stages around the solve (bit-exact with the reference's float32
  * arithmetic given the same currents).  Device pointers, async on stream. ---- */
@@ -211,22 +226,38 @@ int fadesim_adc_shift_add_ex_f32(const float *I, int ref_cols, int nbits, int ns
                                  int cell_bits, int input_bits, int complement, float plus, const float *bias, int L,
                                  float *out, void *stream);
 
+/* Cycle-to-cycle conductance variation of a map of n cells: out[k] = G[k] / divisor[k], one
+ * correctly rounded FP32 division, where divisor holds exp(sigma * N(0,1)) drawn by the caller (the
+ * reference draws them from its CPU generator, conductance_variation.py:6-13, and divides on the
+ * map's device); with divisor == NULL the divisor is exp(sigma * z_k), z_k a standard normal from a
+ * counter hash of (seed, offset + k), the same on every run and device (R becomes R * exp(sigma z),
+ * a lognormal spread, without a host round trip).  out may alias G.  sigma >= 0. */
+int fadesim_vary_conductance_f32(const float *G, const float *divisor, long long n, double sigma,
+                                 unsigned long long seed, unsigned long long offset, float *out, void *stream);
+
 /* Allocation-free variant of the line solve (FP32, bitline currents only).
  * No counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc -- code running inside someone else's stream capture, host
  * callbacks or real-time loops that forbid allocation, programs with a fixed
  * device-memory budget.  Inputs and outputs as fadesim_ir_drop_gs_f32 (method
- * FADESIM_METHOD_LINE, tol 1e-8 V).  Its scratch is one static device array of
- * fadesim_noalloc_scratch_bytes() bytes (24 MiB) that every GPU loading the
- * library holds until exit.  The first call on a device sets up that array's
- * address and should come before any stream capture.  All calls share the
- * array: calls that overlap on the GPU race.  Tiles larger than 128 x 128 are
- * rejected with FADESIM_E_ARG; fadesim_noalloc_last_error() gives the message.
- * It calls no cudaMalloc, cudaFree or allocating library routine. */
+ * FADESIM_METHOD_LINE, tol 1e-8 V, at most 400 line iterations).  Its scratch
+ * is one static device array of fadesim_noalloc_scratch_bytes() bytes (24 MiB)
+ * that every GPU loading the library holds until exit.  The first call on a
+ * device sets up that array's address and should come before any stream
+ * capture; the address is kept, so do not use this entry across a
+ * cudaDeviceReset.  All calls share the array: calls that overlap on the GPU
+ * race.  Tiles larger than 128 x 128 are rejected with FADESIM_E_ARG;
+ * fadesim_noalloc_last_error() gives the message.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine. */
 int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G, int batch_size, int row_size, int col_size,
                                    int numX, int numY, double g_wire, float *out, void *stream);
 size_t fadesim_noalloc_scratch_bytes(void);
 const char *fadesim_noalloc_last_error(void);
+/* The counters of the last fadesim_ir_drop_gs_noalloc_f32 call that finished on this device (solves,
+ * iterations, OR of the FADESIM_ST_* bits: FADESIM_ST_MAXITER or FADESIM_ST_NONFINITE mark a failed
+ * solve), copied from the static array to the HOST struct *stats after the copy, queued on `stream`
+ * behind that call, has completed (this synchronises `stream`).  Allocates nothing. */
+int fadesim_noalloc_last_status(fadesim_solve_stats *stats, void *stream);
 
 /* fadesim_ir_drop_gs_ex started from given node planes (a learned warm start): init is a DEVICE
  * FP32 array [batch, numX, numY, 2, rows, cols] of wordline deviations u - vin and bitline voltages
@@ -247,9 +278,16 @@ int fadesim_ir_drop_gs_warm(int dtype, const void *input, const void *G, int bat
  * multiple of 8 and at most 128; "same" zero padding. ---- */
 
 /* Y = act(conv3x3(X, W) + bias) (+ skip): flags 1 = ReLU, 2 = add skip after
- * the activation, 4 = store FP32 instead of bf16. */
+ * the activation, 4 = store FP32 instead of bf16, 8 = use the mma.sync kernel even where the
+ * tensor-core kernel applies.  The tensor-core kernel (TMA loads, tcgen05.mma into tensor memory)
+ * runs when Cin is a multiple of 32, Cout a multiple of 16, Wd a power of two up to 128, H * Wd a
+ * multiple of 128 and the buffers 16-byte aligned; other shapes run on mma.sync. */
 int fadesim_conv3x3_fwd_bf16(const void *X, const void *W, const float *bias, const void *skip, void *Y, int N,
                              int H, int Wd, int Cin, int Cout, int flags, void *stream);
+/* The tensor-core convolutions' error flag on the current device (0: none; 1-3: a bounded wait of
+ * a launch expired -- a stage never freed / filled, the accumulator never completed), read after
+ * the work queued on `stream` has finished, and cleared.  Negative: FADESIM_E_CUDA. */
+int fadesim_conv_tc_status(void *stream);
 /* dW[Cout][3][3][Cin] += sum over pixels of dY x X (FP32 accumulation with atomics: zero dW first). */
 int fadesim_conv3x3_wgrad_bf16(const void *dY, const void *X, float *dW, int N, int H, int Wd, int Cin, int Cout,
                                void *stream);
@@ -273,6 +311,14 @@ int fadesim_mse_f32(const float *pred, const float *target, void *dpred, float *
  * bf16 copy wb. */
 int fadesim_adam_f32(float *w, void *wb, const float *g, float *m, float *v, long long n, float lr, float b1,
                      float b2, float eps, int step, void *stream);
+
+/* ---- measurement helper (no reference counterpart) ---- */
+
+/* Shared-memory read bandwidth probe: `blocks` CTAs of 1024 threads each read iters (a multiple
+ * of 8) 16-byte shared-memory words per thread, conflict-free, and add one sum per CTA to
+ * sink[blockIdx] (DEVICE, blocks floats).  Bytes read = blocks * 1024 * iters * 16; timed by the
+ * caller, it gives the measured shared-memory peak the line kernels' roofline is quoted against. */
+int fadesim_smem_read_probe(float *sink, int blocks, int iters, void *stream);
 
 /* Message for the last failing call on this thread. */
 const char *fadesim_last_error(void);

@@ -25,7 +25,12 @@ PN and Ref-column arrays, complement-code and negative-pulse inputs, and the
   clamped to 2^b-1 (:1229-1242), two reference columns per column block (state 0
   and state 1, :758-771), the state-0 column's code subtracted from every
   column and, for slice 0, 2^(b-1) times the state-1 column's (:980-996);
-* Conv2d_sp: unfold, matmul, fold (fixedPoint/nn/modules/conv_split.py:106-134).
+* Conv2d_sp: unfold, matmul, fold (fixedPoint/nn/modules/conv_split.py:106-134);
+* cycle-to-cycle variation: every map divided by exp(sigma N(0,1)) per cell,
+  one draw per (input bit, slice, array) call in the reference's loop order
+  (conductance_variation.py:6-13, splitArrayArithmetic.py:758-760,788); the
+  draws come from a caller's function (the reference's are torch's CPU
+  generator, which this restatement does not re-derive).
 
 Every float step is float32 with the reference's operation order; scalar
 operands are rounded to float32 first, which is what torch does for a float32
@@ -84,10 +89,13 @@ def ideal_solver(in_v, G, B, rows, cols, numX, numY):
     return np.cumsum(in_v * G, axis=2)[:, :, -1, :].astype(f32)
 
 
-def slice_matmul(in_b, g_pos, g_neg, p, solver):
+def slice_matmul(in_b, g_pos, g_neg, p, solver, vary=None):
     """One input-bit x weight-slice product through two IR-drop solves.
 
     in_b [B, insize] in {0,1}; g_pos/g_neg [insize, outsize] cell states.
+    vary(shape), if given, returns the float32 divisors exp(sigma N(0,1)) of a
+    cycle-to-cycle variation draw; it is called for the positive map, then the
+    negative one (splitArrayArithmetic.py:758-760).
     Returns float32 [B, outsize] (matmul PN branch, splitArrayArithmetic.py:698-978).
     """
     B, insize = in_b.shape
@@ -104,6 +112,9 @@ def slice_matmul(in_b, g_pos, g_neg, p, solver):
     in_f = (in_b.astype(f32) * f32(inputV)).reshape(B, numX, rows)
     Gp = (g_pos.astype(f32) * f32(p.cellDeltaConduct) + f32(p.cellMinConduct)).reshape(numX, rows, true_out)
     Gn = (g_neg.astype(f32) * f32(p.cellDeltaConduct) + f32(p.cellMinConduct)).reshape(numX, rows, true_out)
+    if vary is not None:
+        Gp = (Gp / np.asarray(vary(Gp.shape), f32)).astype(f32)
+        Gn = (Gn / np.asarray(vary(Gn.shape), f32)).astype(f32)
     Ip = np.asarray(solver(in_f, Gp, B, rows, cols, numX, numY), f32)
     In = np.asarray(solver(in_f, Gn, B, rows, cols, numX, numY), f32)
     levels = f32(2 ** p.adc_bits - 1)
@@ -155,13 +166,14 @@ def droop_solver(in_v, G, B, rows, cols, numX, numY):
     return (ideal * (1.0 - 0.0031 * (j % 11) - 0.0007 * (j // 11))).astype(f32)
 
 
-def slice_matmul_ref(in_v, g, j, p, solver):
+def slice_matmul_ref(in_v, g, j, p, solver, vary=None):
     """One input-bit x weight-slice product on a Ref-column array
     (matmul, splitArrayArithmetic.py:758-771 map, :818 solve, :835-836 ADC,
     :980-996 reference-column subtraction).
 
     in_v [B, insize] input levels (signed for negative pulses); g [insize,
-    outsize] cell states of slice j.  Returns float32 [B, outsize].
+    outsize] cell states of slice j; vary as for slice_matmul, one draw for the
+    whole map with its reference columns (:788).  Returns float32 [B, outsize].
     """
     B, insize = in_v.shape
     outsize = g.shape[1]
@@ -177,6 +189,8 @@ def slice_matmul_ref(in_v, g, j, p, solver):
     extra[..., 1] = 1
     g = np.concatenate([g.reshape(true_in, numY, cols), extra], axis=2)
     G = (g.astype(f32) * f32(p.cellDeltaConduct) + f32(p.cellMinConduct)).reshape(numX, rows, numY * (cols + 2))
+    if vary is not None:
+        G = (G / np.asarray(vary(G.shape), f32)).astype(f32)
     in_f = (in_v.astype(f32) * f32(inputV)).reshape(B, numX, rows)
     I = np.asarray(solver(in_f, G, B, rows, cols + 2, numX, numY), f32)
     code = np.round((I / f32(p.adcUseI)) * f32(2 ** p.adc_bits - 1)).reshape(B, numX, numY, cols + 2)
@@ -188,9 +202,11 @@ def slice_matmul_ref(in_v, g, j, p, solver):
     return (code[..., :cols].sum(axis=1, dtype=f32).reshape(B, -1)[:, :outsize] * scale).astype(f32)
 
 
-def split_matmul_ex(x, w, p, arr="PN", neg_pulse=False, solver=ideal_solver):
+def split_matmul_ex(x, w, p, arr="PN", neg_pulse=False, solver=ideal_solver, vary=None):
     """splitArr_matmul_nn (splitArrayArithmetic.py:1161-1260) for PN or Ref
-    arrays and complement-code or negative-pulse inputs."""
+    arrays and complement-code or negative-pulse inputs; vary(shape) draws the
+    conductance variation of every map in the reference's call order (input
+    bit outer, slice inner, positive before negative)."""
     x = np.asarray(x, f32)
     w = np.asarray(w, f32)
     B = x.shape[0]
@@ -217,7 +233,7 @@ def split_matmul_ex(x, w, p, arr="PN", neg_pulse=False, solver=ideal_solver):
         for i in range(0, p.input_bits, p.dac_bits):
             ib = in_bits(i)
             for j in range(0, p.weight_bits, p.cellBits):
-                o = slice_matmul(ib, (wpos >> j) & mask_cell, (wneg >> j) & mask_cell, p, solver)
+                o = slice_matmul(ib, (wpos >> j) & mask_cell, (wneg >> j) & mask_cell, p, solver, vary)
                 t = o * f32(2.0 ** (i + j + s1 + s2))
                 out = (out + t if sign(i) > 0 else out - t).astype(f32)
         return out
@@ -227,7 +243,7 @@ def split_matmul_ex(x, w, p, arr="PN", neg_pulse=False, solver=ideal_solver):
     for i in range(0, p.input_bits, p.dac_bits):
         ib = in_bits(i)
         for j in range(0, p.weight_bits, p.cellBits):
-            o = slice_matmul_ref(ib, (wi >> j) & mask_cell, j, p, solver)
+            o = slice_matmul_ref(ib, (wi >> j) & mask_cell, j, p, solver, vary)
             t = o * f32(2.0 ** (i + j + s1 + s2))
             out = (out + t if sign(i) > 0 else out - t).astype(f32)
     return out
@@ -253,7 +269,7 @@ def unfold(x, kh, kw, stride=(1, 1), padding=(0, 0), dilation=(1, 1)):
 
 
 def conv2d_sp(x, weight, bias, p, stride=(1, 1), padding=(0, 0), dilation=(1, 1), arr="PN", neg_pulse=False,
-              use_fp_bias=True, solver=ideal_solver):
+              use_fp_bias=True, solver=ideal_solver, vary=None):
     """Conv2d_sp evaluation (conv_split.py:106-134): unfold, the split matmul
     against W reshaped [Cout, C*kh*kw] and transposed, bias in float32 (or
     mapped to an extra array row driven by ones), fold back to NCHW."""
@@ -266,7 +282,7 @@ def conv2d_sp(x, weight, bias, p, stride=(1, 1), padding=(0, 0), dilation=(1, 1)
     if bias is not None and not use_fp_bias:
         cols = np.concatenate([cols, np.ones((cols.shape[0], 1), f32)], axis=1)
         wm = np.concatenate([wm, np.asarray(bias, f32)[None]], axis=0)
-    y = split_matmul_ex(cols, wm, p, arr=arr, neg_pulse=neg_pulse, solver=solver)
+    y = split_matmul_ex(cols, wm, p, arr=arr, neg_pulse=neg_pulse, solver=solver, vary=vary)
     if bias is not None and use_fp_bias:
         y = (y + np.asarray(bias, f32)).astype(f32)
     return np.ascontiguousarray(y.reshape(N, OH * OW, Cout).transpose(0, 2, 1)).reshape(N, Cout, OH, OW)

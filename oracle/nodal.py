@@ -164,13 +164,37 @@ def nonlinear_conductance(V, z, params):
     return 1.0 / ((1.0 - z) * r(a_on, b_on) + z * r(a_off, b_off))
 
 
-def solve_nonlinear(g_lin, g_wire, vin, params, tol=1e-14, max_iter=200):
+def solve_nonlinear(g_lin, g_wire, vin, params, tol=1e-14, max_iter=200, reuse_factor=False):
     """FP64 fixed point of the nonlinear nodal system by Picard iteration: the
     cell conductances are re-evaluated at the current cell voltages and the
     linear system is solved exactly (sparse LU) until the node voltages move
-    less than ``tol``.  Returns (u, d, iterations)."""
+    less than ``tol``.  Returns (u, d, iterations).
+
+    ``reuse_factor=True`` keeps the factorisation of the linear-cell matrix and
+    iterates x += A0^-1 (b - A(x) x) instead (the same fixed point, a few more
+    but far cheaper iterations: for 512 x 512 tiles one triangular solve per
+    iteration instead of a new factorisation); it stops at ``tol`` or where the
+    corrections stop shrinking below 1e-10 V, the FP64 rounding floor of the
+    residual b - A(x) x (~4e-13 V at 512 x 512)."""
     z = nonlinear_z(g_lin, params[0], params[1])
     g = np.asarray(g_lin, np.float64).copy()
+    if reuse_factor:
+        n, m = g.shape
+        vin = np.asarray(vin, np.float64).reshape(n)
+        A0, b = assemble(g, g_wire, vin)
+        lu = spla.splu(A0)
+        x = lu.solve(b)
+        prev = np.inf
+        for it in range(1, max_iter + 1):
+            gv = nonlinear_conductance(x[0::2].reshape(n, m) - x[1::2].reshape(n, m), z, params)
+            A, _ = assemble(gv, g_wire, vin)
+            dx = lu.solve(b - A @ x)
+            x += dx
+            step = np.abs(dx).max()
+            if step < tol or (step < 1e-10 and step > 0.5 * prev):
+                return x[0::2].reshape(n, m), x[1::2].reshape(n, m), it
+            prev = step
+        raise RuntimeError("nonlinear oracle did not converge")
     u, d = solve(g, g_wire, vin)
     for it in range(1, max_iter + 1):
         g = nonlinear_conductance(u - d, z, params)

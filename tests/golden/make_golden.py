@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory from the reference itself.
 
-Runs only where the reference tree is present (it reads it from
-/root/reference).  Three sources:
+Runs only where the reference tree is present (it reads it from the
+directory in $FADESIM_REFERENCE, by default /root/reference).  Three sources:
 
 1. The reference's crossbarHspice V1 ``sim``, compiled from its own sources by
    ``make -C oracle ref`` into ``oracle/_ref/sim``, run on seeded configs written
@@ -14,7 +14,7 @@ Runs only where the reference tree is present (it reads it from
    torch and there is no GPU here).  Nothing from that copy is kept.
 3. Their outputs, saved as small .npz files next to this script.
 
-Usage: python tests/golden/make_golden.py [sim] [pimtorch] [layers] [fcm] [ir2s] [simtext] [sim2text]
+Usage: python tests/golden/make_golden.py [sim] [pimtorch] [layers] [variation] [fcm] [ir2s] [simtext] [sim2text]
 """
 import os
 import re
@@ -28,7 +28,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
-REF = "/root/reference"
+REF = os.environ.get("FADESIM_REFERENCE", "/root/reference")
 NN = os.path.join(REF, "pimtorch", "pimfixedpoint", "fixedPoint", "nn")
 SIM = os.path.join(REPO, "oracle", "_ref", "sim")
 
@@ -421,8 +421,46 @@ def pimtorch_layer_fixtures():
         shutil.rmtree(td, ignore_errors=True)
 
 
+def variation_fixtures():
+    """Cycle-to-cycle conductance variation in the layer path: the reference's
+    splitArr_matmul_nn with phyArrParams.sigma = 0.1, its network generator
+    reset to the default seed first (variations.reset_all), the droop solve
+    standing in for the IR-drop solve; a PN and a Ref-column case."""
+    import torch
+    td, cc, ids, sa = import_pimtorch()
+    try:
+        P = cc.phyArrParams
+        P.cpp_ir_drop_accelerate_flag = True
+        P.cpp_ir_drop_accelerate = _DroopSolve()
+        P.IRdropMode = cc.ir_drop_mode.accurate_GS_math
+        P.useOUSize = False
+        P.useBNN = False
+        P.inputVmode = cc.input_v_mode.complement_code
+        cases = [
+            ("var_pn", dict(Ron=1e3, Roff=1e6, cellBits=2, rows=32, cols=32, inputMaxVoltage=0.2, adc_bits=8), "PN",
+             lambda r: r.integers(0, 256, (4, 70)).astype(np.float32),
+             lambda r: (r.standard_normal((70, 40)) * 0.05).astype(np.float32)),
+            ("var_ref", dict(Ron=1e3, Roff=1e6, cellBits=1, rows=32, cols=16, inputMaxVoltage=1.0, adc_bits=10), "Ref",
+             lambda r: r.standard_normal((3, 40)).astype(np.float32),
+             lambda r: (r.standard_normal((40, 20)) * 0.1).astype(np.float32)),
+        ]
+        for name, kw, amode, mkx, mkw in cases:
+            p = intstages.ArrayParams(**kw)
+            set_params(cc, p)
+            P.sigma = 0.1
+            r = np.random.default_rng(300 + len(name))
+            x, w = mkx(r), mkw(r)
+            cc.variations.reset_all()
+            y = sa.splitArr_matmul_nn(torch.from_numpy(x), torch.from_numpy(w), 8, 1, p.adc_bits, 10, 8,
+                                      getattr(cc.phyArrMode, amode), torch.float32)
+            np.savez_compressed(os.path.join(HERE, "pimtorch_layer_%s.npz" % name), x=x, w=w, y=y.numpy(),
+                                arr_mode=amode, sigma=0.1, seed=cc.variations.var_defaultSeed, **kw)
+    finally:
+        shutil.rmtree(td, ignore_errors=True)
+
+
 if __name__ == "__main__":
-    which = sys.argv[1:] or ["sim", "pimtorch", "layers", "fcm", "ir2s", "simtext", "sim2text"]
+    which = sys.argv[1:] or ["sim", "pimtorch", "layers", "variation", "fcm", "ir2s", "simtext", "sim2text"]
     if "sim2text" in which:
         sim2_text_fixture()
     if "simtext" in which:
@@ -437,4 +475,6 @@ if __name__ == "__main__":
         pimtorch_fixtures()
     if "layers" in which:
         pimtorch_layer_fixtures()
+    if "variation" in which:
+        variation_fixtures()
     print("fixtures written to", HERE)

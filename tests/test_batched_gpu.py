@@ -58,3 +58,37 @@ def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
     monkeypatch.setattr(autotune, "_mem", None)
     assert autotune.lookup(128, 128) == {"vectors_per_cta": 8}
     assert autotune.candidates("rbsor")[0]["omega"] > 1.9
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method,n,m,ld", [("line", 40, 64, 64), ("line", 64, 64, 128), ("line", 128, 128, 256),
+                                           ("line", 100, 77, 256), ("line", 256, 256, 512),
+                                           ("rbsor", 96, 128, 256)])
+def test_forced_layouts_match_oracle(method, n, m, ld):
+    """The autotuner's shape axis: a tile solved on a larger layout than its own
+    (a 64 x 64 tile on the 128 single-CTA kernel, a 128 x 128 tile on a 4-CTA
+    cluster of 64-row bands, a 256 x 256 tile on a 16-CTA cluster) lands on the
+    same nodal solution, the work items claimed from the device queue."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from fadesim_gb300 import cpp_ir_drop_accelerate as acc
+    B, X = 3, 2
+    (G, v), = groups_for([(X, n, m)], B=B, seed=n + m + ld)
+    out, st, _ = acc.ir_drop_gs_ex(torch.from_numpy(v).cuda(), torch.from_numpy(G).cuda(), B, n, m, X, 1,
+                                   g_wire=GW, method=method, kernel_ld=ld, tol_v=1e-8)
+    assert st["status_or"] == 1 and st["solves"] == B * X, st
+    ref = nodal.solve_layer(v.astype(np.float64), G.astype(np.float64), n, m, X, 1, GW)
+    assert np.abs(out.double().cpu().numpy() - ref).max() <= 2e-6 * np.abs(ref).max()
+    with pytest.raises(RuntimeError, match="kernel_ld"):
+        acc.ir_drop_gs_ex(torch.from_numpy(v).cuda(), torch.from_numpy(G).cuda(), B, n, m, X, 1, g_wire=GW,
+                          method=method, kernel_ld=32)
+
+
+def test_autotune_candidates_cover_the_kernel_shapes():
+    from fadesim_gb300 import autotune
+    assert autotune.layouts(64, 64) == [64, 128]
+    assert autotune.layouts(128, 100) == [128, 256]
+    assert autotune.layouts(256, 256) == [256, 512]
+    assert autotune.layouts(512, 300) == [512]
+    lds = {c["kernel_ld"] for c in autotune.candidates("line", 128, 128)}
+    assert lds == {128, 256}

@@ -120,3 +120,54 @@ def test_red_black_sweep_covers_each_colour_once():
                 ii, jj = np.meshgrid(np.arange(n), np.arange(m), indexing="ij")
                 assert np.array_equal(hitU, (((ii + jj) & 1) == c).astype(int)), (n, m, c)
                 assert np.array_equal(hitD, (((ii + jj + 1) & 1) == c).astype(int)), (n, m, c)
+
+
+def test_cluster_red_black_bands_cover_each_colour_once():
+    """csrc/rbsor_cluster.cu: CTA r of a C-CTA cluster holds global rows
+    r*RPC ... r*RPC + nloc - 1; its thread t owns column t % LDM at local rows
+    t / LDM + (1024 / LDM) k and, in half-sweep c, relaxes its cells' wordline
+    node when (r*RPC + t / LDM + col) & 1 == c, else their bitline node.  Over
+    all CTAs each half-sweep updates every node of colour c exactly once, and
+    every value it reads -- including the halo rows of the neighbouring bands
+    -- has the other colour; the halo a band reads is the neighbour's last
+    (above) or first (below) local row, inside that band."""
+    import numpy as np
+    T = 1024
+    for LDM, C, RPC in ((256, 4, 64), (512, 16, 32)):
+        STEP = T // LDM
+        t = np.arange(T)
+        col, lr0 = t % LDM, t // LDM
+        for n, m in ((LDM, LDM), (130, 256), (200, 150), (LDM - 3, LDM - 1), (300, 420), (129, 7)):
+            if max(n, m) > LDM or max(n, m) <= LDM // 2 and LDM == 512:
+                continue
+            for c in (0, 1):
+                hitU = np.zeros((n, m), int)
+                hitD = np.zeros((n, m), int)
+                for r in range(C):
+                    row0 = r * RPC
+                    nloc = max(0, min(RPC, n - row0))
+                    for tt in range(T):
+                        j = col[tt]
+                        if j >= m:
+                            continue
+                        isU = ((row0 + lr0[tt] + j) & 1) == c
+                        for lr in range(lr0[tt], nloc, STEP):
+                            i = row0 + lr
+                            (hitU if isU else hitD)[i, j] += 1
+                            own = (i + j) & 1 if isU else (i + j + 1) & 1
+                            assert own == c
+                            if isU:
+                                nbrs = [(i, j - 1), (i, j + 1)]
+                            else:
+                                nbrs = [(i - 1, j), (i + 1, j)]
+                                if lr == 0 and i > 0:  # halo above: the band above is full
+                                    assert r > 0 and i - 1 == (r - 1) * RPC + RPC - 1
+                                if lr + 1 == nloc and i + 1 < n:  # halo below: the next band's first row
+                                    assert r + 1 < C and i + 1 == (r + 1) * RPC
+                            for a, b in nbrs:
+                                if 0 <= a < n and 0 <= b < m:
+                                    assert (((a + b) & 1) if isU else ((a + b + 1) & 1)) != c
+                            assert (((i + j + 1) & 1) if isU else ((i + j) & 1)) != c
+                ii, jj = np.meshgrid(np.arange(n), np.arange(m), indexing="ij")
+                assert np.array_equal(hitU, (((ii + jj) & 1) == c).astype(int)), (LDM, n, m, c)
+                assert np.array_equal(hitD, (((ii + jj + 1) & 1) == c).astype(int)), (LDM, n, m, c)

@@ -129,6 +129,33 @@ def test_ref_and_negpulse_stages_bit_exact(gold, name):
     assert np.array_equal(y, z["y"])
 
 
+def torch_variation_draws(sigma, seed):
+    """The reference's variation draws, exp(sigma N(0,1)) from a torch CPU
+    generator seeded like its network generator (seed + 2), in call order."""
+    import torch
+    gen = torch.Generator()
+    gen.manual_seed(int(seed) + 2)
+    return lambda shape: torch.exp(torch.randn(tuple(shape), generator=gen) * sigma).numpy()
+
+
+@pytest.mark.parametrize("name", ["var_pn", "var_ref"])
+def test_variation_stages_bit_exact(gold, name):
+    """Cycle-to-cycle variation (sigma 0.1) in the layer path: the restatement's
+    draw order -- input bit outer, slice inner, positive before negative -- and
+    its G / exp(sigma N) reproduce the reference's splitArr_matmul_nn bit for bit
+    (same droop solve); without the draws the result differs."""
+    pytest.importorskip("torch")
+    z = gold("pimtorch_layer_%s.npz" % name)
+    p = layer_params(z)
+    vary = torch_variation_draws(float(z["sigma"]), int(z["seed"]))
+    y = intstages.split_matmul_ex(z["x"], z["w"], p, arr=str(z["arr_mode"]), solver=intstages.droop_solver,
+                                  vary=vary)
+    assert y.dtype == np.float32
+    assert np.array_equal(y, z["y"])
+    y0 = intstages.split_matmul_ex(z["x"], z["w"], p, arr=str(z["arr_mode"]), solver=intstages.droop_solver)
+    assert not np.array_equal(y0, z["y"])
+
+
 @pytest.mark.parametrize("name", LAYER_CONV)
 def test_conv2d_sp_bit_exact(gold, name):
     """Conv2d_sp evaluation (unfold, split matmul, bias, fold) against the reference module."""
@@ -270,3 +297,17 @@ def test_nonlinear_family_float32_tracks_float64():
                                nonlinear=params, **kw)
         assert r32.dtype == np.float32
         assert np.abs(r32 - r64).max() <= 1e-5 * np.abs(r64).max(), mode
+
+
+def test_nonlinear_reused_factor_matches_picard():
+    """The factor-reusing nonlinear oracle (one factorisation, x += A0^-1 (b -
+    A(x) x)) lands on the Picard fixed point."""
+    rng = np.random.default_rng(4)
+    n, m = 48, 40
+    G = 1.0 / np.array([2e6, 1.6e6, 1.3e6, 1e6])[rng.integers(0, 4, (n, m))]
+    G = G / np.exp(0.1 * rng.standard_normal((n, m)))
+    vin = rng.random(n) * 0.2
+    p = nodal.sinh_params(1e6, 2e6)
+    u, d, _ = nodal.solve_nonlinear(G, 1 / 2.93, vin, p)
+    u2, d2, _ = nodal.solve_nonlinear(G, 1 / 2.93, vin, p, reuse_factor=True)
+    assert max(np.abs(u - u2).max(), np.abs(d - d2).max()) < 1e-12

@@ -102,8 +102,13 @@ def test_line_solver_dtypes(acc, dtype):
     assert np.abs(got - cur).max() <= 1e-6 * np.abs(cur).max()
 
 
-@pytest.mark.parametrize("shape", [(2, 1, 1, 16, 24), (1, 2, 1, 64, 64), (1, 1, 1, 128, 128)])
+@pytest.mark.parametrize("shape", [(2, 1, 1, 16, 24), (1, 2, 1, 64, 64), (1, 1, 1, 128, 128),
+                                   (2, 1, 2, 256, 256), (1, 1, 1, 130, 256), (1, 1, 1, 200, 150),
+                                   (1, 1, 1, 512, 512), (1, 1, 1, 300, 420)])
 def test_rbsor_matches_oracle(acc, shape):
+    """The plain red-black SOR, single-CTA up to 128 and cluster-resident above
+    (4-CTA bands up to 256, 16-CTA bands up to 512, halo rows through
+    distributed shared memory, partial and empty bands included)."""
     B, X, Y, n, m = shape
     inp, G = make_case(21, B, X, Y, n, m, CFG1, 0.2)
     cur, U, D = oracle_planes(inp, G, B, X, Y, n, m)
@@ -111,6 +116,9 @@ def test_rbsor_matches_oracle(acc, shape):
     assert stats["status_or"] == 1, stats
     err = max(np.abs(planes[:, :, :, 0] - U).max(), np.abs(planes[:, :, :, 1] - D).max())
     assert err < V_TOL, (err, stats)
+    got, st2, _ = run(acc, inp, G, B, X, Y, n, m, method="rbsor", ret_V=False)
+    assert st2["status_or"] == 1, st2
+    assert np.abs(got - cur).max() <= I_RTOL * np.abs(cur).max()
 
 
 @pytest.mark.parametrize("dt,rtol", [(np.float64, 1e-12), (np.float32, 2e-5)])
@@ -164,7 +172,7 @@ def test_dropin_signature_and_errors(acc):
         acc.ir_drop_gs(ti, tg, B, 1, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
     with pytest.raises(RuntimeError):
         acc.ir_drop_gs(ti, tg.double(), B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
-    with pytest.raises(NotImplementedError):  # sinh cells: the IR2S family runs linear cells only
+    with pytest.raises(RuntimeError, match="nonlinear_params"):  # sinh cells need all six parameters
         acc.ir2s(ti, tg, B, n, m, X, Y, 10, 2.93, False, 1e-7, True, [1.0])
     empty = acc.ir_drop_gs(ti[:0], tg, 0, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
     assert empty.shape == (0, X, Y * m)
@@ -197,7 +205,40 @@ def test_nonfinite_input_reports_status(acc, n):
     assert stats["status_or"] & 4
 
 
-@pytest.mark.parametrize("method,n,cap", [("line", 64, 1), ("line", 256, 2), ("rbsor", 64, 5)])
+def test_dropin_reports_solve_status(acc, monkeypatch):
+    """ir_drop_gs reads every call's status back: a clean call matches the
+    oracle and stays silent; a NaN conductance or an iteration cap far below
+    what the tolerance needs warns (check_status "warn", the default), raises
+    under "raise", and passes silently under "off"."""
+    import warnings
+    B, X, Y, n, m = 3, 2, 1, 64, 64
+    inp, G = make_case(8, B, X, Y, n, m, STRONG, 1.0)
+    ti = torch.tensor(inp, dtype=torch.float32, device="cuda")
+    tg = torch.tensor(G, dtype=torch.float32, device="cuda")
+    call = lambda g: acc.ir_drop_gs(ti, g, B, n, m, X, Y, 600, GW, 1.9, False, 1e-7, False, [], False)
+    with warnings.catch_warnings():
+        warnings.simplefilter("error", acc.SolveStatusWarning)
+        out = call(tg)
+    ref = nodal.solve_layer(inp, G, n, m, X, Y, GW)
+    assert np.abs(out.double().cpu().numpy() - ref).max() <= I_RTOL * np.abs(ref).max()
+    bad = tg.clone()
+    bad[1, 9, 10] = float("nan")
+    with pytest.warns(acc.SolveStatusWarning, match="non-finite"):
+        call(bad)
+    monkeypatch.setattr(acc.options, "check_status", "raise")
+    with pytest.raises(acc.SolveStatusError, match="non-finite"):
+        call(bad)
+    monkeypatch.setattr(acc.options, "max_iters", 1)
+    monkeypatch.setattr(acc.options, "tol_v", 1e-8)
+    with pytest.raises(acc.SolveStatusError, match="iteration cap"):
+        call(tg)
+    monkeypatch.setattr(acc.options, "check_status", "off")
+    with warnings.catch_warnings():
+        warnings.simplefilter("error", acc.SolveStatusWarning)
+        call(bad)
+
+
+@pytest.mark.parametrize("method,n,cap", [("line", 64, 1), ("line", 256, 2), ("rbsor", 64, 5), ("rbsor", 256, 12)])
 def test_iteration_cap_reports_status(acc, method, n, cap):
     """Forced non-convergence: a cap far below what the tolerance needs ends
     every solve with the cap status, never the converged one, at the cap."""
