@@ -353,12 +353,15 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
 
     def step():
+        if args.quick_method != "line":  # profiling the plain comparator
+            return acc.ir_drop_gs_ex(ti, tg, B, ROWS, COLS, X, Y, g_wire=gw, method=args.quick_method,
+                                     return_stats=False)[0]
         return acc.ir_drop_gs(ti, tg, B, ROWS, COLS, X, Y, 600, gw, 1.9, False, 1e-7, False, [], False)
 
     for _ in range(max(3, args.warmup)):
         out = step()
     torch.cuda.synchronize()
-    _, stats, _ = acc.ir_drop_gs_ex(ti, tg, B, ROWS, COLS, X, Y, g_wire=gw, method="line")
+    _, stats, _ = acc.ir_drop_gs_ex(ti, tg, B, ROWS, COLS, X, Y, g_wire=gw, method=args.quick_method)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if dist:
         dist.barrier()
@@ -561,6 +564,8 @@ def main():
     ap.add_argument("--no-warm", action="store_true", help="skip training/evaluating the learned warm start")
     ap.add_argument("--quick", action="store_true",
                     help="time the device-resident solve only (no e2e, comparator or CPU baseline); for profiling")
+    ap.add_argument("--quick-method", default="line", choices=["line", "rbsor"],
+                    help="with --quick: the solver timed (rbsor: the plain red-black SOR, for profiling)")
     ap.add_argument("--size", type=int, default=128,
                     help="with --quick: tile size N (N x N tiles; 256 and 512 run on the cluster kernels)")
     ap.add_argument("--only-large", type=int, default=0, metavar="TILES",

@@ -5,6 +5,7 @@
 // delta break.
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 
 #include <mutex>
 #include <string>
@@ -96,6 +97,18 @@ struct Scratch {
     }
 };
 
+// Margin of the adaptive precision schedule (FADESIM_PRECISE_MARGIN, default
+// 4): an iteration is made precise when its predicted error estimate is
+// within this factor of the tolerance.
+float precise_margin() {
+    static const float v = [] {
+        const char *e = getenv("FADESIM_PRECISE_MARGIN");
+        const float f = e ? (float)atof(e) : 4.f;
+        return f > 0.f ? f : 4.f;
+    }();
+    return v;
+}
+
 int device_sms() {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -143,6 +156,7 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
     a.ctl.tol_v = (opts && opts->tol_v > 0) ? (float)opts->tol_v : 1e-8f;
     a.ctl.residual_period = opts ? opts->residual_period : 0;  // 0: adaptive schedule
     a.ctl.residual_ff = (opts && opts->residual_kind == 1) ? 0 : 1;
+    a.ctl.precise_margin = precise_margin();
     const int sms = device_sms();
     int grid = 0, ld = 0;
     size_t scratch_floats = 0;

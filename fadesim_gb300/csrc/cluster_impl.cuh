@@ -682,9 +682,15 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             __syncthreads();
             // From the ideal state the planes are zero: the first iteration reads
             // neither plane nor the halos, so they need no clearing -- unless every
-            // iteration must be precise (then they are cleared).
-            bool zero = !precise_first;
-            if (precise_first) {
+            // iteration must be precise, or the cells are sinh cells (then they are
+            // cleared).  Sinh-cell solves start with the FP32 pass body: two bodies
+            // then alternate per solve instead of three, which keeps the loop within
+            // the instruction caches (the choice is made at run time, from the
+            // call's controls: a compile-time one lets the compiler restructure the
+            // loop and grow the object).
+            const bool clear_first = precise_first || a.ctl.nl != 0;
+            bool zero = !clear_first;
+            if (clear_first) {
                 for (int e = tid; e < RPC * LDM; e += CL_T) {
                     U[e] = 0.f;
                     D[e] = 0.f;
@@ -798,7 +804,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                     }
                     res64 = true;
                 } else {
-                    res64 = kres > 0 ? (it % kres == 0) : (kres == 0 && stop.want_precise(tol, vm));
+                    res64 = kres > 0 ? (it % kres == 0) : (kres == 0 && stop.want_precise(tol, vm, a.ctl.precise_margin));
                 }
                 if (it >= maxit) {
                     status = FADESIM_ST_MAXITER;

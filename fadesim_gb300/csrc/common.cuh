@@ -24,6 +24,7 @@ struct SolveCtl {
     int residual_period;  // precise residual every k iterations (<0: never)
     float omega;          // <= 0: adaptive
     int residual_ff;      // precise residual in float-float (FP32 pipe) instead of FP64
+    float precise_margin; // adaptive schedule: precise when the predicted estimate is within this factor of tol
     // sinh cells (nonlinear_params = [R_on, R_off, a_on, b_on, a_off, b_off])
     int nl;
     float nl_R_on, nl_inv_dR;        // z = (1/g_lin - R_on) / (R_off - R_on), clamped at 0

@@ -164,13 +164,15 @@ struct LineStop {
     }
 
     // Whether the next iteration should compute its residual precisely.
-    __device__ __forceinline__ bool want_precise(float tol, float vm) const {
+    // margin: how far above the tolerance a predicted estimate may be and the
+    // iteration still be made precise (4 by default).
+    __device__ __forceinline__ bool want_precise(float tol, float vm, float margin = 4.f) const {
         if (it == 0 || !(rho > 0.f)) return false;
         const float r = fminf(rho, 0.999f);
         const float next = h0 * r;
         const float est_next = __fdividef(next * r, 1.f - r);
         const float floor_v = 4.f * 1.1920929e-07f * vm;
-        return est_next <= 4.f * fmaxf(tol, floor_v) || h0 <= 1e-4f * vm || (it >= 3 && h0 >= 0.9f * h1);
+        return est_next <= margin * fmaxf(tol, floor_v) || h0 <= 1e-4f * vm || (it >= 3 && h0 >= 0.9f * h1);
     }
 
     // First-step rate of the finished solve, to seed the next vector of the tile.

@@ -542,7 +542,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 } else {
                     // kres 0: adaptive (precise when the next iteration should be
                     // the last or nears the FP32 residual noise); k > 0: every k
-                    res64 = kres > 0 ? (it % kres == 0) : (kres == 0 && stop.want_precise(tol, vm));
+                    res64 = kres > 0 ? (it % kres == 0) : (kres == 0 && stop.want_precise(tol, vm, a.ctl.precise_margin));
                 }
                 if (it >= maxit) {
                     status |= FADESIM_ST_MAXITER;

@@ -128,6 +128,7 @@ extern "C" int fadesim_ir_drop_gs_noalloc_f32(const float *input, const float *G
     a.ctl.residual_period = 0;  // adaptive, as the default of the allocating entry
     a.ctl.omega = 0.f;
     a.ctl.residual_ff = 1;
+    a.ctl.precise_margin = 4.f;
     long long grid = (long long)per_sm * sms;
     if (grid > max_ctas) grid = max_ctas;
     // whole tiles per work item when tiles are plentiful, else split vectors

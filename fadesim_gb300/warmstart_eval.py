@@ -8,7 +8,7 @@ SOR) from the ideal state and from the prediction, the fallback (rejection) rate
 and the end-to-end solves/s including inference.
 
   python -m fadesim_gb300.warmstart_eval [--size 128] [--train 200000] [--infer 8192] [--cells weak|strong]
-  python -m fadesim_gb300.warmstart_eval --conv      (one convolution on both kernels, TFLOP/s)
+  python -m fadesim_gb300.warmstart_eval --conv [--conv-shape N,H,W,Cin,Cout]   (one convolution, both kernels)
 """
 import argparse
 import json
@@ -140,11 +140,13 @@ def main():
     ap.add_argument("--cells", default="weak", choices=["weak", "strong"])
     ap.add_argument("--conv", action="store_true",
                     help="only time one network convolution on both kernels (for profiling)")
+    ap.add_argument("--conv-shape", default="64,128,128,64,32", help="N,H,W,Cin,Cout of --conv")
     a = ap.parse_args()
     if a.conv:
         from .build import build
         build()
-        print(json.dumps([conv_throughput(), conv_throughput(legacy=True)]))
+        N, H, W, cin, cout = (int(v) for v in a.conv_shape.split(","))
+        print(json.dumps([conv_throughput(N, H, W, cin, cout), conv_throughput(N, H, W, cin, cout, legacy=True)]))
         return
     print(json.dumps(train_and_evaluate(a.size, a.train, a.batch, a.infer, cells=a.cells)))
 
