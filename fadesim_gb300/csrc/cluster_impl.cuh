@@ -682,15 +682,11 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             __syncthreads();
             // From the ideal state the planes are zero: the first iteration reads
             // neither plane nor the halos, so they need no clearing -- unless every
-            // iteration must be precise, or the cells are sinh cells (then they are
-            // cleared).  Sinh-cell solves start with the FP32 pass body: two bodies
-            // then alternate per solve instead of three, which keeps the loop within
-            // the instruction caches (the choice is made at run time, from the
-            // call's controls: a compile-time one lets the compiler restructure the
-            // loop and grow the object).
-            const bool clear_first = precise_first || a.ctl.nl != 0;
-            bool zero = !clear_first;
-            if (clear_first) {
+            // iteration must be precise (then they are cleared).  (Clearing them for
+            // sinh cells too, so that two pass bodies alternate instead of three,
+            // measured 2% slower on the 512x512 sinh-cell workload.)
+            bool zero = !precise_first;
+            if (precise_first) {
                 for (int e = tid; e < RPC * LDM; e += CL_T) {
                     U[e] = 0.f;
                     D[e] = 0.f;

