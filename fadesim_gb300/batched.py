@@ -72,13 +72,18 @@ class TileBatch:
             return [res[i] for i in range(len(self.groups))] if stats else None
         ev = torch.cuda.Event()
         ev.record(main)
-        out = []
-        for g, s in zip(self.groups, self.streams):
-            s.wait_event(ev)
-            out.append(self._launch(g, s, stats))
+        # largest tiles first: the cluster kernels take whole clusters of SMs
+        # (36 four-CTA clusters use 144 of 152), and the tile-per-CTA kernels
+        # launched after them start on the SMs left over, their CTAs claiming
+        # work items from the device queue as SMs free up
+        order = sorted(range(len(self.groups)), key=lambda i: -self.groups[i].n * self.groups[i].m)
+        res = {}
+        for i in order:
+            self.streams[i].wait_event(ev)
+            res[i] = self._launch(self.groups[i], self.streams[i], stats)
         for s in self.streams:
             main.wait_stream(s)
-        return out if stats else None
+        return [res[i] for i in range(len(self.groups))] if stats else None
 
     def tune(self, sample_tiles=304, reps=2):
         """Autotune every group's launch parameters (kernel layout, vectors per

@@ -170,3 +170,52 @@ def test_mlp_layer_path_runs_both_strategies(sa):
     r = mlp_eval.evaluate(batch=20)   # 160 vectors per call: more than a tile's 128 rows
     assert r["direct"]["solves_per_batch"] == sum(mlp_eval.solves_per_batch(20, mlp_eval.config()))
     assert r["superposition"]["max_rel_current_diff_vs_direct"] < 1e-4   # the current contract
+
+
+def test_mlp_first_layer_end_to_end_against_oracle(sa):
+    """The MLP configuration itself, end to end: the first layer (784 -> 512,
+    weights N(0, 0.05^2), 2-bit cells of 1 kohm - 1 Mohm on 128x128 PN
+    crossbars, 0.2 V reads, 8-bit ADC) on two synthetic images through the GPU
+    path with the real CUDA solves.  The oracle's restatement of the integer
+    stages, fed the recorded currents, gives the same output bits, and the
+    recorded currents of one (slice, array) map match the FP64 nodal solve of
+    the same voltages and conductances within the 1e-4 current contract."""
+    from fadesim_gb300 import mlp_eval
+    from oracle import nodal
+    cfg = mlp_eval.config()
+    w = mlp_eval.build(3)[0]                                   # [512, 784]
+    g = torch.Generator().manual_seed(4)
+    x = torch.randint(0, 256, (2, 784), generator=g).float()
+    recorded = []
+
+    def record(v, G, B, rows, cols, numX, numY, out):
+        r = sa.default_solver(cfg)(v, G, B, rows, cols, numX, numY, out)
+        recorded.append((v.cpu().numpy(), G.cpu().numpy(), r.cpu().numpy().copy()))
+        return r
+
+    y = sa.splitArr_matmul_nn(x, w.t().contiguous(), 8, 1, 8, 10, 8, "PN", torch.float32, cfg=cfg, solver=record)
+    p = intstages.ArrayParams(Ron=1e3, Roff=1e6, cellBits=2, rows=128, cols=128, inputMaxVoltage=0.2, adc_bits=8)
+    state = {"k": 0}
+
+    def replay(in_v, G, B, rows, cols, numX, numY):
+        k = state["k"]
+        state["k"] += 1
+        i, rem = divmod(k, 8)           # oracle order: bit i, slice j, pos then neg
+        j, pn = divmod(rem, 2)
+        v_all, G_rec, cur = recorded[j * 2 + pn]
+        assert np.array_equal(G_rec, G)
+        assert np.array_equal(v_all[i * B:(i + 1) * B], in_v)
+        return cur[i * B:(i + 1) * B]
+
+    ref = intstages.split_matmul(x.numpy(), w.t().contiguous().cpu().numpy(), p, replay)
+    assert np.array_equal(y.cpu().numpy(), ref)
+    # the currents of the most significant slice's positive array on two tiles, against FP64
+    v_all, G_rec, cur = recorded[3 * 2]
+    numX, rows, cols = 7, 128, 128
+    for x_t, y_t in ((0, 0), (6, 3)):
+        Gt = G_rec[x_t, :, y_t * cols:(y_t + 1) * cols].astype(np.float64)
+        vin = v_all[:, x_t].astype(np.float64)
+        u, d = nodal.solve(Gt, 1 / cfg.r_wire, vin)
+        ref_i = nodal.currents(Gt, u, d)
+        got = cur[:, x_t, y_t * cols:(y_t + 1) * cols].astype(np.float64)
+        assert np.abs(got - ref_i).max() <= 1e-4 * np.abs(ref_i).max()
