@@ -29,6 +29,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include <mutex>
 
@@ -40,11 +41,11 @@ namespace {
 
 constexpr int TC_M = 128;          // pixels per tile = TMEM lanes
 constexpr int TC_KC = 32;          // channels per K chunk (64-byte rows)
-constexpr int TC_STAGES = 6;
 constexpr int TC_A_BYTES = TC_M * TC_KC * 2;   // 8 KB
 constexpr int TC_B_BYTES = 128 * TC_KC * 2;    // 8 KB (Cout <= 128)
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024 /* alignment */ + 256 /* barriers */;
+// dynamic shared memory of a kernel with S stages
+constexpr int tc_smem(int S) { return S * TC_STAGE_BYTES + 1024 /* alignment */ + 256 /* barriers */; }
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -141,6 +142,9 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// STAGES: depth of the TMA ring; fewer stages let more CTAs share an SM
+// (STAGES x 16 KB each), which hides the per-tile latency chain better.
+template <int TC_STAGES>
 __global__ void __launch_bounds__(128, 1)
     conv3x3_fwd_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW,
                           const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ skip, void *__restrict__ Y,
@@ -284,6 +288,19 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// TMA ring depth of the convolution (FADESIM_CONV_STAGES: 2, 3, 4 or 6).  A
+// CTA computes one 128-pixel tile, so the depth trades prefetch against how
+// many CTAs share an SM (shared memory: 4 at 3 stages, 2 at 6); 3 measured
+// fastest on every layer shape of the network.
+int conv_tc_stages() {
+    static const int v = [] {
+        const char *e = getenv("FADESIM_CONV_STAGES");
+        const int k = e ? atoi(e) : 3;
+        return (k == 2 || k == 3 || k == 4 || k == 6) ? k : 3;
+    }();
+    return v;
+}
+
 EncodeTiledFn encode_fn() {
     static std::once_flag once;
     static EncodeTiledFn fn = nullptr;
@@ -346,13 +363,19 @@ cudaError_t conv3x3_fwd_tc(const void *X, const void *Wt, const float *bias, con
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(conv3x3_fwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
-    if (e != cudaSuccess) return e;
     const long long tiles = (long long)N * H * W / TC_M;
     if (tiles < 1) return cudaSuccess;
-    conv3x3_fwd_tc_kernel<<<(unsigned)tiles, 128, TC_SMEM, st>>>(mx, mw, bias,
-                                                                 static_cast<const __nv_bfloat16 *>(skip), Y, H, W,
-                                                                 Cin, Cout, flags, err);
+    const int stages = conv_tc_stages();
+    void (*kern)(CUtensorMap, CUtensorMap, const float *, const __nv_bfloat16 *, void *, int, int, int, int, int,
+                 int *) = stages == 2   ? conv3x3_fwd_tc_kernel<2>
+                          : stages == 4 ? conv3x3_fwd_tc_kernel<4>
+                          : stages == 6 ? conv3x3_fwd_tc_kernel<6>
+                                        : conv3x3_fwd_tc_kernel<3>;
+    const int smem = tc_smem(stages);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    kern<<<(unsigned)tiles, 128, smem, st>>>(mx, mw, bias, static_cast<const __nv_bfloat16 *>(skip), Y, H, W, Cin,
+                                             Cout, flags, err);
     return cudaGetLastError();
 }
 
