@@ -202,12 +202,50 @@ __device__ __forceinline__ float compose_below(cg::cluster_group &cluster, const
     return v;
 }
 
-// Wordline pass over the CTA's rows (lines local to the CTA).  Gs holds g / gw
-// (or the sinh cells' positions z), cm the chain multipliers gw / pivot;
-// ZOWN / ZOTH: the own / other plane is known to be zero (first iteration).
-// FULL: every row of the band and every column present (bounds tests fold away).
+// Residual of the wordline pass over the CTA's rows (lines local to the CTA)
+// into x[], one 32-node segment per thread.  Gs holds g / gw (or the sinh
+// cells' positions z); ZOWN / ZOTH: the own / other plane is known to be zero
+// (first iteration).  FULL: every row of the band and every column present
+// (bounds tests fold away).
 template <int LDM, int RES, bool NL, bool ZOWN, bool ZOTH, bool FULL>
-__device__ __forceinline__ void cl_word_pass(float *__restrict__ U, const float *__restrict__ D,
+__device__ __forceinline__ void cl_word_residual(float (&x)[CL_SEG], const float *__restrict__ U,
+                                                 const float *__restrict__ D, const float *__restrict__ Gs,
+                                                 const float *__restrict__ vin, int nloc, int m, float inv_gw,
+                                                 const SolveCtl &ctl) {
+    constexpr int LPW = CCfg<LDM>::LPW_W, SEG = CL_SEG;
+    const int tid = threadIdx.x, lane = tid & 31, s = lane / LPW;
+    const int line = (tid >> 5) * LPW + (lane % LPW);  // < RPC by the shape
+    const bool ok = FULL || line < nloc;
+    const int p0 = s * SEG;
+    const int Bw = cswz<LDM>(line, p0);  // node p0 + k sits at Bw ^ k
+    const float vl = ok ? vin[line] : 0.f;
+    float prev = (!ZOWN && ok && p0 > 0 && (FULL || p0 - 1 < m)) ? U[cswz<LDM>(line, p0 - 1)] : 0.f;
+    float cur = (!ZOWN && ok && (FULL || p0 < m)) ? U[Bw] : 0.f;
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) {
+        const int p = p0 + k;
+        const bool has_next = (FULL && k + 1 < SEG) || (ok && p + 1 < m);
+        const float nxt = (!ZOWN && has_next) ? U[k + 1 < SEG ? (Bw ^ (k + 1)) : cswz<LDM>(line, p + 1)] : 0.f;
+        float r = 0.f;
+        if (FULL || (ok && p < m)) {
+            const int q = Bw ^ k;
+            const float o = ZOTH ? 0.f : D[q];
+            const float gs = NL ? nl_gs(Gs[q], (cur + vl) - o, ctl, inv_gw) : Gs[q];
+            r = line_residual_s<true, RES>(prev, cur, nxt, gs, o, vl, true, (FULL && k + 1 < SEG) || p + 1 < m);
+        }
+        x[k] = r;
+        prev = cur;
+        cur = nxt;
+    }
+}
+
+// Wordline pass: the residual form selected by mode (4: both planes zero, 0:
+// FP32, 3: exact line differences with an FP32 cell term, 2: float-float, 1:
+// FP64; uniform across the cluster), then one shared Thomas solve and update
+// in the multiplier form (cm the chain multipliers gw / pivot), so that the
+// kernel carries a single copy of the solve whatever the residual forms.
+template <int LDM, bool NL, bool FULL>
+__device__ __forceinline__ void cl_word_pass(int mode, float *__restrict__ U, const float *__restrict__ D,
                                              const float *__restrict__ Gs, const float *__restrict__ vin,
                                              const float *__restrict__ cm, const float *__restrict__ segprod,
                                              int nloc_in, int m_in, float inv_gw, float omega, float &dmax,
@@ -215,32 +253,23 @@ __device__ __forceinline__ void cl_word_pass(float *__restrict__ U, const float 
     constexpr int NSEG = CCfg<LDM>::NSEG_W, LPW = CCfg<LDM>::LPW_W, SEG = CL_SEG;
     const int nloc = FULL ? CCfg<LDM>::RPC : nloc_in, m = FULL ? LDM : m_in;
     const int tid = threadIdx.x, lane = tid & 31, s = lane / LPW;
-    const int line = (tid >> 5) * LPW + (lane % LPW);  // < RPC by the shape
+    const int line = (tid >> 5) * LPW + (lane % LPW);
     const bool ok = FULL || line < nloc;
     const int p0 = s * SEG;
-    const int Bw = cswz<LDM>(line, p0);  // node p0 + k sits at Bw ^ k
+    const int Bw = cswz<LDM>(line, p0);
     float x[SEG];
-    {
-        const float vl = ok ? vin[line] : 0.f;
-        float prev = (!ZOWN && ok && p0 > 0 && (FULL || p0 - 1 < m)) ? U[cswz<LDM>(line, p0 - 1)] : 0.f;
-        float cur = (!ZOWN && ok && (FULL || p0 < m)) ? U[Bw] : 0.f;
-#pragma unroll
-        for (int k = 0; k < SEG; ++k) {
-            const int p = p0 + k;
-            const bool has_next = (FULL && k + 1 < SEG) || (ok && p + 1 < m);
-            const float nxt = (!ZOWN && has_next) ? U[k + 1 < SEG ? (Bw ^ (k + 1)) : cswz<LDM>(line, p + 1)] : 0.f;
-            float r = 0.f;
-            if (FULL || (ok && p < m)) {
-                const int q = Bw ^ k;
-                const float o = ZOTH ? 0.f : D[q];
-                const float gs = NL ? nl_gs(Gs[q], (cur + vl) - o, ctl, inv_gw) : Gs[q];
-                r = line_residual_s<true, RES>(prev, cur, nxt, gs, o, vl, true, (FULL && k + 1 < SEG) || p + 1 < m);
+    switch (mode) {
+        case 4: cl_word_residual<LDM, 0, NL, true, true, FULL>(x, U, D, Gs, vin, nloc, m, inv_gw, ctl); break;
+        case 0: cl_word_residual<LDM, 0, NL, false, false, FULL>(x, U, D, Gs, vin, nloc, m, inv_gw, ctl); break;
+        case 3:
+            if constexpr (!NL) {  // (sinh cells never take the FP32 cell term)
+                cl_word_residual<LDM, 3, NL, false, false, FULL>(x, U, D, Gs, vin, nloc, m, inv_gw, ctl);
+                break;
             }
-            x[k] = r;
-            prev = cur;
-            cur = nxt;
-        }
+        case 2: cl_word_residual<LDM, 2, NL, false, false, FULL>(x, U, D, Gs, vin, nloc, m, inv_gw, ctl); break;
+        default: cl_word_residual<LDM, 1, NL, false, false, FULL>(x, U, D, Gs, vin, nloc, m, inv_gw, ctl); break;
     }
+    const bool zown = mode == 4;
     float c[SEG];
 #pragma unroll
     for (int k = 0; k < SEG; ++k) c[k] = cm[k * CL_T + tid];
@@ -257,7 +286,7 @@ __device__ __forceinline__ void cl_word_pass(float *__restrict__ U, const float 
     for (int k = 0; k < SEG; ++k) {
         if (FULL || (ok && p0 + k < m)) {
             const int q = Bw ^ k;
-            const float nv = ZOWN ? omega * x[k] : fmaf(omega, x[k], U[q]);
+            const float nv = zown ? omega * x[k] : fmaf(omega, x[k], U[q]);
             U[q] = nv;
             dm = fmaxf(dm, fabsf(x[k]));
             vmax = fmaxf(vmax, fabsf(nv));
@@ -266,10 +295,53 @@ __device__ __forceinline__ void cl_word_pass(float *__restrict__ U, const float 
     dmax = fmaxf(dmax, omega * dm);
 }
 
-// Bitline pass: columns cross the cluster.  Contains two cluster barriers.
-// ZOWN: the bitline plane (and so the halos) is known to be zero.
+// Residual of the bitline pass into x[] (columns cross the cluster; hup / hdn
+// the halo rows above and below the band).  ZOWN: the bitline plane (and so
+// the halos) is known to be zero.
 template <int LDM, int RES, bool NL, bool ZOWN, bool FULL>
-__device__ __forceinline__ void cl_bit_pass(cg::cluster_group &cluster, int rank, float *__restrict__ D,
+__device__ __forceinline__ void cl_bit_residual(float (&x)[CL_SEG], const float *__restrict__ D,
+                                                const float *__restrict__ U, const float *__restrict__ Gs,
+                                                const float *__restrict__ vin, const float *__restrict__ hup,
+                                                const float *__restrict__ hdn, int row0, int nloc, int m,
+                                                float inv_gw, const SolveCtl &ctl) {
+    constexpr int LPW = CCfg<LDM>::LPW_B, SEG = CL_SEG, V = CCfg<LDM>::V;
+    const int tid = threadIdx.x, lane = tid & 31, s = lane / LPW;
+    const int col = (tid >> 5) * LPW + (lane % LPW);  // < LDM by the shape
+    const bool ok = FULL || col < m;
+    const int p0 = s * SEG;  // first local row of the segment
+    int Rb[V];               // node p0 + k sits at Rb[k % V] + k * LDM
+#pragma unroll
+    for (int t = 0; t < V; ++t) Rb[t] = cswz<LDM>(p0 + t, col) - t * LDM;
+    auto qk = [&](int k) { return Rb[k % V] + k * LDM; };
+    float prev = ZOWN ? 0.f
+                      : ((p0 > 0) ? ((ok && (FULL || p0 - 1 < nloc)) ? D[cswz<LDM>(p0 - 1, col)] : 0.f)
+                                  : (ok ? hup[col] : 0.f));
+    float cur = (!ZOWN && ok && (FULL || p0 < nloc)) ? D[qk(0)] : 0.f;
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) {
+        const int lr = p0 + k;
+        float nxt = 0.f;
+        if (!ZOWN && ok)
+            nxt = ((FULL && k + 1 < SEG) || lr + 1 < nloc) ? D[k + 1 < SEG ? qk(k + 1) : cswz<LDM>(lr + 1, col)]
+                                                           : hdn[col];
+        float r = 0.f;
+        if (FULL || (ok && lr < nloc)) {
+            const int q = qk(k);
+            const float o = U[q];
+            const float gs = NL ? nl_gs(Gs[q], (o + vin[lr]) - cur, ctl, inv_gw) : Gs[q];
+            r = line_residual_s<false, RES>(prev, cur, nxt, gs, o, vin[lr], k > 0 || p0 > 0 || row0 > 0, true);
+        }
+        x[k] = r;
+        prev = cur;
+        cur = nxt;
+    }
+}
+
+// Bitline pass: the residual form selected by mode (as the wordline pass),
+// then one shared cross-cluster Thomas solve and update.  Contains two cluster
+// barriers.
+template <int LDM, bool NL, bool FULL>
+__device__ __forceinline__ void cl_bit_pass(int mode, cg::cluster_group &cluster, int rank, float *__restrict__ D,
                                             const float *__restrict__ U, const float *__restrict__ Gs,
                                             const float *__restrict__ vin, const float *__restrict__ cm,
                                             const float *__restrict__ segprod, const float *__restrict__ hup,
@@ -280,38 +352,26 @@ __device__ __forceinline__ void cl_bit_pass(cg::cluster_group &cluster, int rank
     constexpr int V = CCfg<LDM>::V;
     const int nloc = FULL ? CCfg<LDM>::RPC : nloc_in, m = FULL ? LDM : m_in;
     const int tid = threadIdx.x, lane = tid & 31, s = lane / LPW;
-    const int col = (tid >> 5) * LPW + (lane % LPW);  // < LDM by the shape
+    const int col = (tid >> 5) * LPW + (lane % LPW);
     const bool ok = FULL || col < m;
-    const int p0 = s * SEG;  // first local row of the segment
-    int Rb[V];               // node p0 + k sits at Rb[k % V] + k * LDM
+    const int p0 = s * SEG;
+    float x[SEG];
+    switch (mode) {
+        case 4: cl_bit_residual<LDM, 0, NL, true, FULL>(x, D, U, Gs, vin, hup, hdn, row0, nloc, m, inv_gw, ctl); break;
+        case 0: cl_bit_residual<LDM, 0, NL, false, FULL>(x, D, U, Gs, vin, hup, hdn, row0, nloc, m, inv_gw, ctl); break;
+        case 3:
+            if constexpr (!NL) {
+                cl_bit_residual<LDM, 3, NL, false, FULL>(x, D, U, Gs, vin, hup, hdn, row0, nloc, m, inv_gw, ctl);
+                break;
+            }
+        case 2: cl_bit_residual<LDM, 2, NL, false, FULL>(x, D, U, Gs, vin, hup, hdn, row0, nloc, m, inv_gw, ctl); break;
+        default: cl_bit_residual<LDM, 1, NL, false, FULL>(x, D, U, Gs, vin, hup, hdn, row0, nloc, m, inv_gw, ctl); break;
+    }
+    const bool zown = mode == 4;
+    int Rb[V];
 #pragma unroll
     for (int t = 0; t < V; ++t) Rb[t] = cswz<LDM>(p0 + t, col) - t * LDM;
     auto qk = [&](int k) { return Rb[k % V] + k * LDM; };
-    float x[SEG];
-    {
-        float prev = ZOWN ? 0.f
-                          : ((p0 > 0) ? ((ok && (FULL || p0 - 1 < nloc)) ? D[cswz<LDM>(p0 - 1, col)] : 0.f)
-                                      : (ok ? hup[col] : 0.f));
-        float cur = (!ZOWN && ok && (FULL || p0 < nloc)) ? D[qk(0)] : 0.f;
-#pragma unroll
-        for (int k = 0; k < SEG; ++k) {
-            const int lr = p0 + k;
-            float nxt = 0.f;
-            if (!ZOWN && ok)
-                nxt = ((FULL && k + 1 < SEG) || lr + 1 < nloc) ? D[k + 1 < SEG ? qk(k + 1) : cswz<LDM>(lr + 1, col)]
-                                                               : hdn[col];
-            float r = 0.f;
-            if (FULL || (ok && lr < nloc)) {
-                const int q = qk(k);
-                const float o = U[q];
-                const float gs = NL ? nl_gs(Gs[q], (o + vin[lr]) - cur, ctl, inv_gw) : Gs[q];
-                r = line_residual_s<false, RES>(prev, cur, nxt, gs, o, vin[lr], k > 0 || p0 > 0 || row0 > 0, true);
-            }
-            x[k] = r;
-            prev = cur;
-            cur = nxt;
-        }
-    }
     float c[SEG];
 #pragma unroll
     for (int k = 0; k < SEG; ++k) c[k] = cm[k * CL_T + tid];
@@ -347,7 +407,7 @@ __device__ __forceinline__ void cl_bit_pass(cg::cluster_group &cluster, int rank
         const int lr = p0 + k;
         if (FULL || (ok && lr < nloc)) {
             const int q = qk(k);
-            const float nv = ZOWN ? omega * x[k] : fmaf(omega, x[k], D[q]);
+            const float nv = zown ? omega * x[k] : fmaf(omega, x[k], D[q]);
             D[q] = nv;
             dm = fmaxf(dm, fabsf(x[k]));
             vmax = fmaxf(vmax, fabsf(nv));
@@ -566,7 +626,6 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
     // the compiler hoists a whole segment's loads and spills (measured); the
     // bitline pass, where the cross-band scans dominate, drops them.
     constexpr bool WFULL = false;
-    constexpr int LPW_B = CCfg<LDM>::LPW_B;
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     extern __shared__ float4 smem4[];
@@ -729,13 +788,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 omega_last = omega;
                 const int mode = zero ? 4 : (!res64 ? 0 : (semi ? 3 : (ff ? 2 : 1)));
                 const float *pW = piv, *sW = piv + 2 * SEG * CL_T;
-                switch (mode) {
-                    case 4: cl_word_pass<LDM, 0, NL, true, true, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    case 0: cl_word_pass<LDM, 0, NL, false, false, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    case 3: cl_word_pass<LDM, 3, NL, false, false, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    case 2: cl_word_pass<LDM, 2, NL, false, false, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    default: cl_word_pass<LDM, 1, NL, false, false, WFULL>(U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                }
+                cl_word_pass<LDM, NL, WFULL>(mode, U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl);
                 __syncthreads();
                 for (int j = tid; j < LDM; j += CL_T) {
                     // halo rows: the row above the band and the row below it (0 V ground below the last row)
@@ -747,13 +800,8 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 }
                 __syncthreads();
                 const float *pB = piv + SEG * CL_T, *sB = piv + 2 * SEG * CL_T + CL_T;
-                switch (mode) {
-                    case 4: cl_bit_pass<LDM, 0, NL, true, FULL>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    case 0: cl_bit_pass<LDM, 0, NL, false, FULL>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    case 3: cl_bit_pass<LDM, 3, NL, false, FULL>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    case 2: cl_bit_pass<LDM, 2, NL, false, FULL>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                    default: cl_bit_pass<LDM, 1, NL, false, FULL>(cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m, inv_gw, omega, dmax, vmax, a.ctl); break;
-                }
+                cl_bit_pass<LDM, NL, FULL>(mode, cluster, rank, D, U, Gs, vin, pB, sB, hup, hdn, aggF, aggB, row0, nloc, m,
+                                           inv_gw, omega, dmax, vmax, a.ctl);
                 zero = false;
                 dmax = warp_max(dmax);
                 vmax = warp_max(vmax);

@@ -83,7 +83,7 @@ __device__ __forceinline__ float line_residual_s(float prev, float cur, float nx
         const double lap = (has_l ? dp - dc : 0.0) + (has_r ? dn - dc : 0.0);  // exact: widened FP32 inputs
         return __double2float_rn(fma(widen_f64(gs), src, lap));
     } else if (RES == 2) {
-        float sh, sl, th, tl, lh, ll;
+        float sh, sl, th, tl, lh;
         two_sum(o, WORD ? -vin : vin, sh, sl);           // o -/+ vin
         two_sum(sh, -cur, th, tl);                        // ... - own
         float lap_lo;
