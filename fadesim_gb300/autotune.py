@@ -88,7 +88,10 @@ def tune(G, vin, g_wire=1 / 2.93, method="line", reps=3):
     T, n, m = G.shape
     B = vin.shape[0]
     best = None
+    losing = set()  # kernel layouts whose first setting already took twice the best time
     for kw in candidates(method, n, m):
+        if kw.get("kernel_ld") in losing:
+            continue
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         _, st, _ = _acc.ir_drop_gs_ex(vin, G, B, n, m, T, 1, g_wire=g_wire, method=method, **kw)
@@ -96,8 +99,11 @@ def tune(G, vin, g_wire=1 / 2.93, method="line", reps=3):
             continue
         torch.cuda.synchronize()
         # a setting whose first call (stats read back included) already took twice
-        # the best time so far cannot win: skip its timed repetitions
+        # the best time so far cannot win: skip its timed repetitions, and the
+        # other settings of its layout when the best is on another layout
         if best is not None and (time.perf_counter() - t0) * 1e3 > 2 * best[1]:
+            if "kernel_ld" in kw and kw["kernel_ld"] != best[0].get("kernel_ld"):
+                losing.add(kw["kernel_ld"])
             continue
         t0 = time.perf_counter()
         for _ in range(reps):

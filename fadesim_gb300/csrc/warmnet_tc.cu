@@ -2,28 +2,33 @@
 // (sm_103a): TMA tile loads, tcgen05.mma with the accumulator in tensor memory
 // (TMEM), BF16 operands, FP32 accumulation.
 //
-// Implicit GEMM, one CTA per 128-pixel output tile: M = 128 pixels (TMEM lanes),
-// N = Cout (TMEM columns), K = 9 taps x Cin in chunks of 32 channels.
-// * A (pixels x 32 channels of one tap): one 4-D TMA box (32 channels, W
-//   columns, 128 / W rows, 1 image) of the NHWC input at (c, dx, h0 + dy, n):
-//   the "same" padding comes from the TMA's zero fill of out-of-range
-//   coordinates (the channel coordinate, the only one with an alignment rule,
-//   is always a multiple of 32).  Rows of 64 bytes, 64-byte swizzle: the
-//   K-major operand layout of the MMA, 8-row groups 512 bytes apart.
-// * B (Cout x 32 channels of one tap): a 2-D TMA box of the weights viewed as
-//   [Cout][9 Cin], same layout.
-// * A six-stage ring of (A, B) buffers with full / empty mbarriers: thread 0
-//   (warp 0) issues the TMA loads, thread 32 (warp 1) the MMAs -- two
-//   K = 16 instructions per stage, the second with the descriptors advanced
-//   by 32 bytes -- and releases each stage with tcgen05.commit.
+// Implicit GEMM, one CTA per 128-pixel output tile of TW columns x TH rows
+// (TW = 16, TH = 8): M = 128 pixels (TMEM lanes), N = Cout (TMEM columns),
+// K = 9 taps x Cin in chunks of 32 channels.
+// * A: for every column shift dx and 32-channel chunk, one 4-D TMA box (32
+//   channels, TW columns, TH + 2 rows, 1 image) of the NHWC input at
+//   (c, w0 + dx, h0 - 1, n), so that the three row shifts dy of that dx are
+//   the same box read from row 0, 1 or 2: the input is fetched 3 x (TH + 2) / TH
+//   times instead of 9.  The "same" padding comes from the TMA's zero fill of
+//   out-of-range coordinates (the channel coordinate, the only one with an
+//   alignment rule, is always a multiple of 32).  Rows of 64 bytes, 64-byte
+//   swizzle: the K-major operand layout of the MMA, 8-row groups 512 bytes
+//   apart; a row shift moves the operand by TW rows (1 KB, whole swizzle
+//   atoms).
+// * B: the three taps (dy, dx) of the stage, each a 2-D TMA box (32 channels,
+//   Cout rows) of the weights viewed as [Cout][9 Cin], same layout.
+// * A ring of (A, 3 x B) stages with full / empty mbarriers: thread 0 (warp 0)
+//   issues the TMA loads, thread 32 (warp 1) the MMAs -- per tap two K = 16
+//   instructions, the second with the descriptors advanced by 32 bytes -- and
+//   releases each stage with tcgen05.commit.
 // * Epilogue: the four warps read their 32 TMEM lanes (tcgen05.ld 32x32b, 16
 //   columns at a time), add the bias, apply ReLU and the skip connection, and
-//   store BF16 (or FP32) NHWC rows.
+//   store BF16 (or FP32) NHWC pixels.
 // Every mbarrier wait is bounded (about a second of clock64); on expiry the
 // kernel records an error code, stops issuing, and still frees its TMEM.
 //
 // Shapes: Cin a multiple of 32, Cout a multiple of 16 up to 128, W a power of
-// two up to 128, H x W a multiple of 128 (the warm-start network's levels,
+// two from 16 to 128 and H a multiple of 8 (the warm-start network's levels
 // 128 x 128 down to 16 x 16).  Other shapes use the mma.sync kernel in
 // warmnet.cu.
 #include <cuda.h>
@@ -40,12 +45,15 @@ namespace fadesim {
 namespace {
 
 constexpr int TC_M = 128;          // pixels per tile = TMEM lanes
+constexpr int TC_TW = 16;          // tile columns
+constexpr int TC_TH = TC_M / TC_TW;  // tile rows
 constexpr int TC_KC = 32;          // channels per K chunk (64-byte rows)
-constexpr int TC_A_BYTES = TC_M * TC_KC * 2;   // 8 KB
-constexpr int TC_B_BYTES = 128 * TC_KC * 2;    // 8 KB (Cout <= 128)
-constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
+constexpr int TC_A_BYTES = (TC_TH + 2) * TC_TW * TC_KC * 2;  // 10 KB: the tile's rows and one above and below
+constexpr int TC_ROW_BYTES = TC_TW * TC_KC * 2;              // 1 KB: one row shift of the A operand
+// bytes of one stage: A and the three taps' B (Cout x 64 bytes each)
+__host__ __device__ constexpr int tc_stage_bytes(int Cout) { return TC_A_BYTES + 3 * Cout * TC_KC * 2; }
 // dynamic shared memory of a kernel with S stages
-constexpr int tc_smem(int S) { return S * TC_STAGE_BYTES + 1024 /* alignment */ + 256 /* barriers */; }
+constexpr int tc_smem(int S, int Cout) { return S * tc_stage_bytes(Cout) + 1024 /* alignment */ + 256 /* barriers */; }
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -142,8 +150,8 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// STAGES: depth of the TMA ring; fewer stages let more CTAs share an SM
-// (STAGES x 16 KB each), which hides the per-tile latency chain better.
+// STAGES: depth of the TMA ring; fewer stages let more CTAs share an SM,
+// which hides the per-tile latency chain better.
 template <int TC_STAGES>
 __global__ void __launch_bounds__(128, 1)
     conv3x3_fwd_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW,
@@ -153,18 +161,20 @@ __global__ void __launch_bounds__(128, 1)
     // stage buffers 1024-byte aligned in the shared window (the swizzle pattern
     // is a function of the shared-memory address)
     unsigned char *base = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
-    uint64_t *full = reinterpret_cast<uint64_t *>(base + TC_STAGES * TC_STAGE_BYTES);
+    const int SB = tc_stage_bytes(Cout);
+    const int BT = Cout * TC_KC * 2;  // bytes of one tap's B
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + TC_STAGES * SB);
     uint64_t *empty = full + TC_STAGES;
     uint64_t *done = empty + TC_STAGES;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
     __shared__ int s_fail;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const long long p0 = (long long)blockIdx.x * TC_M;  // first output pixel
-    const long long HW = (long long)H * W;
-    const int n = (int)(p0 / HW);
-    const int h0 = (int)((p0 % HW) / W);
-    const int kchunks = Cin / TC_KC, kiters = 9 * kchunks;
+    const int tiles_w = W / TC_TW, tiles_h = H / TC_TH;
+    const int n = (int)(blockIdx.x / (unsigned)(tiles_w * tiles_h));
+    const int t = (int)(blockIdx.x % (unsigned)(tiles_w * tiles_h));
+    const int h0 = (t / tiles_w) * TC_TH, w0 = (t % tiles_w) * TC_TW;
+    const int kchunks = Cin / TC_KC, kiters = 3 * kchunks;
     const uint32_t ncols = Cout <= 32 ? 32 : (Cout <= 64 ? 64 : 128);
 
     if (tid == 0) {
@@ -189,8 +199,8 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t tmem = *tmem_slot;
 
     if (tid == 0) {
-        // producer: TMA loads of A and B for every K step
-        const uint32_t tx = (uint32_t)(TC_A_BYTES + Cout * TC_KC * 2);
+        // producer: per (dx, chunk) the A box and the three taps' B
+        const uint32_t tx = (uint32_t)SB;
         for (int it = 0; it < kiters; ++it) {
             const int s = it % TC_STAGES;
             const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
@@ -198,15 +208,17 @@ __global__ void __launch_bounds__(128, 1)
                 atomicExch(&s_fail, 1);
                 break;
             }
-            const int tap = it / kchunks, c0 = (it % kchunks) * TC_KC;
-            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-            unsigned char *sa = base + s * TC_STAGE_BYTES;
+            const int dxi = it / kchunks, c0 = (it % kchunks) * TC_KC;
+            unsigned char *sa = base + s * SB;
             mbar_expect_tx(&full[s], tx);
-            tma_load_4d(sa, &tmX, c0, dx, h0 + dy, n, &full[s]);
-            tma_load_2d(sa + TC_A_BYTES, &tmW, tap * Cin + c0, 0, &full[s]);
+            tma_load_4d(sa, &tmX, c0, w0 + dxi - 1, h0 - 1, n, &full[s]);
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                tma_load_2d(sa + TC_A_BYTES + j * BT, &tmW, (j * 3 + dxi) * Cin + c0, 0, &full[s]);
         }
     } else if (tid == 32) {
-        // MMA issuer: two K = 16 steps per stage into the TMEM accumulator
+        // MMA issuer: per stage three taps (row shifts dy = -1, 0, 1 of the A
+        // box) of two K = 16 steps into the TMEM accumulator
         const uint32_t idesc = idesc_bf16(TC_M, Cout);
         bool ok = true;
         for (int it = 0; it < kiters; ++it) {
@@ -218,22 +230,27 @@ __global__ void __launch_bounds__(128, 1)
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t sa = smem_u32(base + s * TC_STAGE_BYTES);
+            const uint32_t sa = smem_u32(base + s * SB);
             const uint32_t sb = sa + TC_A_BYTES;
 #pragma unroll
-            for (int k = 0; k < TC_KC / 16; ++k)
-                umma_bf16(tmem, desc_sw64(sa + 32 * k), desc_sw64(sb + 32 * k), idesc, (it | k) ? 1u : 0u);
+            for (int j = 0; j < 3; ++j)
+#pragma unroll
+                for (int k = 0; k < TC_KC / 16; ++k)
+                    umma_bf16(tmem, desc_sw64(sa + j * TC_ROW_BYTES + 32 * k), desc_sw64(sb + j * BT + 32 * k), idesc,
+                              (it | j | k) ? 1u : 0u);
             umma_commit(&empty[s]);  // the stage is free once these MMAs have read it
         }
         if (ok) umma_commit(done);  // the accumulator is final once every MMA has completed
     }
     __syncwarp();
-    // epilogue: warp w owns TMEM lanes 32w .. 32w + 31 (pixels p0 + 32w + lane)
+    // epilogue: warp w owns TMEM lanes 32w .. 32w + 31 (two rows of the tile)
     const bool ready = __all_sync(0xffffffffu, mbar_wait(done, 0));
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!ready && lane == 0) atomicExch(&s_fail, 3);
     if (ready) {
-        const long long p = p0 + warp * 32 + lane;
+        // TMEM lane (tile pixel) r * TW + c holds output pixel (h0 + r, w0 + c)
+        const int L = warp * 32 + lane;
+        const long long p = ((long long)n * H + h0 + L / TC_TW) * W + w0 + (L % TC_TW);
         const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
         for (int j0 = 0; j0 < Cout; j0 += 16) {
             float v[16];
@@ -290,13 +307,14 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
 
 // TMA ring depth of the convolution (FADESIM_CONV_STAGES: 2, 3, 4 or 6).  A
 // CTA computes one 128-pixel tile, so the depth trades prefetch against how
-// many CTAs share an SM (shared memory: 4 at 3 stages, 2 at 6); 3 measured
-// fastest on every layer shape of the network.
+// many CTAs share an SM (a stage is 16 KB at Cout = 32, 34 KB at 128); 2
+// measured fastest on the network's layer shapes (3 within 2% on 96 -> 128
+// at 16 x 16).
 int conv_tc_stages() {
     static const int v = [] {
         const char *e = getenv("FADESIM_CONV_STAGES");
-        const int k = e ? atoi(e) : 3;
-        return (k == 2 || k == 3 || k == 4 || k == 6) ? k : 3;
+        const int k = e ? atoi(e) : 2;
+        return (k == 2 || k == 3 || k == 4 || k == 6) ? k : 2;
     }();
     return v;
 }
@@ -335,7 +353,7 @@ int *conv_tc_error_flag() {
 
 bool conv3x3_tc_supported(const void *X, const void *Wt, const void *Y, int H, int W, int Cin, int Cout) {
     if (Cin < TC_KC || Cin % TC_KC || Cout < 16 || Cout > 128 || Cout % 16) return false;
-    if (W < 1 || W > TC_M || (TC_M % W) || ((long long)H * W) % TC_M) return false;
+    if (W < TC_TW || W > TC_M || (W & (W - 1)) || H < TC_TH || H % TC_TH) return false;
     if ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(Wt) | reinterpret_cast<uintptr_t>(Y)) & 15)
         return false;
     return encode_fn() != nullptr;
@@ -350,7 +368,7 @@ cudaError_t conv3x3_fwd_tc(const void *X, const void *Wt, const float *bias, con
     CUtensorMap mx, mw;
     const cuuint64_t xdim[4] = {(cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
     const cuuint64_t xstr[3] = {(cuuint64_t)Cin * 2, (cuuint64_t)W * Cin * 2, (cuuint64_t)H * W * Cin * 2};
-    const cuuint32_t xbox[4] = {(cuuint32_t)TC_KC, (cuuint32_t)W, (cuuint32_t)(TC_M / W), 1};
+    const cuuint32_t xbox[4] = {(cuuint32_t)TC_KC, (cuuint32_t)TC_TW, (cuuint32_t)(TC_TH + 2), 1};
     const cuuint32_t ones[4] = {1, 1, 1, 1};
     if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(X), xdim, xstr, xbox, ones,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -363,15 +381,15 @@ cudaError_t conv3x3_fwd_tc(const void *X, const void *Wt, const float *bias, con
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return cudaErrorInvalidValue;
-    const long long tiles = (long long)N * H * W / TC_M;
+    const long long tiles = (long long)N * (H / TC_TH) * (W / TC_TW);
     if (tiles < 1) return cudaSuccess;
     const int stages = conv_tc_stages();
     void (*kern)(CUtensorMap, CUtensorMap, const float *, const __nv_bfloat16 *, void *, int, int, int, int, int,
-                 int *) = stages == 2   ? conv3x3_fwd_tc_kernel<2>
+                 int *) = stages == 3   ? conv3x3_fwd_tc_kernel<3>
                           : stages == 4 ? conv3x3_fwd_tc_kernel<4>
                           : stages == 6 ? conv3x3_fwd_tc_kernel<6>
-                                        : conv3x3_fwd_tc_kernel<3>;
-    const int smem = tc_smem(stages);
+                                        : conv3x3_fwd_tc_kernel<2>;
+    const int smem = tc_smem(stages, Cout);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     kern<<<(unsigned)tiles, 128, smem, st>>>(mx, mw, bias, static_cast<const __nv_bfloat16 *>(skip), Y, H, W, Cin,
@@ -394,4 +412,10 @@ extern "C" int fadesim_conv_tc_status(void *stream) {
         cudaStreamSynchronize(st);
     }
     return h;
+}
+
+extern "C" int fadesim_conv_tc_shape(int H, int Wd, int Cin, int Cout) {
+    static const __nv_bfloat16 probe[8] = {};  // any 16-byte-aligned address: only the shape is tested
+    const void *p = reinterpret_cast<const void *>((reinterpret_cast<uintptr_t>(probe) + 15) & ~(uintptr_t)15);
+    return fadesim::conv3x3_tc_supported(p, p, p, H, Wd, Cin, Cout) ? 1 : 0;
 }

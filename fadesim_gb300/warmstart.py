@@ -47,6 +47,7 @@ _SIGS = {
     "fadesim_mse_f32": "pppvliiv",
     "fadesim_adam_f32": "pvppplffffiv",
     "fadesim_conv_tc_status": "v",
+    "fadesim_conv_tc_shape": "iiii",
 }
 
 

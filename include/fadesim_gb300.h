@@ -280,14 +280,17 @@ int fadesim_ir_drop_gs_warm(int dtype, const void *input, const void *G, int bat
 /* Y = act(conv3x3(X, W) + bias) (+ skip): flags 1 = ReLU, 2 = add skip after
  * the activation, 4 = store FP32 instead of bf16, 8 = use the mma.sync kernel even where the
  * tensor-core kernel applies.  The tensor-core kernel (TMA loads, tcgen05.mma into tensor memory)
- * runs when Cin is a multiple of 32, Cout a multiple of 16, Wd a power of two up to 128, H * Wd a
- * multiple of 128 and the buffers 16-byte aligned; other shapes run on mma.sync. */
+ * runs when Cin is a multiple of 32, Cout a multiple of 16, Wd a power of two from 16 to 128, H a
+ * multiple of 8 and the buffers 16-byte aligned; other shapes run on mma.sync. */
 int fadesim_conv3x3_fwd_bf16(const void *X, const void *W, const float *bias, const void *skip, void *Y, int N,
                              int H, int Wd, int Cin, int Cout, int flags, void *stream);
 /* The tensor-core convolutions' error flag on the current device (0: none; 1-3: a bounded wait of
  * a launch expired -- a stage never freed / filled, the accumulator never completed), read after
  * the work queued on `stream` has finished, and cleared.  Negative: FADESIM_E_CUDA. */
 int fadesim_conv_tc_status(void *stream);
+/* 1 when fadesim_conv3x3_fwd_bf16 runs an H x Wd, Cin -> Cout convolution (16-byte aligned
+ * buffers, flag 8 clear) on the tensor-core kernel, else 0. */
+int fadesim_conv_tc_shape(int H, int Wd, int Cin, int Cout);
 /* dW[Cout][3][3][Cin] += sum over pixels of dY x X (FP32 accumulation with atomics: zero dW first). */
 int fadesim_conv3x3_wgrad_bf16(const void *dY, const void *X, float *dW, int N, int H, int Wd, int Cin, int Cout,
                                void *stream);

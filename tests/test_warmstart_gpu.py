@@ -63,10 +63,12 @@ def test_conv_kernels_match_torch(ws, cin, cout, H, W):
                                              (128, 96, 1, 64, 64), (64, 32, 3, 16, 16), (128, 16, 2, 32, 32)])
 def test_tensor_core_conv_matches_torch(ws, cin, cout, N, H, W):
     """The tcgen05 / TMA convolution (the network's shapes: Cin a multiple of
-    32, 128-pixel tiles of whole rows, "same" padding from the TMA zero fill)
-    against torch's FP32 convolution of the same bf16 operands and against the
-    mma.sync kernel; ReLU, skip connection and bf16 output in the epilogue; the
-    input gradient through the same kernel; no bounded wait expired."""
+    32, 16 x 8-pixel tiles whose input box serves all three row shifts, "same"
+    padding from the TMA zero fill) against torch's FP32 convolution of the
+    same bf16 operands and against the mma.sync kernel; ReLU, skip connection
+    and bf16 output in the epilogue; the input gradient through the same
+    kernel; no bounded wait expired."""
+    assert ws._k().fadesim_conv_tc_shape(H, W, cin, cout) == 1
     g = torch.Generator().manual_seed(cin * 7 + cout + H)
     x = bf(torch.randn((N, H, W, cin), generator=g)).cuda()
     conv = ws.Conv(cin, cout, g, "cuda")
