@@ -72,6 +72,13 @@ __device__ __forceinline__ float sinhc(float t) {
     return sinhf(t) / t;
 }
 
+// sinhc as a real call: the line kernels evaluate it once per node of a fully
+// unrolled 32-node segment, for two passes and up to three residual forms, and
+// inlined copies of the series push the sinh-cell kernels' code past the
+// instruction caches (38% of the 512 x 512 kernel's stall samples waited for
+// instructions; one shared copy: 41.5k -> 51.3k solves/s).
+static __device__ __noinline__ float sinhc_call(float t) { return sinhc(t); }
+
 // Chord conductance I(V)/V of the reference's sinh cell at cell voltage V for
 // a cell at position z between the on and off states:
 // 1/R(V), R(V) = (1-z) |V| / (b_on sinh(a_on |V|)) + z |V| / (b_off sinh(a_off |V|)),
@@ -79,7 +86,7 @@ __device__ __forceinline__ float sinhc(float t) {
 // evaluated as s_on s_off / ((1-z) r0_on s_off + z r0_off s_on) -- one division.
 __device__ __forceinline__ float nl_geff(float z, float V, const SolveCtl &c) {
     const float x = fabsf(V);
-    const float s_on = sinhc(c.nl_a_on * x), s_off = sinhc(c.nl_a_off * x);
+    const float s_on = sinhc_call(c.nl_a_on * x), s_off = sinhc_call(c.nl_a_off * x);
     return __fdividef(s_on * s_off, fmaf((1.f - z) * c.nl_r0_on, s_off, z * c.nl_r0_off * s_on));
 }
 
@@ -98,7 +105,7 @@ __device__ __forceinline__ float nl_cell(float g, const SolveCtl &c, float inv_g
 
 // Chord conductance over gw at cell voltage V, from the value nl_cell keeps.
 __device__ __forceinline__ float nl_gs(float cell, float V, const SolveCtl &c, float inv_gw) {
-    return c.nl_single_a ? cell * sinhc(c.nl_a_on * fabsf(V)) : nl_geff(cell, V, c) * inv_gw;
+    return c.nl_single_a ? cell * sinhc_call(c.nl_a_on * fabsf(V)) : nl_geff(cell, V, c) * inv_gw;
 }
 
 // Chord conductance at cell voltage V, from the value nl_cell keeps.

@@ -82,12 +82,18 @@ int family_gs_nonlinear(int dtype, const void *input, const void *G, int B, int 
 
 // Tensor-core 3x3 convolution of the warm-start network (warmnet_tc.cu): TMA
 // loads, tcgen05.mma into TMEM.  conv3x3_tc_supported: Cin a multiple of 32,
-// Cout a multiple of 16 up to 128, W a power of two up to 128, H x W a multiple
-// of 128, 16-byte aligned buffers.  err: device flag set when a bounded wait
+// Cout a multiple of 16 up to 128, W a power of two from 16 to 128, H a
+// multiple of 8, 16-byte aligned buffers.  err: device flag set when a bounded wait
 // expires (conv_tc_error_flag: the library's own, per device).
 bool conv3x3_tc_supported(const void *X, const void *Wt, const void *Y, int H, int W, int Cin, int Cout);
 cudaError_t conv3x3_fwd_tc(const void *X, const void *Wt, const float *bias, const void *skip, void *Y, int N, int H,
                            int W, int Cin, int Cout, int flags, int *err, cudaStream_t st);
 int *conv_tc_error_flag();
+// Tensor-core weight gradient dW[Cout][9][Cin] += (FP32 atomics): Cin and Cout
+// multiples of 32, Cout <= 128, W a power of two from 16 to 128, H a multiple
+// of 8, 16-byte aligned activations.
+bool conv3x3_wgrad_tc_supported(const void *dY, const void *X, int H, int W, int Cin, int Cout);
+cudaError_t conv3x3_wgrad_tc(const void *dY, const void *X, float *dW, int N, int H, int W, int Cin, int Cout,
+                             int *err, cudaStream_t st);
 
 }  // namespace fadesim

@@ -334,6 +334,11 @@ extern "C" int fadesim_conv3x3_fwd_bf16(const void *X, const void *W, const floa
 extern "C" int fadesim_conv3x3_wgrad_bf16(const void *dY, const void *X, float *dW, int N, int H, int Wd, int Cin,
                                           int Cout, void *stream) {
     if (!dY || !X || !dW || Cout > 128 || Cin < 1) return FADESIM_E_ARG;
+    if (fadesim::conv3x3_wgrad_tc_supported(dY, X, H, Wd, Cin, Cout)) {
+        const cudaError_t e = fadesim::conv3x3_wgrad_tc(dY, X, dW, N, H, Wd, Cin, Cout, fadesim::conv_tc_error_flag(),
+                                                        (cudaStream_t)stream);
+        return e == cudaSuccess ? FADESIM_OK : FADESIM_E_CUDA;
+    }
     const long long P = (long long)N * H * Wd;
     long long chunk = 1024;
     long long nchunks = (P + chunk - 1) / chunk;

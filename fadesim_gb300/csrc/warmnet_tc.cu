@@ -299,6 +299,159 @@ __global__ void __launch_bounds__(128, 1)
     if (tid == 0 && s_fail && err) atomicExch(err, s_fail);
 }
 
+// ---- weight gradient ---------------------------------------------------------
+// dW[co][tap][ci] += sum over pixels p of dY[p][co] X[p + tap][ci]: a GEMM with
+// M = Cout (TMEM lanes), N = 32 input channels per CTA, K = pixels, one FP32
+// accumulator of 32 TMEM columns per tap (9 x 32 = 288 of 512).  Both operands
+// are the NHWC activations as TMA loads them, read MN-major (channels
+// contiguous): per 16 x 8-pixel tile, A = dY in 32-channel boxes (32 x 128
+// pixels, 8 KB, boxes LBO = 8 KB apart along M) and B = X in three boxes, one
+// per column shift dx, of the tile's rows and one above and below (32 x 160
+// pixels, 10 KB); the tap's row shift dy is the B box read from row dy, and a
+// K = 16 step is one tile row -- both whole-atom offsets (1 KB) of the 64-byte
+// swizzle.  Each CTA sums a run of tiles (split-K) for one 32-channel slice of
+// Cin and adds its accumulators to dW with FP32 atomics.
+constexpr int WG_AG_BYTES = TC_M * TC_KC * 2;                  // one 32-channel dY box: 8 KB
+constexpr int WG_A_BYTES = 4 * WG_AG_BYTES;                     // Cout <= 128
+constexpr int WG_B_BYTES = (TC_TH + 2) * TC_TW * TC_KC * 2;     // one X box: 10 KB
+constexpr int WG_STAGE_BYTES = WG_A_BYTES + 3 * WG_B_BYTES;     // 62 KB
+constexpr int WG_STAGES = 3;
+constexpr int WG_SMEM = WG_STAGES * WG_STAGE_BYTES + 1024 /* alignment */ + 256 /* barriers */;
+constexpr uint32_t WG_COLS = 512;                               // 9 taps x 32 columns, rounded to a power of two
+
+// Shared-memory descriptor of an MN-major operand in the 64-byte swizzle: rows
+// of 64 bytes hold 32 consecutive M (or N) elements, consecutive K elements are
+// consecutive rows (8-row groups 512 bytes apart), and blocks of 32 M elements
+// lie lbo bytes apart.
+__device__ __forceinline__ uint64_t desc_mn_sw64(uint32_t saddr, uint32_t lbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)(512 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)4 << 61;
+    return d;
+}
+
+__global__ void __launch_bounds__(128, 1)
+    conv3x3_wgrad_tc_kernel(const __grid_constant__ CUtensorMap tmY, const __grid_constant__ CUtensorMap tmX,
+                            float *__restrict__ dW, int H, int W, int Cin, int Cout, long long tiles,
+                            int tiles_per_cta, int *err) {
+    extern __shared__ unsigned char tc_smem_raw[];
+    unsigned char *base = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
+    uint64_t *full = reinterpret_cast<uint64_t *>(base + WG_STAGES * WG_STAGE_BYTES);
+    uint64_t *empty = full + WG_STAGES;
+    uint64_t *done = empty + WG_STAGES;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + 1);
+    __shared__ int s_fail;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ci0 = (int)blockIdx.y * TC_KC;
+    const long long t0 = (long long)blockIdx.x * tiles_per_cta;
+    const int nt = (int)min((long long)tiles_per_cta, tiles - t0);  // >= 1 by the grid
+    const int tiles_w = W / TC_TW, tiles_img = tiles_w * (H / TC_TH);
+    const int groups = Cout / TC_KC;
+
+    if (tid == 0) {
+        s_fail = 0;
+        for (int s = 0; s < WG_STAGES; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(WG_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (tid == 0) {
+        // producer: per tile the dY boxes of every 32 output channels and the
+        // three column-shifted X boxes of this CTA's 32 input channels
+        const uint32_t tx = (uint32_t)(groups * WG_AG_BYTES + 3 * WG_B_BYTES);
+        for (int i = 0; i < nt; ++i) {
+            const int s = i % WG_STAGES;
+            const uint32_t ph = (uint32_t)(i / WG_STAGES) & 1u;
+            if (!mbar_wait(&empty[s], ph ^ 1u)) {
+                atomicExch(&s_fail, 1);
+                break;
+            }
+            const long long t = t0 + i;
+            const int n = (int)(t / tiles_img), r = (int)(t % tiles_img);
+            const int h0 = (r / tiles_w) * TC_TH, w0 = (r % tiles_w) * TC_TW;
+            unsigned char *sa = base + s * WG_STAGE_BYTES;
+            mbar_expect_tx(&full[s], tx);
+            for (int g = 0; g < groups; ++g) tma_load_4d(sa + g * WG_AG_BYTES, &tmY, g * TC_KC, w0, h0, n, &full[s]);
+#pragma unroll
+            for (int dx = 0; dx < 3; ++dx)
+                tma_load_4d(sa + WG_A_BYTES + dx * WG_B_BYTES, &tmX, ci0, w0 + dx - 1, h0 - 1, n, &full[s]);
+        }
+    } else if (tid == 32) {
+        // MMA issuer: 9 taps x 8 K = 16 steps (tile rows) per tile
+        const uint32_t idesc = idesc_bf16(TC_M, TC_KC) | (1u << 15) | (1u << 16);  // A and B MN-major
+        bool ok = true;
+        for (int i = 0; i < nt; ++i) {
+            const int s = i % WG_STAGES;
+            const uint32_t ph = (uint32_t)(i / WG_STAGES) & 1u;
+            if (!mbar_wait(&full[s], ph)) {
+                atomicExch(&s_fail, 2);
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t sa = smem_u32(base + s * WG_STAGE_BYTES);
+            const uint32_t sb = sa + WG_A_BYTES;
+#pragma unroll
+            for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+                for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+                    for (int k = 0; k < TC_TH; ++k)
+                        umma_bf16(tmem + (uint32_t)((dy * 3 + dx) * TC_KC),
+                                  desc_mn_sw64(sa + k * TC_ROW_BYTES, WG_AG_BYTES),
+                                  desc_mn_sw64(sb + dx * WG_B_BYTES + (dy + k) * TC_ROW_BYTES, 16), idesc,
+                                  (i | k) ? 1u : 0u);
+            umma_commit(&empty[s]);
+        }
+        if (ok) umma_commit(done);
+    }
+    __syncwarp();
+    const bool ready = __all_sync(0xffffffffu, mbar_wait(done, 0));
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!ready && lane == 0) atomicExch(&s_fail, 3);
+    if (ready) {
+        // warp w reads TMEM lanes 32w .. 32w + 31: output channels co
+        const int co = warp * 32 + lane;
+        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int tap = 0; tap < 9; ++tap)
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                float v[16];
+                tmem_ld16(lane_base + (uint32_t)(tap * TC_KC + half * 16), v);
+                if (co < Cout) {
+                    float *d = dW + ((long long)co * 9 + tap) * Cin + ci0 + half * 16;
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) atomicAdd(d + q, v[q]);
+                }
+            }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(WG_COLS) : "memory");
+    }
+    if (tid == 0 && s_fail && err) atomicExch(err, s_fail);
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link
 // against the driver library).
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -397,6 +550,54 @@ cudaError_t conv3x3_fwd_tc(const void *X, const void *Wt, const float *bias, con
     return cudaGetLastError();
 }
 
+
+bool conv3x3_wgrad_tc_supported(const void *dY, const void *X, int H, int W, int Cin, int Cout) {
+    if (Cin < TC_KC || Cin % TC_KC || Cout < TC_KC || Cout > 128 || Cout % TC_KC) return false;
+    if (W < TC_TW || W > TC_M || (W & (W - 1)) || H < TC_TH || H % TC_TH) return false;
+    if ((reinterpret_cast<uintptr_t>(dY) | reinterpret_cast<uintptr_t>(X)) & 15) return false;
+    return encode_fn() != nullptr;
+}
+
+// The tensor-core weight gradient (dW += ...); assumes conv3x3_wgrad_tc_supported.
+cudaError_t conv3x3_wgrad_tc(const void *dY, const void *X, float *dW, int N, int H, int W, int Cin, int Cout,
+                             int *err, cudaStream_t st) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    CUtensorMap my, mx;
+    const cuuint32_t ones[4] = {1, 1, 1, 1};
+    const cuuint64_t ydim[4] = {(cuuint64_t)Cout, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+    const cuuint64_t ystr[3] = {(cuuint64_t)Cout * 2, (cuuint64_t)W * Cout * 2, (cuuint64_t)H * W * Cout * 2};
+    const cuuint32_t ybox[4] = {(cuuint32_t)TC_KC, (cuuint32_t)TC_TW, (cuuint32_t)TC_TH, 1};
+    if (enc(&my, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(dY), ydim, ystr, ybox, ones,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const cuuint64_t xdim[4] = {(cuuint64_t)Cin, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+    const cuuint64_t xstr[3] = {(cuuint64_t)Cin * 2, (cuuint64_t)W * Cin * 2, (cuuint64_t)H * W * Cin * 2};
+    const cuuint32_t xbox[4] = {(cuuint32_t)TC_KC, (cuuint32_t)TC_TW, (cuuint32_t)(TC_TH + 2), 1};
+    if (enc(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(X), xdim, xstr, xbox, ones,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return cudaErrorInvalidValue;
+    const long long tiles = (long long)N * (H / TC_TH) * (W / TC_TW);
+    if (tiles < 1) return cudaSuccess;
+    // one CTA per SM (shared memory and TMEM): split the tiles so that the
+    // Cin / 32 channel slices together fill the SMs
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        return cudaErrorInvalidValue;
+    const int slices = Cin / TC_KC;
+    const long long want = max(1, sms / slices);
+    const long long per = (tiles + want - 1) / want;
+    const long long splits = (tiles + per - 1) / per;  // every CTA gets at least one tile
+    cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, WG_SMEM);
+    if (e != cudaSuccess) return e;
+    conv3x3_wgrad_tc_kernel<<<dim3((unsigned)splits, (unsigned)slices), 128, WG_SMEM, st>>>(
+        my, mx, dW, H, W, Cin, Cout, tiles, (int)per, err);
+    return cudaGetLastError();
+}
+
 }  // namespace fadesim
 
 extern "C" int fadesim_conv_tc_status(void *stream) {
@@ -417,5 +618,6 @@ extern "C" int fadesim_conv_tc_status(void *stream) {
 extern "C" int fadesim_conv_tc_shape(int H, int Wd, int Cin, int Cout) {
     static const __nv_bfloat16 probe[8] = {};  // any 16-byte-aligned address: only the shape is tested
     const void *p = reinterpret_cast<const void *>((reinterpret_cast<uintptr_t>(probe) + 15) & ~(uintptr_t)15);
-    return fadesim::conv3x3_tc_supported(p, p, p, H, Wd, Cin, Cout) ? 1 : 0;
+    return (fadesim::conv3x3_tc_supported(p, p, p, H, Wd, Cin, Cout) ? 1 : 0) |
+           (fadesim::conv3x3_wgrad_tc_supported(p, p, H, Wd, Cin, Cout) ? 2 : 0);
 }

@@ -127,8 +127,23 @@ def conv_throughput(N=64, H=128, W=128, cin=64, cout=32, reps=10, legacy=False):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     flops = 2.0 * 9 * cin * cout * N * H * W
-    return {"kernel": "mma.sync" if legacy else "tcgen05+TMA", "shape": "N%d %dx%d %d->%d" % (N, H, W, cin, cout),
-            "ms": ms, "tflops": flops / (ms / 1e3) / 1e12}
+    out = {"kernel": "mma.sync" if legacy else "tcgen05+TMA", "shape": "N%d %dx%d %d->%d" % (N, H, W, cin, cout),
+           "ms": ms, "tflops": flops / (ms / 1e3) / 1e12}
+    if not legacy:
+        # the weight gradient of the same layer (tensor cores where Cin and Cout are multiples of 32)
+        dy = torch.randn((N, H, W, cout), generator=g).to(torch.bfloat16).cuda()
+        for _ in range(2):
+            conv.bwd(dy, x, need_dx=False)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            conv.bwd(dy, x, need_dx=False)
+        e1.record()
+        torch.cuda.synchronize()
+        wms = e0.elapsed_time(e1) / reps
+        out.update({"wgrad_tc": bool(ws._k().fadesim_conv_tc_shape(H, W, cin, cout) & 2), "wgrad_ms": wms,
+                    "wgrad_tflops": flops / (wms / 1e3) / 1e12})
+    return out
 
 
 def main():

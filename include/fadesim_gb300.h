@@ -288,10 +288,14 @@ int fadesim_conv3x3_fwd_bf16(const void *X, const void *W, const float *bias, co
  * a launch expired -- a stage never freed / filled, the accumulator never completed), read after
  * the work queued on `stream` has finished, and cleared.  Negative: FADESIM_E_CUDA. */
 int fadesim_conv_tc_status(void *stream);
-/* 1 when fadesim_conv3x3_fwd_bf16 runs an H x Wd, Cin -> Cout convolution (16-byte aligned
- * buffers, flag 8 clear) on the tensor-core kernel, else 0. */
+/* Which parts of an H x Wd, Cin -> Cout convolution run on the tensor-core kernels (16-byte
+ * aligned buffers): bit 0 fadesim_conv3x3_fwd_bf16 (flag 8 clear), bit 1
+ * fadesim_conv3x3_wgrad_bf16 (Cin and Cout multiples of 32 as well). */
 int fadesim_conv_tc_shape(int H, int Wd, int Cin, int Cout);
-/* dW[Cout][3][3][Cin] += sum over pixels of dY x X (FP32 accumulation with atomics: zero dW first). */
+/* dW[Cout][3][3][Cin] += sum over pixels of dY x X (FP32 accumulation with atomics: zero dW first).
+ * On the tensor cores (tcgen05, MN-major operands straight from the NHWC activations) when Cin and
+ * Cout are multiples of 32, Cout <= 128, Wd a power of two from 16 to 128 and H a multiple of 8;
+ * mma.sync otherwise. */
 int fadesim_conv3x3_wgrad_bf16(const void *dY, const void *X, float *dW, int N, int H, int Wd, int Cin, int Cout,
                                void *stream);
 /* Wf[ci][8 - tap][co] = W[co][tap][ci], ci padded to Cin_pad8: the weights of the input-gradient convolution. */

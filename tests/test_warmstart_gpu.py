@@ -67,8 +67,10 @@ def test_tensor_core_conv_matches_torch(ws, cin, cout, N, H, W):
     padding from the TMA zero fill) against torch's FP32 convolution of the
     same bf16 operands and against the mma.sync kernel; ReLU, skip connection
     and bf16 output in the epilogue; the input gradient through the same
-    kernel; no bounded wait expired."""
-    assert ws._k().fadesim_conv_tc_shape(H, W, cin, cout) == 1
+    kernel; the weight gradient on the tensor-core kernel (MN-major operands)
+    where Cout is a multiple of 32; no bounded wait expired."""
+    tc = ws._k().fadesim_conv_tc_shape(H, W, cin, cout)
+    assert tc & 1 and bool(tc & 2) == (cout % 32 == 0)  # forward / weight gradient on the tensor cores
     g = torch.Generator().manual_seed(cin * 7 + cout + H)
     x = bf(torch.randn((N, H, W, cin), generator=g)).cuda()
     conv = ws.Conv(cin, cout, g, "cuda")
@@ -90,6 +92,8 @@ def test_tensor_core_conv_matches_torch(ws, cin, cout, N, H, W):
     dx = conv.bwd(dy, x)
     dx_ref = torch.nn.grad.conv2d_input((N, cin, H, W), wr, nchw(dy), padding=1)
     assert rel(nchw(dx), dx_ref) < 1e-2
+    dw_ref = torch.nn.grad.conv2d_weight(nchw(x), wr.shape, nchw(dy), padding=1)
+    assert rel(conv.gw.cpu().permute(0, 3, 1, 2), dw_ref) < 1e-4
     assert ws._k().fadesim_conv_tc_status(stream) == 0
 
 
