@@ -467,7 +467,11 @@ def run_ours(args):
                 "weak_cells": train_and_evaluate(size=ROWS, train_instances=200000, batch=64, infer=8192,
                                                  cells="weak"),
                 "strong_cells": train_and_evaluate(size=ROWS, train_instances=65536, batch=64, infer=8192,
-                                                   cells="strong")}
+                                                   cells="strong"),
+                # the large non-ideal setting: 512 x 512 sinh cells with variation, on the
+                # cluster kernels (the network is fully convolutional: any tile size)
+                "sinh_cells_512": train_and_evaluate(size=512, train_instances=4096, batch=8, infer=512,
+                                                     cells="sinh", sor_omegas=())}
 
     # the plain red-black SOR kernel on a bounded sample of the same workload
     nps = 256

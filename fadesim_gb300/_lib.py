@@ -40,8 +40,8 @@ EXPORTS = {
                               ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _vp, _vp],
     "fadesim_ir_drop_gs_host": [_i, _vp, _vp, _i, _i, _i, _i, _i, _i, _d, _d, _i, _d, _i, _vp, _i, _i, _vp,
                                 ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _i, _vp],
-    "fadesim_ir_drop_gs_warm": [_i, _vp, _vp, _i, _i, _i, _i, _i, _d, _vp, _vp, ctypes.POINTER(SolveOpts),
-                                ctypes.POINTER(SolveStats), _vp, _vp],
+    "fadesim_ir_drop_gs_warm": [_i, _vp, _vp, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _vp,
+                                ctypes.POINTER(SolveOpts), ctypes.POINTER(SolveStats), _vp, _vp],
     "fadesim_release_memory": [],
     "fadesim_last_error": [],
     "fadesim_version": [],

@@ -354,10 +354,12 @@ def ir_gs_ou(input, G, batch_size, row_size, col_size, ou_row_size, ou_col_size,
 
 
 def ir_drop_gs_warm(input, G, batch_size, row_size, col_size, numX, numY, init, g_wire=1 / 2.93, tol_v=None,
-                    residual=None, return_iters=False, method="line", omega=None):
+                    residual=None, return_iters=False, method="line", omega=None, nonlinear_params=None,
+                    read_noise_sigma=None, noise_seed=None):
     """Line solve from given initial planes ``init`` [batch, numX, numY, 2, rows, cols]
     (FP32 wordline deviations u - vin and bitline voltages d, e.g. a learned
-    prediction).  Returns (currents, stats, iters)."""
+    prediction), any tile size up to 512 x 512; ``nonlinear_params`` (the six
+    sinh-cell parameters) for sinh cells.  Returns (currents, stats, iters)."""
     _check_input(input, "input")
     _check_input(G, "G")
     _check_input(init, "init")
@@ -370,6 +372,13 @@ def ir_drop_gs_warm(input, G, batch_size, row_size, col_size, numX, numY, init, 
         o.residual = residual
     if omega is not None:
         o.omega = omega
+    if read_noise_sigma is not None:
+        o.read_noise_sigma = read_noise_sigma
+    if noise_seed is not None:
+        o.noise_seed = noise_seed
+    if nonlinear_params is not None and len(nonlinear_params) != 6:
+        raise RuntimeError("nonlinear_params: [R_on, R_off, a_on, b_on, a_off, b_off]")
+    nl = (ctypes.c_double * 6)(*[float(v) for v in nonlinear_params]) if nonlinear_params is not None else None
     out = torch.empty((batch_size, numX, numY * col_size), dtype=input.dtype, device=input.device)
     iters = torch.empty((batch_size, numX, numY), dtype=torch.int32, device=input.device) if return_iters else None
     st = _lib.SolveStats()
@@ -377,8 +386,9 @@ def ir_drop_gs_warm(input, G, batch_size, row_size, col_size, numX, numY, init, 
     with torch.cuda.device(input.device):
         rc = lib.fadesim_ir_drop_gs_warm(_lib.F64 if input.dtype == torch.float64 else _lib.F32, input.data_ptr(),
                                          G.data_ptr(), batch_size, row_size, col_size, numX, numY, float(g_wire),
-                                         init.data_ptr(), out.data_ptr(), ctypes.byref(o.to_c(method)),
-                                         ctypes.byref(st), iters.data_ptr() if return_iters else None,
+                                         init.data_ptr(), 1 if nl is not None else 0, nl, 6 if nl is not None else 0,
+                                         out.data_ptr(), ctypes.byref(o.to_c(method)), ctypes.byref(st),
+                                         iters.data_ptr() if return_iters else None,
                                          torch.cuda.current_stream(input.device).cuda_stream)
     _lib.check(rc)
     return out, dict(solves=int(st.solves), iters_sum=int(st.iters_sum), iters_max=int(st.iters_max),

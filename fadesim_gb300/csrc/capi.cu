@@ -172,7 +172,6 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
             if (L > want) return fail(FADESIM_E_ARG, "kernel_ld is smaller than the tile");
             ld = want <= 128 ? want : 0;
             cld = want > 128 ? want : 0;
-            if (a.init && cld) return fail(FADESIM_E_UNSUPPORTED, "warm starts run on the single-CTA layouts");
         }
         a.ctl.max_iters = (opts && opts->max_iters > 0) ? opts->max_iters : 400;
         a.ctl.omega = (opts && opts->omega > 0) ? (float)opts->omega : 0.f;
@@ -208,8 +207,9 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
                 return fail(FADESIM_E_ARG, "kernel_ld must be 0, 128, 256 or 512 for red-black SOR");
             if (L > want) return fail(FADESIM_E_ARG, "kernel_ld is smaller than the tile");
             cld = want > 128 ? want : 0;
-            if (a.init && cld) return fail(FADESIM_E_UNSUPPORTED, "warm starts run on the single-CTA layouts");
         }
+        if (a.init && cld)
+            return fail(FADESIM_E_UNSUPPORTED, "red-black SOR starts from given planes on tiles up to 128 x 128");
         if (!cld) {
             CUDA_TRY(rbsor_prepare(dtype));
             grid = sms;
@@ -336,8 +336,7 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
     a.iters_out = per_solve_iters;
     a.init = g_warm_init;
     a.f64 = dtype == FADESIM_F64 ? 1 : 0;
-    if (a.init && (ret_V == 1 || !line_relax_ld(row_size, col_size)))
-        return fail(FADESIM_E_UNSUPPORTED, "warm starts apply to tiles up to 128 x 128");
+    if (a.init && ret_V == 1) return fail(FADESIM_E_UNSUPPORTED, "warm starts return currents or both planes");
     if (nonlinear_cell_enable) {
         const double *q = nonlinear_params;
         a.ctl.nl = 1;
@@ -422,9 +421,10 @@ extern "C" int fadesim_ir_drop_gs_f64(const double *input, const double *G, int 
 }
 
 extern "C" int fadesim_ir_drop_gs_warm(int dtype, const void *input, const void *G, int batch_size, int row_size,
-                                       int col_size, int numX, int numY, double g_wire, const float *init, void *out,
-                                       const fadesim_solve_opts *opts, fadesim_solve_stats *stats,
-                                       int *per_solve_iters, void *stream) {
+                                       int col_size, int numX, int numY, double g_wire, const float *init,
+                                       int nonlinear_cell_enable, const double *nonlinear_params,
+                                       int n_nonlinear_params, void *out, const fadesim_solve_opts *opts,
+                                       fadesim_solve_stats *stats, int *per_solve_iters, void *stream) {
     if (!init) return fail(FADESIM_E_ARG, "init planes required");
     fadesim_solve_opts o = opts ? *opts : fadesim_solve_opts{};
     if (o.method == FADESIM_METHOD_AUTO) o.method = FADESIM_METHOD_LINE;
@@ -432,7 +432,8 @@ extern "C" int fadesim_ir_drop_gs_warm(int dtype, const void *input, const void 
         return fail(FADESIM_E_UNSUPPORTED, "warm starts apply to the line and red-black SOR methods");
     g_warm_init = init;
     const int rc = fadesim_ir_drop_gs_ex(dtype, input, G, batch_size, row_size, col_size, numX, numY, 0, g_wire, 1.0,
-                                         0, 0.0, 0, nullptr, 0, 0, out, &o, stats, per_solve_iters, stream);
+                                         0, 0.0, nonlinear_cell_enable, nonlinear_params, n_nonlinear_params, 0, out,
+                                         &o, stats, per_solve_iters, stream);
     g_warm_init = nullptr;
     return rc;
 }

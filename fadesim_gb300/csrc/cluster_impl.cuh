@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
     float *red = aux + 8 * LDM;     // [2][2][CL_NW]
     float *cred = red + 4 * CL_NW;  // [2][2] this CTA's maxima, read by the cluster
     float *aggF = aux, *aggB = aux + 2 * LDM, *part = aux + 4 * LDM;
-    __shared__ unsigned long long st_solves, st_iters;
+    __shared__ unsigned long long st_solves, st_iters, st_rej;
     __shared__ int st_max, st_or, nonfinite_flag;
     __shared__ float bmax_scratch[CL_NW];
     __shared__ float band_gsmax, band_vmax;  // this CTA's maxima, read by the cluster
@@ -660,6 +660,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
     if (tid == 0) {
         st_solves = 0;
         st_iters = 0;
+        st_rej = 0;
         st_max = 0;
         st_or = 0;
     }
@@ -743,9 +744,20 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             // neither plane nor the halos, so they need no clearing -- unless every
             // iteration must be precise (then they are cleared).  (Clearing them for
             // sinh cells too, so that two pass bodies alternate instead of three,
-            // measured 2% slower on the 512x512 sinh-cell workload.)
-            bool zero = !precise_first;
-            if (precise_first) {
+            // measured 2% slower on the 512x512 sinh-cell workload.)  A warm start
+            // loads this band's rows of the initial deviation planes [2][n][m].
+            bool warm = a.init != nullptr;
+            bool zero = !warm && !precise_first;
+            if (warm) {
+                const float *w0 = a.init + (((size_t)b * a.numX + x) * a.numY + y) * 2 * n * m;
+                for (int e = tid; e < RPC * LDM; e += CL_T) {
+                    const int lr = e / LDM, c = e - lr * LDM;
+                    const bool in = lr < nloc && c < m;
+                    const size_t o = (size_t)(row0 + lr) * m + c;
+                    U[cswz<LDM>(lr, c)] = in ? w0[o] : 0.f;
+                    D[cswz<LDM>(lr, c)] = in ? w0[(size_t)n * m + o] : 0.f;
+                }
+            } else if (precise_first) {
                 for (int e = tid; e < RPC * LDM; e += CL_T) {
                     U[e] = 0.f;
                     D[e] = 0.f;
@@ -836,14 +848,33 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 ++it;
                 if (!isfinite(delta) || !isfinite(vm)) {
                     // the same cluster-wide values in every CTA: every CTA leaves here
-                    status = FADESIM_ST_NONFINITE;
+                    status |= FADESIM_ST_NONFINITE;
                     break;
+                }
+                if (warm && it == 1 && !(delta < vm)) {
+                    // the prediction moved as much as the solution is large: discard
+                    // it and start again from the ideal state (cluster-uniform)
+                    if (precise_first) {
+                        __syncthreads();
+                        for (int e = tid; e < RPC * LDM; e += CL_T) {
+                            U[e] = 0.f;
+                            D[e] = 0.f;
+                        }
+                    }
+                    cluster.sync();  // every band restarted before any halo is read again
+                    zero = !precise_first;
+                    warm = false;
+                    status |= FADESIM_ST_WARM_REJECTED;
+                    stop.init(a.ctl.omega, rate_hint, omega_prev);
+                    omega = stop.omega;
+                    res64 = precise_first;
+                    continue;
                 }
                 const bool small = stop.update(delta, vm, tol);
                 omega = stop.omega;
                 if (small) {
                     if (res64 || kres < 0) {
-                        status = FADESIM_ST_CONVERGED;
+                        status |= FADESIM_ST_CONVERGED;
                         break;
                     }
                     res64 = true;
@@ -851,7 +882,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                     res64 = kres > 0 ? (it % kres == 0) : (kres == 0 && stop.want_precise(tol, vm, a.ctl.precise_margin));
                 }
                 if (it >= maxit) {
-                    status = FADESIM_ST_MAXITER;
+                    status |= FADESIM_ST_MAXITER;
                     break;
                 }
             }
@@ -891,6 +922,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 st_solves += 1;
                 st_iters += it;
                 st_max = max(st_max, it);
+                if (status & FADESIM_ST_WARM_REJECTED) st_rej += 1;
                 atomicOr(&st_or, status);  // the last row's CTA may flag it too
             }
         }
@@ -902,6 +934,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             atomicAdd(&a.stats->solves, st_solves);
             atomicAdd(&a.stats->iters_sum, st_iters);
             atomicMax(&a.stats->iters_max, st_max);
+            if (st_rej) atomicAdd(&a.stats->warm_rejected, st_rej);
         }
         if (st_or) atomicOr(&a.stats->status_or, st_or);  // rank 0's, or a flag of the last row's CTA
     }

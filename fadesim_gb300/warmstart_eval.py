@@ -7,7 +7,7 @@ own throughput, and for both solvers the iterations (line) or sweeps (red-black
 SOR) from the ideal state and from the prediction, the fallback (rejection) rate
 and the end-to-end solves/s including inference.
 
-  python -m fadesim_gb300.warmstart_eval [--size 128] [--train 200000] [--infer 8192] [--cells weak|strong]
+  python -m fadesim_gb300.warmstart_eval [--size 128] [--train 200000] [--infer 8192] [--cells weak|strong|sinh]
   python -m fadesim_gb300.warmstart_eval --conv [--conv-shape N,H,W,Cin,Cout]   (one convolution, both kernels)
 """
 import argparse
@@ -22,6 +22,8 @@ from . import warmstart as ws
 R_STATES = (2e6, 1.6e6, 1.3e6, 1e6)
 # 2-bit cells between 1 kohm and 1 Mohm, linear in conductance (the MLP layers' arrays)
 G_STRONG = tuple(1e-6 + k * (1e-3 - 1e-6) / 3 for k in range(4))
+# sinh cells I = (V / R) sinh(2V) / (2V) between 1 and 2 Mohm: [R_on, R_off, a_on, b_on, a_off, b_off]
+SINH_PARAMS = (1e6, 2e6, 2.0, 1.0 / (2.0 * 1e6), 2.0, 1.0 / (2.0 * 2e6))
 
 
 def _timed(fn):
@@ -37,8 +39,10 @@ def _timed(fn):
 def train_and_evaluate(size=128, train_instances=200000, batch=64, infer=8192, lr=1e-3, g_wire=1 / 2.93, seed=0,
                        cells="weak", sor_omegas=(1.96, 1.98), sor_sample=304):
     """Train on ``train_instances`` solver-generated tiles of the given cells
-    ("weak": four states 1-2 Mohm; "strong": 2-bit 1 kohm - 1 Mohm) with
-    Bernoulli 0.2 V inputs, then on a fresh batch of ``infer`` tiles report the
+    ("weak": four states 1-2 Mohm; "strong": 2-bit 1 kohm - 1 Mohm; both with
+    Bernoulli 0.2 V inputs; "sinh": the large non-ideal setting -- four states
+    1-2 Mohm with lognormal variation sigma 0.1, sinh cells, inputs uniform in
+    [0, 0.2] V), then on a fresh batch of ``infer`` tiles report the
     prediction error, the network's throughput, and for the line solver and the
     plain red-black SOR the iterations / sweeps from the ideal state and from
     the prediction, the fallback rate (predictions the line solver discarded)
@@ -46,16 +50,26 @@ def train_and_evaluate(size=128, train_instances=200000, batch=64, infer=8192, l
     n = size
     gvals = torch.tensor(G_STRONG if cells == "strong" else [1.0 / r for r in R_STATES])
     gen = torch.Generator().manual_seed(seed)
+    sinh = cells == "sinh"
+    nl = dict(nonlinear_cell_enable=True, nonlinear_params=SINH_PARAMS) if sinh else {}
+    draws = [0]
 
     def draw(N):
         G = gvals[torch.randint(0, len(gvals), (N, n, n), generator=gen)].float().cuda()
-        vin = (torch.randint(0, 2, (N, n), generator=gen).float() * 0.2).cuda()
+        if sinh:
+            # the large non-ideal setting: lognormal variation, inputs uniform in [0, 0.2] V
+            from .variation import add_variation_device
+            draws[0] += 1
+            G = add_variation_device(G, 0.1, seed=seed * 1000 + draws[0])
+            vin = (torch.rand((N, n), generator=gen) * 0.2).cuda()
+        else:
+            vin = (torch.randint(0, 2, (N, n), generator=gen).float() * 0.2).cuda()
         return G, vin
 
     def solve_planes(G, vin):
         N = G.shape[0]
         planes, _, _ = acc.ir_drop_gs_ex(vin[None].contiguous(), G.contiguous(), 1, n, n, N, 1, g_wire=g_wire,
-                                         ret_V=2, method="line")
+                                         ret_V=2, method="line", **nl)
         p = planes[0, :, 0].clone()
         p[:, 0] -= vin[:, :, None]
         return p
@@ -77,8 +91,10 @@ def train_and_evaluate(size=128, train_instances=200000, batch=64, infer=8192, l
     rel = float((pred - true).norm() / true.norm())
     ti = vin[None].contiguous()
     init = pred[None, :, None].contiguous()
-    (_, cold, _), t_cold = _timed(lambda: acc.ir_drop_gs_ex(ti, G, 1, n, n, infer, 1, g_wire=g_wire, method="line"))
-    (_, warm, _), t_warm = _timed(lambda: acc.ir_drop_gs_warm(ti, G, 1, n, n, infer, 1, init, g_wire=g_wire))
+    (_, cold, _), t_cold = _timed(lambda: acc.ir_drop_gs_ex(ti, G, 1, n, n, infer, 1, g_wire=g_wire, method="line",
+                                                            **nl))
+    (_, warm, _), t_warm = _timed(lambda: acc.ir_drop_gs_warm(ti, G, 1, n, n, infer, 1, init, g_wire=g_wire,
+                                                              nonlinear_params=SINH_PARAMS if sinh else None))
     line = {"iters_mean_cold": cold["iters_sum"] / cold["solves"], "iters_mean_warm": warm["iters_sum"] / warm["solves"],
             "iters_saved_frac": 1 - warm["iters_sum"] / cold["iters_sum"],
             "fallback_rate": warm["warm_rejected"] / warm["solves"],
@@ -152,7 +168,7 @@ def main():
     ap.add_argument("--train", type=int, default=200000, help="training instances")
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--infer", type=int, default=8192)
-    ap.add_argument("--cells", default="weak", choices=["weak", "strong"])
+    ap.add_argument("--cells", default="weak", choices=["weak", "strong", "sinh"])
     ap.add_argument("--conv", action="store_true",
                     help="only time one network convolution on both kernels (for profiling)")
     ap.add_argument("--conv-shape", default="64,128,128,64,32", help="N,H,W,Cin,Cout of --conv")
@@ -163,7 +179,8 @@ def main():
         N, H, W, cin, cout = (int(v) for v in a.conv_shape.split(","))
         print(json.dumps([conv_throughput(N, H, W, cin, cout), conv_throughput(N, H, W, cin, cout, legacy=True)]))
         return
-    print(json.dumps(train_and_evaluate(a.size, a.train, a.batch, a.infer, cells=a.cells)))
+    print(json.dumps(train_and_evaluate(a.size, a.train, a.batch, a.infer, cells=a.cells,
+                                        sor_omegas=() if a.cells == "sinh" or a.size > 128 else (1.96, 1.98))))
 
 
 if __name__ == "__main__":

@@ -261,12 +261,15 @@ int fadesim_noalloc_last_status(fadesim_solve_stats *stats, void *stream);
 
 /* fadesim_ir_drop_gs_ex started from given node planes (a learned warm start): init is a DEVICE
  * FP32 array [batch, numX, numY, 2, rows, cols] of wordline deviations u - vin and bitline voltages
- * d.  The line method (rows, cols <= 128) iterates from them to the same tolerance; a prediction
- * whose first correction is as large as the solution is discarded (FADESIM_ST_WARM_REJECTED) and
- * the solve restarts from the ideal state.  opts->method FADESIM_METHOD_RBSOR starts the plain
- * red-black SOR from the planes instead (the comparator the learned start is measured against). */
+ * d.  The line method (every tile size up to 512 x 512, linear or sinh cells -- nonlinear_* as in
+ * fadesim_ir_drop_gs_ex) iterates from them to the same tolerance; a prediction whose first
+ * correction is as large as the solution is discarded (FADESIM_ST_WARM_REJECTED) and the solve
+ * restarts from the ideal state.  opts->method FADESIM_METHOD_RBSOR starts the plain red-black SOR
+ * from the planes instead (tiles up to 128 x 128, linear cells: the comparator the learned start
+ * is measured against). */
 int fadesim_ir_drop_gs_warm(int dtype, const void *input, const void *G, int batch_size, int row_size, int col_size,
-                            int numX, int numY, double g_wire, const float *init, void *out,
+                            int numX, int numY, double g_wire, const float *init, int nonlinear_cell_enable,
+                            const double *nonlinear_params, int n_nonlinear_params, void *out,
                             const fadesim_solve_opts *opts, fadesim_solve_stats *stats, int *per_solve_iters,
                             void *stream);
 

@@ -175,6 +175,40 @@ def test_solver_warm_start_exact_and_garbage(ws):
     assert np.abs(out.double().cpu().numpy()[:, 0] - ref).max() <= 1e-4 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("n,sinh", [(256, False), (512, False), (256, True), (512, True)])
+def test_cluster_warm_start_exact_and_garbage(ws, n, sinh):
+    """Warm starts on the cluster layouts (256 x 256 on 4-CTA clusters, 512 x
+    512 on 16-CTA clusters; linear and sinh cells with lognormal variation):
+    started from the converged planes the solve takes fewer iterations and
+    returns the same currents; started from planes that are far off it discards them
+    (FADESIM_ST_WARM_REJECTED), restarts from the ideal state and lands on the
+    same currents again."""
+    from fadesim_gb300 import cpp_ir_drop_accelerate as acc
+    from fadesim_gb300.variation import add_variation_device
+    B, X = 2, 1
+    rng = np.random.default_rng(n + sinh)
+    R4 = np.array([2e6, 1.6e6, 1.3e6, 1e6])
+    G0 = torch.tensor(1.0 / R4[rng.integers(0, 4, (X, n, n))], dtype=torch.float32, device="cuda")
+    tg = add_variation_device(G0, 0.1, seed=5) if sinh else G0
+    vin = torch.tensor(rng.random((B, X, n)) * 0.2, dtype=torch.float32, device="cuda")
+    nl = dict(nonlinear_cell_enable=True, nonlinear_params=nodal.sinh_params(1e6, 2e6)) if sinh else {}
+    planes, st0, _ = acc.ir_drop_gs_ex(vin, tg, B, n, n, X, 1, g_wire=GW, ret_V=2, method="line", **nl)
+    cold, st1, _ = acc.ir_drop_gs_ex(vin, tg, B, n, n, X, 1, g_wire=GW, method="line", **nl)
+    assert st0["status_or"] == 1 and st1["status_or"] == 1
+    init = planes.float().clone()
+    init[:, :, :, 0] -= vin[:, :, None, :, None]
+    wkw = dict(g_wire=GW, nonlinear_params=nodal.sinh_params(1e6, 2e6) if sinh else None)
+    warm, st2, _ = acc.ir_drop_gs_warm(vin, tg, B, n, n, X, 1, init.contiguous(), **wkw)
+    assert st2["status_or"] == 1 and st2["warm_rejected"] == 0
+    assert st2["iters_max"] <= 3 and st2["iters_sum"] < st1["iters_sum"], (st2, st1)
+    scale = cold.abs().max().item()
+    assert (warm - cold).abs().max().item() <= 1e-5 * scale
+    junk = torch.full(init.shape, 0.7, dtype=torch.float32, device="cuda")
+    out, st3, _ = acc.ir_drop_gs_warm(vin, tg, B, n, n, X, 1, junk, **wkw)
+    assert st3["status_or"] & 8 and st3["status_or"] & 1 and st3["warm_rejected"] == B * X
+    assert (out - cold).abs().max().item() <= 1e-5 * scale
+
+
 def test_trained_network_prediction_and_warm_solve(ws, tmp_path):
     """Train briefly on solver-generated data with the strong 2-bit cells of the
     MLP layers (1 kohm - 1 Mohm, linear in conductance, 64x64 tiles, Bernoulli
