@@ -746,7 +746,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
             // sinh cells too, so that two pass bodies alternate instead of three,
             // measured 2% slower on the 512x512 sinh-cell workload.)  A warm start
             // loads this band's rows of the initial deviation planes [2][n][m].
-            bool warm = a.init != nullptr;
+            bool warm = a.init != nullptr, rejected = false;
             bool zero = !warm && !precise_first;
             if (warm) {
                 const float *w0 = a.init + (((size_t)b * a.numX + x) * a.numY + y) * 2 * n * m;
@@ -848,7 +848,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 ++it;
                 if (!isfinite(delta) || !isfinite(vm)) {
                     // the same cluster-wide values in every CTA: every CTA leaves here
-                    status |= FADESIM_ST_NONFINITE;
+                    status = FADESIM_ST_NONFINITE;
                     break;
                 }
                 if (warm && it == 1 && !(delta < vm)) {
@@ -864,7 +864,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                     cluster.sync();  // every band restarted before any halo is read again
                     zero = !precise_first;
                     warm = false;
-                    status |= FADESIM_ST_WARM_REJECTED;
+                    rejected = true;
                     stop.init(a.ctl.omega, rate_hint, omega_prev);
                     omega = stop.omega;
                     res64 = precise_first;
@@ -874,7 +874,7 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 omega = stop.omega;
                 if (small) {
                     if (res64 || kres < 0) {
-                        status |= FADESIM_ST_CONVERGED;
+                        status = FADESIM_ST_CONVERGED;
                         break;
                     }
                     res64 = true;
@@ -882,10 +882,11 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                     res64 = kres > 0 ? (it % kres == 0) : (kres == 0 && stop.want_precise(tol, vm, a.ctl.precise_margin));
                 }
                 if (it >= maxit) {
-                    status |= FADESIM_ST_MAXITER;
+                    status = FADESIM_ST_MAXITER;
                     break;
                 }
             }
+            if (rejected) status |= FADESIM_ST_WARM_REJECTED;
             rate_hint = stop.final_rate();
             omega_prev = stop.omega;
             // ---- outputs --------------------------------------------------------
