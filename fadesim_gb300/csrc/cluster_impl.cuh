@@ -622,10 +622,11 @@ __device__ __forceinline__ void cl_outputs(cg::cluster_group &cluster, int rank,
 template <int LDM, bool NL, bool FULL>
 __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a) {
     constexpr int C = CCfg<LDM>::C, RPC = CCfg<LDM>::RPC, SEG = CL_SEG;
-    // The wordline pass keeps its bounds tests even on full tiles: without them
-    // the compiler hoists a whole segment's loads and spills (measured); the
-    // bitline pass, where the cross-band scans dominate, drops them.
-    constexpr bool WFULL = false;
+    // Full tiles drop the bounds tests of both passes.  (With one pass body per
+    // residual form, a bounds-free wordline pass made the compiler hoist a whole
+    // segment's loads and spill 650 bytes; with the residual forms sharing one
+    // Thomas solve it does not, and the 256 x 256 solve is 15% faster.)
+    constexpr bool WFULL = FULL;
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     extern __shared__ float4 smem4[];
