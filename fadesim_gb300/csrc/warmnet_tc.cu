@@ -301,28 +301,38 @@ __global__ void __launch_bounds__(128, 1)
 
 // ---- weight gradient ---------------------------------------------------------
 // dW[co][tap][ci] += sum over pixels p of dY[p][co] X[p + tap][ci]: a GEMM with
-// M = Cout (TMEM lanes), N = 32 input channels per CTA, K = pixels, one FP32
-// accumulator of 32 TMEM columns per tap (9 x 32 = 288 of 512).  Both operands
-// are the NHWC activations as TMA loads them, read MN-major (channels
-// contiguous): per 16 x 8-pixel tile, A = dY in 32-channel boxes (32 x 128
-// pixels, 8 KB, boxes LBO = 8 KB apart along M) and B = X in three boxes, one
-// per column shift dx, of the tile's rows and one above and below (32 x 160
-// pixels, 10 KB); the tap's row shift dy is the B box read from row dy, and a
-// K = 16 step is one tile row -- both whole-atom offsets (1 KB) of the 64-byte
-// swizzle.  Each CTA sums a run of tiles (split-K) for one 32-channel slice of
-// Cin and adds its accumulators to dW with FP32 atomics.
+// M = Cout (TMEM lanes), N = a slice of up to 128 input channels, K = pixels.
+// A CTA handles one column shift dx and one channel slice: its three taps
+// (row shifts dy) share one input box, so it keeps three accumulators of N
+// TMEM columns.  Both operands are the NHWC activations as TMA loads them,
+// read MN-major (channels contiguous): per 16 x 8-pixel tile, A = dY in
+// 32-channel boxes (32 x 128 pixels, 8 KB, LBO = 8 KB apart along M) and B = X
+// in 32-channel boxes of the tile's rows and one above and below (32 x 160
+// pixels, 10 KB, LBO = 10 KB apart along N); tap dy is the B boxes read from
+// row dy, and a K = 16 step is one tile row -- both whole-atom offsets (1 KB)
+// of the 64-byte swizzle.  Wide N keeps the operand reads from shared memory
+// per MMA below the SM's bandwidth (an M128 x N32 MMA reads 5 KB for 21 cycles
+// of tensor work, an M128 x N128 one 8 KB for 84).  Each CTA sums a run of
+// tiles (split-K) and adds its accumulators to dW with FP32 atomics.
 constexpr int WG_AG_BYTES = TC_M * TC_KC * 2;                  // one 32-channel dY box: 8 KB
 constexpr int WG_A_BYTES = 4 * WG_AG_BYTES;                     // Cout <= 128
-constexpr int WG_B_BYTES = (TC_TH + 2) * TC_TW * TC_KC * 2;     // one X box: 10 KB
-constexpr int WG_STAGE_BYTES = WG_A_BYTES + 3 * WG_B_BYTES;     // 62 KB
+constexpr int WG_BG_BYTES = (TC_TH + 2) * TC_TW * TC_KC * 2;    // one 32-channel X box: 10 KB
+constexpr int WG_NMAX = 128;                                    // input channels per CTA
+constexpr int WG_B_BYTES = (WG_NMAX / TC_KC) * WG_BG_BYTES;     // 40 KB
+constexpr int WG_STAGE_BYTES = WG_A_BYTES + WG_B_BYTES;         // 72 KB
 constexpr int WG_STAGES = 3;
 constexpr int WG_SMEM = WG_STAGES * WG_STAGE_BYTES + 1024 /* alignment */ + 256 /* barriers */;
-constexpr uint32_t WG_COLS = 512;                               // 9 taps x 32 columns, rounded to a power of two
+
+// The input-channel slice of a weight-gradient CTA: the largest of 128, 96, 64,
+// 32 that divides Cin.
+__host__ __device__ constexpr int wg_slice(int Cin) {
+    return Cin % 128 == 0 ? 128 : (Cin % 96 == 0 ? 96 : (Cin % 64 == 0 ? 64 : 32));
+}
 
 // Shared-memory descriptor of an MN-major operand in the 64-byte swizzle: rows
 // of 64 bytes hold 32 consecutive M (or N) elements, consecutive K elements are
-// consecutive rows (8-row groups 512 bytes apart), and blocks of 32 M elements
-// lie lbo bytes apart.
+// consecutive rows (8-row groups 512 bytes apart), and blocks of 32 M (N)
+// elements lie lbo bytes apart.
 __device__ __forceinline__ uint64_t desc_mn_sw64(uint32_t saddr, uint32_t lbo) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
@@ -346,11 +356,14 @@ __global__ void __launch_bounds__(128, 1)
     __shared__ int s_fail;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int ci0 = (int)blockIdx.y * TC_KC;
+    const int NS = wg_slice(Cin);                    // N: this CTA's input channels
+    const int ci0 = (int)blockIdx.y * NS;
+    const int dx = (int)blockIdx.z;                  // column shift 0, 1, 2 (-1, 0, +1)
     const long long t0 = (long long)blockIdx.x * tiles_per_cta;
     const int nt = (int)min((long long)tiles_per_cta, tiles - t0);  // >= 1 by the grid
     const int tiles_w = W / TC_TW, tiles_img = tiles_w * (H / TC_TH);
-    const int groups = Cout / TC_KC;
+    const int ygroups = Cout / TC_KC, xgroups = NS / TC_KC;
+    const uint32_t ncols = 3 * NS <= 256 ? 256u : 512u;  // three accumulators of NS columns
 
     if (tid == 0) {
         s_fail = 0;
@@ -364,7 +377,7 @@ __global__ void __launch_bounds__(128, 1)
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(WG_COLS)
+                     "r"(ncols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -374,9 +387,9 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t tmem = *tmem_slot;
 
     if (tid == 0) {
-        // producer: per tile the dY boxes of every 32 output channels and the
-        // three column-shifted X boxes of this CTA's 32 input channels
-        const uint32_t tx = (uint32_t)(groups * WG_AG_BYTES + 3 * WG_B_BYTES);
+        // producer: per tile the dY boxes of every 32 output channels and this
+        // CTA's column-shifted X boxes of its input channels
+        const uint32_t tx = (uint32_t)(ygroups * WG_AG_BYTES + xgroups * WG_BG_BYTES);
         for (int i = 0; i < nt; ++i) {
             const int s = i % WG_STAGES;
             const uint32_t ph = (uint32_t)(i / WG_STAGES) & 1u;
@@ -389,14 +402,14 @@ __global__ void __launch_bounds__(128, 1)
             const int h0 = (r / tiles_w) * TC_TH, w0 = (r % tiles_w) * TC_TW;
             unsigned char *sa = base + s * WG_STAGE_BYTES;
             mbar_expect_tx(&full[s], tx);
-            for (int g = 0; g < groups; ++g) tma_load_4d(sa + g * WG_AG_BYTES, &tmY, g * TC_KC, w0, h0, n, &full[s]);
-#pragma unroll
-            for (int dx = 0; dx < 3; ++dx)
-                tma_load_4d(sa + WG_A_BYTES + dx * WG_B_BYTES, &tmX, ci0, w0 + dx - 1, h0 - 1, n, &full[s]);
+            for (int g = 0; g < ygroups; ++g) tma_load_4d(sa + g * WG_AG_BYTES, &tmY, g * TC_KC, w0, h0, n, &full[s]);
+            for (int g = 0; g < xgroups; ++g)
+                tma_load_4d(sa + WG_A_BYTES + g * WG_BG_BYTES, &tmX, ci0 + g * TC_KC, w0 + dx - 1, h0 - 1, n,
+                            &full[s]);
         }
     } else if (tid == 32) {
-        // MMA issuer: 9 taps x 8 K = 16 steps (tile rows) per tile
-        const uint32_t idesc = idesc_bf16(TC_M, TC_KC) | (1u << 15) | (1u << 16);  // A and B MN-major
+        // MMA issuer: 3 taps (row shifts) x 8 K = 16 steps (tile rows) per tile
+        const uint32_t idesc = idesc_bf16(TC_M, NS) | (1u << 15) | (1u << 16);  // A and B MN-major
         bool ok = true;
         for (int i = 0; i < nt; ++i) {
             const int s = i % WG_STAGES;
@@ -412,13 +425,9 @@ __global__ void __launch_bounds__(128, 1)
 #pragma unroll
             for (int dy = 0; dy < 3; ++dy)
 #pragma unroll
-                for (int dx = 0; dx < 3; ++dx)
-#pragma unroll
-                    for (int k = 0; k < TC_TH; ++k)
-                        umma_bf16(tmem + (uint32_t)((dy * 3 + dx) * TC_KC),
-                                  desc_mn_sw64(sa + k * TC_ROW_BYTES, WG_AG_BYTES),
-                                  desc_mn_sw64(sb + dx * WG_B_BYTES + (dy + k) * TC_ROW_BYTES, 16), idesc,
-                                  (i | k) ? 1u : 0u);
+                for (int k = 0; k < TC_TH; ++k)
+                    umma_bf16(tmem + (uint32_t)(dy * NS), desc_mn_sw64(sa + k * TC_ROW_BYTES, WG_AG_BYTES),
+                              desc_mn_sw64(sb + (dy + k) * TC_ROW_BYTES, WG_BG_BYTES), idesc, (i | k) ? 1u : 0u);
             umma_commit(&empty[s]);
         }
         if (ok) umma_commit(done);
@@ -431,23 +440,25 @@ __global__ void __launch_bounds__(128, 1)
         // warp w reads TMEM lanes 32w .. 32w + 31: output channels co
         const int co = warp * 32 + lane;
         const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int tap = 0; tap < 9; ++tap)
-#pragma unroll
-            for (int half = 0; half < 2; ++half) {
+        for (int dy = 0; dy < 3; ++dy) {
+            const int tap = dy * 3 + dx;
+            for (int j0 = 0; j0 < NS; j0 += 16) {
                 float v[16];
-                tmem_ld16(lane_base + (uint32_t)(tap * TC_KC + half * 16), v);
+                tmem_ld16(lane_base + (uint32_t)(dy * NS + j0), v);
                 if (co < Cout) {
-                    float *d = dW + ((long long)co * 9 + tap) * Cin + ci0 + half * 16;
+                    float *d = dW + ((long long)co * 9 + tap) * Cin + ci0 + j0;
 #pragma unroll
                     for (int q = 0; q < 16; ++q) atomicAdd(d + q, v[q]);
                 }
             }
+        }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
+        __syncwarp();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(WG_COLS) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
     }
     if (tid == 0 && s_fail && err) atomicExch(err, s_fail);
 }
@@ -581,19 +592,19 @@ cudaError_t conv3x3_wgrad_tc(const void *dY, const void *X, float *dW, int N, in
         return cudaErrorInvalidValue;
     const long long tiles = (long long)N * (H / TC_TH) * (W / TC_TW);
     if (tiles < 1) return cudaSuccess;
-    // one CTA per SM (shared memory and TMEM): split the tiles so that the
-    // Cin / 32 channel slices together fill the SMs
+    // one CTA per SM (shared memory): split the tiles so that the 3 column
+    // shifts x Cin / N channel slices together fill the SMs
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
                                                   cudaSuccess)
         return cudaErrorInvalidValue;
-    const int slices = Cin / TC_KC;
-    const long long want = max(1, sms / slices);
+    const int slices = Cin / wg_slice(Cin);
+    const long long want = max(1, sms / (3 * slices));
     const long long per = (tiles + want - 1) / want;
     const long long splits = (tiles + per - 1) / per;  // every CTA gets at least one tile
     cudaError_t e = cudaFuncSetAttribute(conv3x3_wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, WG_SMEM);
     if (e != cudaSuccess) return e;
-    conv3x3_wgrad_tc_kernel<<<dim3((unsigned)splits, (unsigned)slices), 128, WG_SMEM, st>>>(
+    conv3x3_wgrad_tc_kernel<<<dim3((unsigned)splits, (unsigned)slices, 3), 128, WG_SMEM, st>>>(
         my, mx, dW, H, W, Cin, Cout, tiles, (int)per, err);
     return cudaGetLastError();
 }
