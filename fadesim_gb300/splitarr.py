@@ -167,6 +167,11 @@ def _check_modes(arr, in_mode, dacBits, cfg):
         raise NotImplementedError("OU and BNN modes are not implemented")
 
 
+# bytes of repeated input vectors and currents that one batched solver call of
+# the layer driver may hold (the maps of a layer are grouped to stay under it)
+MAP_GROUP_BYTES = 1 << 30
+
+
 def _split_matmul_core(xq, geom, M, insize, has_ones, ones_q, s1, w, inputBits, dacBits, adcBits, weightBits, arr,
                        neg_pulse, cfg, solver, bias=None, L=0, rand_gen=None):
     """The bit-serial, bit-sliced product of splitArr_matmul_nn from quantised
@@ -226,20 +231,30 @@ def _split_matmul_core(xq, geom, M, insize, has_ones, ones_q, s1, w, inputBits, 
 
     sigma = float(getattr(cfg, "sigma", 0) or 0)
     if sigma == 0:
-        # every (slice, array) map solved in one call: the maps stacked along the
-        # tile axis, each with all input bits' vectors (one launch per layer
-        # instead of one per map; each (tile, vector) solve is the same)
+        # the (slice, array) maps solved together: stacked along the tile axis,
+        # each with all input bits' vectors (one launch per layer instead of one
+        # per map; each (tile, vector) solve is the same), in groups whose
+        # repeated inputs and currents stay within MAP_GROUP_BYTES
         nm = nslices * narr
-        maps = torch.empty((nm * numX, rows, numY * cb), dtype=torch.float32, device=dev)
-        for j in range(nslices):
-            for a in range(narr):
-                map_slice(j, a, maps[(j * narr + a) * numX:(j * narr + a + 1) * numX])
-        vv = v.repeat(1, nm, 1)
-        res = torch.empty((nbits * M, nm * numX, numY * cb), dtype=torch.float32, device=dev)
-        r = solver(vv, maps, nbits * M, rows, cb, nm * numX, numY, res)
-        if r is not None and r.data_ptr() != res.data_ptr():
-            res.copy_(r.reshape(res.shape))
-        I.copy_(res.reshape(nbits * M, nslices, narr, numX, numY * cb).permute(1, 2, 0, 3, 4))
+        per_map = v.numel() * 4 + I[0, 0].numel() * 4
+        g = max(1, min(nm, MAP_GROUP_BYTES // max(1, per_map)))
+        maps = torch.empty((g * numX, rows, numY * cb), dtype=torch.float32, device=dev)
+        for k0 in range(0, nm, g):
+            gk = min(g, nm - k0)
+            for k in range(gk):
+                j, a = divmod(k0 + k, narr)
+                map_slice(j, a, maps[k * numX:(k + 1) * numX])
+            if gk == 1:
+                j, a = divmod(k0, narr)
+                solve_into(v, maps[:numX], nbits * M, I[j, a])
+                continue
+            vv = v.repeat(1, gk, 1)
+            res = torch.empty((nbits * M, gk * numX, numY * cb), dtype=torch.float32, device=dev)
+            r = solver(vv, maps[:gk * numX], nbits * M, rows, cb, gk * numX, numY, res)
+            if r is not None and r.data_ptr() != res.data_ptr():
+                res.copy_(r.reshape(res.shape))
+            dst = I.reshape(nm, nbits * M, numX, numY * cb)[k0:k0 + gk]
+            dst.copy_(res.reshape(nbits * M, gk, numX, numY * cb).permute(1, 0, 2, 3))
     else:
         gen = rand_gen if rand_gen is not None else _variation.variations.rand_gen_network
         maps = torch.empty((nslices, narr) + tuple(G.shape), dtype=torch.float32, device=dev)

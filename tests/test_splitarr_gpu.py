@@ -87,6 +87,24 @@ def test_split_matmul_matches_oracle_with_gpu_solver_currents(sa):
     assert np.array_equal(y.cpu().numpy(), ref)
 
 
+def test_map_grouping_gives_the_same_bits(sa, gold, monkeypatch):
+    """The layer driver's batching of weight-slice maps into one solver call
+    (bounded by MAP_GROUP_BYTES) changes nothing: one map per call, a few per
+    call and all in one give the same output bits."""
+    z = gold("pimtorch_split_c3like.npz")
+    cfg = sa.ArrayConfig(Ron=float(z["Ron"]), Roff=float(z["Roff"]), cellBits=int(z["cellBits"]),
+                         arrRowSize=int(z["rows"]), arrColSize=int(z["cols"]),
+                         inputMaxVoltage=float(z["inputMaxVoltage"]))
+    run = lambda: sa.splitArr_matmul_nn(torch.from_numpy(z["x"]), torch.from_numpy(z["w"]), 8, 1, int(z["adc_bits"]),
+                                        10, 8, "PN", torch.float32, cfg=cfg, solver=droop_on_host).cpu().numpy()
+    whole = run()
+    v_bytes = z["x"].shape[0] * 8 * 4   # bytes of one map's input vectors per row of tiles
+    for budget in (1, 2 * v_bytes * 64):
+        monkeypatch.setattr(sa, "MAP_GROUP_BYTES", budget)
+        assert np.array_equal(run(), whole)
+    assert np.array_equal(whole, z["y"])
+
+
 def layer_cfg(sa, z):
     return sa.ArrayConfig(Ron=float(z["Ron"]), Roff=float(z["Roff"]), cellBits=int(z["cellBits"]),
                           arrRowSize=int(z["rows"]), arrColSize=int(z["cols"]),
