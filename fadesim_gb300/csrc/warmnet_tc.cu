@@ -50,10 +50,12 @@ constexpr int TC_TH = TC_M / TC_TW;  // tile rows
 constexpr int TC_KC = 32;          // channels per K chunk (64-byte rows)
 constexpr int TC_A_BYTES = (TC_TH + 2) * TC_TW * TC_KC * 2;  // 10 KB: the tile's rows and one above and below
 constexpr int TC_ROW_BYTES = TC_TW * TC_KC * 2;              // 1 KB: one row shift of the A operand
-// bytes of one stage: A and the three taps' B (Cout x 64 bytes each)
-__host__ __device__ constexpr int tc_stage_bytes(int Cout) { return TC_A_BYTES + 3 * Cout * TC_KC * 2; }
+// bytes of one stage: the A boxes of TP tiles and the three taps' B (Cout x 64 bytes each)
+__host__ __device__ constexpr int tc_stage_bytes(int Cout, int TP) { return TP * TC_A_BYTES + 3 * Cout * TC_KC * 2; }
 // dynamic shared memory of a kernel with S stages
-constexpr int tc_smem(int S, int Cout) { return S * tc_stage_bytes(Cout) + 1024 /* alignment */ + 256 /* barriers */; }
+constexpr int tc_smem(int S, int Cout, int TP) {
+    return S * tc_stage_bytes(Cout, TP) + 1024 /* alignment */ + 256 /* barriers */;
+}
 constexpr long long TC_WAIT_CYCLES = 2000000000LL;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -151,17 +153,19 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 }
 
 // STAGES: depth of the TMA ring; fewer stages let more CTAs share an SM,
-// which hides the per-tile latency chain better.
-template <int TC_STAGES>
+// which hides the per-tile latency chain better.  TP: tiles per CTA (1 or 2):
+// two tiles share every stage's weight boxes (one B operand for two MMAs into
+// two accumulators), which halves the weight traffic per tile.
+template <int TC_STAGES, int TP>
 __global__ void __launch_bounds__(128, 1)
     conv3x3_fwd_tc_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmW,
                           const float *__restrict__ bias, const __nv_bfloat16 *__restrict__ skip, void *__restrict__ Y,
-                          int H, int W, int Cin, int Cout, int flags, int *err) {
+                          int H, int W, int Cin, int Cout, long long tiles, int flags, int *err) {
     extern __shared__ unsigned char tc_smem_raw[];
     // stage buffers 1024-byte aligned in the shared window (the swizzle pattern
     // is a function of the shared-memory address)
     unsigned char *base = tc_smem_raw + ((1024u - (smem_u32(tc_smem_raw) & 1023u)) & 1023u);
-    const int SB = tc_stage_bytes(Cout);
+    const int SB = tc_stage_bytes(Cout, TP);
     const int BT = Cout * TC_KC * 2;  // bytes of one tap's B
     uint64_t *full = reinterpret_cast<uint64_t *>(base + TC_STAGES * SB);
     uint64_t *empty = full + TC_STAGES;
@@ -170,12 +174,20 @@ __global__ void __launch_bounds__(128, 1)
     __shared__ int s_fail;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tiles_w = W / TC_TW, tiles_h = H / TC_TH;
-    const int n = (int)(blockIdx.x / (unsigned)(tiles_w * tiles_h));
-    const int t = (int)(blockIdx.x % (unsigned)(tiles_w * tiles_h));
-    const int h0 = (t / tiles_w) * TC_TH, w0 = (t % tiles_w) * TC_TW;
+    const int tiles_w = W / TC_TW, tiles_img = tiles_w * (H / TC_TH);
+    const long long t0 = (long long)blockIdx.x * TP;
+    const int ntp = (int)min((long long)TP, tiles - t0);  // >= 1 by the grid
+    int tn[TP], th[TP], tw[TP];
+#pragma unroll
+    for (int i = 0; i < TP; ++i) {
+        const long long t = min(t0 + i, tiles - 1);
+        tn[i] = (int)(t / tiles_img);
+        const int r = (int)(t % tiles_img);
+        th[i] = (r / tiles_w) * TC_TH;
+        tw[i] = (r % tiles_w) * TC_TW;
+    }
     const int kchunks = Cin / TC_KC, kiters = 3 * kchunks;
-    const uint32_t ncols = Cout <= 32 ? 32 : (Cout <= 64 ? 64 : 128);
+    const uint32_t ncols = Cout <= 32 ? 32 : (Cout <= 64 ? 64 : 128);  // one accumulator
 
     if (tid == 0) {
         s_fail = 0;
@@ -189,7 +201,7 @@ __global__ void __launch_bounds__(128, 1)
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(ncols)
+                     "r"(TP * ncols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -199,8 +211,8 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t tmem = *tmem_slot;
 
     if (tid == 0) {
-        // producer: per (dx, chunk) the A box and the three taps' B
-        const uint32_t tx = (uint32_t)SB;
+        // producer: per (dx, chunk) the A box of each tile and the three taps' B
+        const uint32_t tx = (uint32_t)(ntp * TC_A_BYTES + 3 * BT);
         for (int it = 0; it < kiters; ++it) {
             const int s = it % TC_STAGES;
             const uint32_t ph = (uint32_t)(it / TC_STAGES) & 1u;
@@ -211,14 +223,16 @@ __global__ void __launch_bounds__(128, 1)
             const int dxi = it / kchunks, c0 = (it % kchunks) * TC_KC;
             unsigned char *sa = base + s * SB;
             mbar_expect_tx(&full[s], tx);
-            tma_load_4d(sa, &tmX, c0, w0 + dxi - 1, h0 - 1, n, &full[s]);
+#pragma unroll
+            for (int i = 0; i < TP; ++i)
+                if (i < ntp) tma_load_4d(sa + i * TC_A_BYTES, &tmX, c0, tw[i] + dxi - 1, th[i] - 1, tn[i], &full[s]);
 #pragma unroll
             for (int j = 0; j < 3; ++j)
-                tma_load_2d(sa + TC_A_BYTES + j * BT, &tmW, (j * 3 + dxi) * Cin + c0, 0, &full[s]);
+                tma_load_2d(sa + TP * TC_A_BYTES + j * BT, &tmW, (j * 3 + dxi) * Cin + c0, 0, &full[s]);
         }
     } else if (tid == 32) {
         // MMA issuer: per stage three taps (row shifts dy = -1, 0, 1 of the A
-        // box) of two K = 16 steps into the TMEM accumulator
+        // box) of two K = 16 steps into each tile's accumulator
         const uint32_t idesc = idesc_bf16(TC_M, Cout);
         bool ok = true;
         for (int it = 0; it < kiters; ++it) {
@@ -231,70 +245,79 @@ __global__ void __launch_bounds__(128, 1)
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t sa = smem_u32(base + s * SB);
-            const uint32_t sb = sa + TC_A_BYTES;
+            const uint32_t sb = sa + TP * TC_A_BYTES;
 #pragma unroll
             for (int j = 0; j < 3; ++j)
 #pragma unroll
-                for (int k = 0; k < TC_KC / 16; ++k)
-                    umma_bf16(tmem, desc_sw64(sa + j * TC_ROW_BYTES + 32 * k), desc_sw64(sb + j * BT + 32 * k), idesc,
-                              (it | j | k) ? 1u : 0u);
+                for (int k = 0; k < TC_KC / 16; ++k) {
+                    const uint64_t db = desc_sw64(sb + j * BT + 32 * k);
+#pragma unroll
+                    for (int i = 0; i < TP; ++i)
+                        if (i < ntp)
+                            umma_bf16(tmem + (uint32_t)(i * ncols), desc_sw64(sa + i * TC_A_BYTES + j * TC_ROW_BYTES + 32 * k),
+                                      db, idesc, (it | j | k) ? 1u : 0u);
+                }
             umma_commit(&empty[s]);  // the stage is free once these MMAs have read it
         }
-        if (ok) umma_commit(done);  // the accumulator is final once every MMA has completed
+        if (ok) umma_commit(done);  // the accumulators are final once every MMA has completed
     }
     __syncwarp();
-    // epilogue: warp w owns TMEM lanes 32w .. 32w + 31 (two rows of the tile)
+    // epilogue: warp w owns TMEM lanes 32w .. 32w + 31 (two rows of each tile)
     const bool ready = __all_sync(0xffffffffu, mbar_wait(done, 0));
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (!ready && lane == 0) atomicExch(&s_fail, 3);
     if (ready) {
         // TMEM lane (tile pixel) r * TW + c holds output pixel (h0 + r, w0 + c)
         const int L = warp * 32 + lane;
-        const long long p = ((long long)n * H + h0 + L / TC_TW) * W + w0 + (L % TC_TW);
-        const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-        for (int j0 = 0; j0 < Cout; j0 += 16) {
-            float v[16];
-            tmem_ld16(lane_base + (uint32_t)j0, v);
+#pragma unroll 1
+        for (int i = 0; i < ntp; ++i) {
+            const long long p = ((long long)tn[i] * H + th[i] + L / TC_TW) * W + tw[i] + (L % TC_TW);
+            const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * ncols);
+            for (int j0 = 0; j0 < Cout; j0 += 16) {
+                float v[16];
+                tmem_ld16(lane_base + (uint32_t)j0, v);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                float t = v[i] + (bias ? bias[j0 + i] : 0.f);
-                if (flags & 1) t = fmaxf(t, 0.f);
-                v[i] = t;
-            }
-            if (flags & 2) {
-                const uint4 *sk = reinterpret_cast<const uint4 *>(skip + p * Cout + j0);
+                for (int q = 0; q < 16; ++q) {
+                    float x = v[q] + (bias ? bias[j0 + q] : 0.f);
+                    if (flags & 1) x = fmaxf(x, 0.f);
+                    v[q] = x;
+                }
+                if (flags & 2) {
+                    const uint4 *sk = reinterpret_cast<const uint4 *>(skip + p * Cout + j0);
 #pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const uint4 w4 = sk[q];
-                    const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&w4);
+                    for (int q = 0; q < 2; ++q) {
+                        const uint4 w4 = sk[q];
+                        const __nv_bfloat162 *h2 = reinterpret_cast<const __nv_bfloat162 *>(&w4);
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const float2 f = __bfloat1622float2(h2[e]);
-                        v[q * 8 + 2 * e] += f.x;
-                        v[q * 8 + 2 * e + 1] += f.y;
+                        for (int e = 0; e < 4; ++e) {
+                            const float2 f = __bfloat1622float2(h2[e]);
+                            v[q * 8 + 2 * e] += f.x;
+                            v[q * 8 + 2 * e + 1] += f.y;
+                        }
                     }
                 }
-            }
-            if (flags & 4) {
-                float4 *o = reinterpret_cast<float4 *>(reinterpret_cast<float *>(Y) + p * Cout + j0);
+                if (flags & 4) {
+                    float4 *o = reinterpret_cast<float4 *>(reinterpret_cast<float *>(Y) + p * Cout + j0);
 #pragma unroll
-                for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-            } else {
-                uint4 pk[2];
-                __nv_bfloat162 *h2 = reinterpret_cast<__nv_bfloat162 *>(pk);
+                    for (int q = 0; q < 4; ++q) o[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+                } else {
+                    uint4 pk[2];
+                    __nv_bfloat162 *h2 = reinterpret_cast<__nv_bfloat162 *>(pk);
 #pragma unroll
-                for (int e = 0; e < 8; ++e) h2[e] = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
-                uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(Y) + p * Cout + j0);
-                o[0] = pk[0];
-                o[1] = pk[1];
+                    for (int e = 0; e < 8; ++e) h2[e] = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
+                    uint4 *o = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(Y) + p * Cout + j0);
+                    o[0] = pk[0];
+                    o[1] = pk[1];
+                }
             }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) {
+        __syncwarp();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TP * ncols) : "memory");
     }
     if (tid == 0 && s_fail && err) atomicExch(err, s_fail);
 }
@@ -469,16 +492,26 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-// TMA ring depth of the convolution (FADESIM_CONV_STAGES: 2, 3, 4 or 6).  A
-// CTA computes one 128-pixel tile, so the depth trades prefetch against how
-// many CTAs share an SM (a stage is 16 KB at Cout = 32, 34 KB at 128); 2
-// measured fastest on the network's layer shapes (3 within 2% on 96 -> 128
-// at 16 x 16).
+// TMA ring depth of the convolution (FADESIM_CONV_STAGES: 2, 3 or 4; default
+// 2).  A CTA computes one or two 128-pixel tiles, so the depth trades
+// prefetch against how many CTAs share an SM; 2 measured fastest on the
+// network's layer shapes.
 int conv_tc_stages() {
     static const int v = [] {
         const char *e = getenv("FADESIM_CONV_STAGES");
         const int k = e ? atoi(e) : 2;
-        return (k == 2 || k == 3 || k == 4 || k == 6) ? k : 2;
+        return (k == 2 || k == 3 || k == 4) ? k : 2;
+    }();
+    return v;
+}
+
+// Two tiles per CTA sharing the weight boxes (FADESIM_CONV_PAIR: 1 on, 0 off;
+// default: where Cout >= 96, whose weight boxes outweigh the input box --
+// measured +14% and +25% on the 96 -> 96 and 96 -> 128 layers, -9% on 64 -> 32).
+int conv_tc_pair() {
+    static const int v = [] {
+        const char *e = getenv("FADESIM_CONV_PAIR");
+        return e ? (atoi(e) != 0 ? 1 : 0) : -1;
     }();
     return v;
 }
@@ -547,17 +580,22 @@ cudaError_t conv3x3_fwd_tc(const void *X, const void *Wt, const float *bias, con
         return cudaErrorInvalidValue;
     const long long tiles = (long long)N * (H / TC_TH) * (W / TC_TW);
     if (tiles < 1) return cudaSuccess;
-    const int stages = conv_tc_stages();
-    void (*kern)(CUtensorMap, CUtensorMap, const float *, const __nv_bfloat16 *, void *, int, int, int, int, int,
-                 int *) = stages == 3   ? conv3x3_fwd_tc_kernel<3>
-                          : stages == 4 ? conv3x3_fwd_tc_kernel<4>
-                          : stages == 6 ? conv3x3_fwd_tc_kernel<6>
-                                        : conv3x3_fwd_tc_kernel<2>;
-    const int smem = tc_smem(stages, Cout);
+    const int pair = conv_tc_pair();
+    const int stages = conv_tc_stages(), tp = (pair == 1 || (pair < 0 && Cout >= 96)) && tiles > 1 ? 2 : 1;
+    typedef void (*Kern)(CUtensorMap, CUtensorMap, const float *, const __nv_bfloat16 *, void *, int, int, int, int,
+                         long long, int, int *);
+    Kern kern;
+    if (tp == 2)
+        kern = stages == 3 ? conv3x3_fwd_tc_kernel<3, 2> : stages == 4 ? conv3x3_fwd_tc_kernel<4, 2>
+                                                                        : conv3x3_fwd_tc_kernel<2, 2>;
+    else
+        kern = stages == 3 ? conv3x3_fwd_tc_kernel<3, 1> : stages == 4 ? conv3x3_fwd_tc_kernel<4, 1>
+                                                                        : conv3x3_fwd_tc_kernel<2, 1>;
+    const int smem = tc_smem(stages, Cout, tp);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    kern<<<(unsigned)tiles, 128, smem, st>>>(mx, mw, bias, static_cast<const __nv_bfloat16 *>(skip), Y, H, W, Cin,
-                                             Cout, flags, err);
+    kern<<<(unsigned)((tiles + tp - 1) / tp), 128, smem, st>>>(mx, mw, bias, static_cast<const __nv_bfloat16 *>(skip),
+                                                              Y, H, W, Cin, Cout, tiles, flags, err);
     return cudaGetLastError();
 }
 

@@ -60,7 +60,8 @@ def test_conv_kernels_match_torch(ws, cin, cout, H, W):
 
 
 @pytest.mark.parametrize("cin,cout,N,H,W", [(32, 32, 1, 128, 128), (32, 64, 2, 32, 32), (96, 128, 2, 16, 16),
-                                             (128, 96, 1, 64, 64), (64, 32, 3, 16, 16), (128, 16, 2, 32, 32)])
+                                             (128, 96, 1, 64, 64), (64, 32, 3, 16, 16), (128, 16, 2, 32, 32),
+                                             (32, 32, 1, 24, 16)])
 def test_tensor_core_conv_matches_torch(ws, cin, cout, N, H, W):
     """The tcgen05 / TMA convolution (the network's shapes: Cin a multiple of
     32, 16 x 8-pixel tiles whose input box serves all three row shifts, "same"
