@@ -25,8 +25,11 @@ int line_relax_ld(int n, int m) {
 static int nwarps(int ld) { return ld == 128 ? LineCfg<128>::NW : (ld == 64 ? LineCfg<64>::NW : LineCfg<32>::NW); }
 int line_relax_threads(int ld) { return nwarps(ld) * 32; }
 size_t line_relax_smem(int ld) { return line_relax_smem_ld(ld, nwarps(ld)); }
-// chain multipliers of both passes (2 x SEG x T = 2 x LD x LD floats) and segment products (2 x T)
-size_t line_relax_scratch_floats_per_cta(int ld) { return (size_t)2 * ld * ld + 2 * (size_t)nwarps(ld) * 32; }
+// chain multipliers of both passes (2 x SEG x T = 2 x LD x LD floats), segment products (2 x T) and, on
+// the 32 and 64 layouts, the wordline unit response of linear cells (SEG x T)
+size_t line_relax_scratch_floats_per_cta(int ld) {
+    return (size_t)(ld < 128 ? 3 : 2) * ld * ld + 2 * (size_t)nwarps(ld) * 32;
+}
 
 // The I/O type is carried by the launch arguments (SolveArgs::f64); dtype is
 // accepted for symmetry with the other solvers.
