@@ -244,12 +244,16 @@ __device__ __forceinline__ void cl_word_residual(float (&x)[CL_SEG], const float
 // FP64; uniform across the cluster), then one shared Thomas solve and update
 // in the multiplier form (cm the chain multipliers gw / pivot), so that the
 // kernel carries a single copy of the solve whatever the residual forms.
+// Modes beyond the residual forms (linear cells): 5 computes the band's
+// wordline unit response T'^-1 (g / gw) into w1[k * CL_T + tid]; 6 is the
+// first iteration from the ideal state taken from it (its residual is -vin
+// g / gw on every node, so its correction is -vin times the unit response).
 template <int LDM, bool NL, bool FULL>
 __device__ __forceinline__ void cl_word_pass(int mode, float *__restrict__ U, const float *__restrict__ D,
                                              const float *__restrict__ Gs, const float *__restrict__ vin,
                                              const float *__restrict__ cm, const float *__restrict__ segprod,
                                              int nloc_in, int m_in, float inv_gw, float omega, float &dmax,
-                                             float &vmax, const SolveCtl &ctl) {
+                                             float &vmax, const SolveCtl &ctl, float *__restrict__ w1 = nullptr) {
     constexpr int NSEG = CCfg<LDM>::NSEG_W, LPW = CCfg<LDM>::LPW_W, SEG = CL_SEG;
     const int nloc = FULL ? CCfg<LDM>::RPC : nloc_in, m = FULL ? LDM : m_in;
     const int tid = threadIdx.x, lane = tid & 31, s = lane / LPW;
@@ -257,7 +261,29 @@ __device__ __forceinline__ void cl_word_pass(int mode, float *__restrict__ U, co
     const bool ok = FULL || line < nloc;
     const int p0 = s * SEG;
     const int Bw = cswz<LDM>(line, p0);
+    if constexpr (!NL) {
+        if (mode == 6) {
+            const float sc = ok ? -vin[line] : 0.f;
+            float dm = 0.f;
+#pragma unroll
+            for (int k = 0; k < SEG; ++k) {
+                if (FULL || (ok && p0 + k < m)) {
+                    const float xk = sc * w1[k * CL_T + tid];
+                    const float nv = omega * xk;
+                    U[Bw ^ k] = nv;
+                    dm = fmaxf(dm, fabsf(xk));
+                    vmax = fmaxf(vmax, fabsf(nv));
+                }
+            }
+            dmax = fmaxf(dmax, omega * dm);
+            return;
+        }
+    }
     float x[SEG];
+    if (!NL && mode == 5) {
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) x[k] = (FULL || (ok && p0 + k < m)) ? Gs[Bw ^ k] : 0.f;
+    } else
     switch (mode) {
         case 4: cl_word_residual<LDM, 0, NL, true, true, FULL>(x, U, D, Gs, vin, nloc, m, inv_gw, ctl); break;
         case 0: cl_word_residual<LDM, 0, NL, false, false, FULL>(x, U, D, Gs, vin, nloc, m, inv_gw, ctl); break;
@@ -281,6 +307,11 @@ __device__ __forceinline__ void cl_word_pass(int mode, float *__restrict__ U, co
     float Cb, Xb, Cbx, Xbx;
     scan_down<NSEG, LPW>(C, X, s, Cb, Xb, Cbx, Xbx);
     seg_apply_bwd<SEG>(x, c, Xbx);
+    if (!NL && mode == 5) {
+#pragma unroll
+        for (int k = 0; k < SEG; ++k) w1[k * CL_T + tid] = x[k];
+        return;
+    }
     float dm = 0.f;
 #pragma unroll
     for (int k = 0; k < SEG; ++k) {
@@ -651,7 +682,10 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
     const int row0 = rank * RPC;
     const int nloc = FULL ? RPC : max(0, min(RPC, n - row0));
     const bool f64 = a.f64 != 0;
-    float *piv = a.scratch + (size_t)blockIdx.x * (2 * SEG * CL_T + 2 * CL_T);
+    // per CTA: the chain multipliers of both passes, their segment products and
+    // the band's wordline unit response (linear cells)
+    float *piv = a.scratch + (size_t)blockIdx.x * (3 * SEG * CL_T + 2 * CL_T);
+    float *w1 = piv + 2 * SEG * CL_T + 2 * CL_T;
     const float gw = a.gw, tol = a.ctl.tol_v;
     const float inv_gw = 1.f / gw;
     const int kres = a.ctl.residual_period, maxit = a.ctl.max_iters;
@@ -727,6 +761,11 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 }
                 __syncthreads();
                 gs_max = cl_bcast[0];
+                // the band's wordline unit response (each thread writes and later
+                // reads only its own entries)
+                float dn0 = 0.f, dn1 = 0.f;
+                cl_word_pass<LDM, NL, WFULL>(5, U, D, Gs, vin, piv, piv + 2 * SEG * CL_T, nloc, m, inv_gw, 1.f, dn0,
+                                             dn1, a.ctl, w1);
             } else {
                 // the sinh cells keep their on/off position; the linear values served the pivots
                 for (int e = tid; e < RPC * LDM; e += CL_T) {
@@ -801,7 +840,8 @@ __global__ void __launch_bounds__(CL_T, 1) line_relax_cluster_kernel(SolveArgs a
                 omega_last = omega;
                 const int mode = zero ? 4 : (!res64 ? 0 : (semi ? 3 : (ff ? 2 : 1)));
                 const float *pW = piv, *sW = piv + 2 * SEG * CL_T;
-                cl_word_pass<LDM, NL, WFULL>(mode, U, D, Gs, vin, pW, sW, nloc, m, inv_gw, omega, dmax, vmax, a.ctl);
+                cl_word_pass<LDM, NL, WFULL>(!NL && mode == 4 ? 6 : mode, U, D, Gs, vin, pW, sW, nloc, m, inv_gw,
+                                             omega, dmax, vmax, a.ctl, w1);
                 __syncthreads();
                 for (int j = tid; j < LDM; j += CL_T) {
                     // halo rows: the row above the band and the row below it (0 V ground below the last row)

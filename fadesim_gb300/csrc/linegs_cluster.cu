@@ -19,7 +19,7 @@ int cluster_relax_ld(int n, int m) {
 
 int cluster_relax_size(int ld) { return ld == 256 ? CCfg<256>::C : CCfg<512>::C; }
 
-size_t cluster_relax_scratch_floats_per_cta(int) { return (size_t)2 * CL_SEG * CL_T + 2 * CL_T; }
+size_t cluster_relax_scratch_floats_per_cta(int) { return (size_t)3 * CL_SEG * CL_T + 2 * CL_T; }
 
 // The I/O type travels in the launch arguments (SolveArgs::f64).
 cudaError_t cluster_relax_occupancy(int ld, int, int *clusters) {
