@@ -250,6 +250,7 @@ def ir_drop_gs_host(input, G, batch_size, row_size, col_size, numX, numY, iter_t
     params = [float(v) for v in (nonlinear_params or [])]
     cparams = (ctypes.c_double * max(1, len(params)))(*params) if params else None
     stats = _lib.SolveStats()
+    want = return_stats or o.check_status != "off"
     dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
     with torch.cuda.device(dev):
         stream = torch.cuda.current_stream(dev).cuda_stream
@@ -259,12 +260,15 @@ def ir_drop_gs_host(input, G, batch_size, row_size, col_size, numX, numY, iter_t
                                          int(bool(enable_break)), float(break_threshould),
                                          int(bool(nonlinear_cell_enable)), cparams, len(params),
                                          2 if ret_V == 2 else int(bool(ret_V)), out.data_ptr(),
-                                         ctypes.byref(o.to_c()), ctypes.byref(stats) if return_stats else None,
+                                         ctypes.byref(o.to_c()), ctypes.byref(stats) if want else None,
                                          int(group_x), stream)
     _lib.check(rc)
+    st = dict(solves=int(stats.solves), iters_sum=int(stats.iters_sum), iters_max=int(stats.iters_max),
+              status_or=int(stats.status_or), warm_rejected=int(stats.warm_rejected)) if want else None
+    # the groups' counters come back once, after the call's own final synchronisation
+    check_solve_status(st, resolved_method(o.method, row_size, col_size), o.check_status)
     if return_stats:
-        return out, dict(solves=int(stats.solves), iters_sum=int(stats.iters_sum), iters_max=int(stats.iters_max),
-                         status_or=int(stats.status_or), warm_rejected=int(stats.warm_rejected))
+        return out, st
     return out
 
 

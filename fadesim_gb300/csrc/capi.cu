@@ -137,6 +137,11 @@ void plan_items(SolveArgs &a, int grid, int vectors_per_cta) {
     a.nitems = tiles * a.nchunks;
 }
 
+// Set by the host-buffer entry around each group's call: the group's device
+// counters (zeroed by the caller), so that no group reads its counters back
+// and the pipeline never waits on the host.
+thread_local DevStats *g_group_stats = nullptr;
+
 int finish_stats(DevStats *dst, fadesim_solve_stats *stats, cudaStream_t st) {
     if (!stats) return FADESIM_OK;
     DevStats h;
@@ -230,10 +235,10 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
     scr.st = st;
     const size_t bytes = scratch_floats * sizeof(float) + sizeof(DevStats) + 256;
     CUDA_TRY(lib_malloc_async(&scr.p, bytes, st));
-    DevStats *dst = reinterpret_cast<DevStats *>(scr.p);
+    DevStats *dst = g_group_stats ? g_group_stats : reinterpret_cast<DevStats *>(scr.p);
     a.stats = dst;
     a.scratch = reinterpret_cast<float *>(reinterpret_cast<char *>(scr.p) + 256);
-    CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(DevStats), st));
+    if (!g_group_stats) CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(DevStats), st));
     if (method == FADESIM_METHOD_LINE && ld) {
         CUDA_TRY(launch_line_relax(a, ld, dtype, grid, st));
     } else if (method == FADESIM_METHOD_LINE) {
@@ -243,7 +248,7 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
     } else {
         CUDA_TRY(launch_rbsor(a, dtype, grid, st));
     }
-    return finish_stats(dst, stats, st);
+    return g_group_stats ? FADESIM_OK : finish_stats(dst, stats, st);
 }
 
 int run_sweeps(int dtype, SolveArgs a, int iter_times, double gw, double beta, int enable_break, double thr,
@@ -291,6 +296,10 @@ int run_sweeps(int dtype, SolveArgs a, int iter_times, double gw, double beta, i
 }
 
 }  // namespace
+
+namespace fadesim {
+void set_group_stats(DevStats *d) { g_group_stats = d; }
+}  // namespace fadesim
 
 static thread_local const float *g_warm_init = nullptr;
 

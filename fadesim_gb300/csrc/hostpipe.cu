@@ -17,6 +17,7 @@
 
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "kernels.h"
 #include "trace.h"
@@ -66,6 +67,16 @@ struct SlotSet {
     }
 };
 
+// The group counters of one call, returned to the library's pool on every
+// return path (after the caller's stream has passed them).
+struct GroupStats {
+    fadesim::DevStats *d = nullptr;
+    cudaStream_t st = nullptr;
+    ~GroupStats() {
+        if (d) cudaFreeAsync(d, st);
+    }
+};
+
 int fail_cuda(const char *what, cudaError_t e) {
     std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
     return fadesim::report_error(FADESIM_E_CUDA, msg.c_str());
@@ -96,18 +107,32 @@ extern "C" int fadesim_ir_drop_gs_host(int dtype, const void *input, const void 
     const size_t in_x = n;
     const size_t out_x = ret_V == 2 ? (size_t)numY * 2 * n * m : ret_V == 1 ? (size_t)numY * n * m : (size_t)numY * m;
 
-    // group size: about 8 groups, in whole multiples of the SM count of tiles
+    // groups of numX: automatic -- about 8 groups in whole multiples of the SM
+    // count of tiles, with a first and a last group of one SM count each, so
+    // that the copy-in before the first solve and the copy-out after the last
+    // one (the only copies nothing overlaps) are short -- or group_x each
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    std::vector<int> gx0;  // first x of every group, then numX
     if (group_x <= 0) {
         const long long tiles = (long long)numX * numY;
         long long per = (tiles + 7) / 8;
         per = ((per + sms - 1) / sms) * sms;
         group_x = (int)((per + numY - 1) / numY);
+        const int edge = (sms + numY - 1) / numY;  // x values of one SM count of tiles
+        if (group_x > numX) group_x = numX;
+        if (numX > 2 * edge + group_x) {
+            gx0.push_back(0);
+            for (int x = edge; x < numX - edge; x += group_x) gx0.push_back(x);
+            gx0.push_back(numX - edge);
+        }
     }
     if (group_x > numX) group_x = numX;
-    const int ngroups = (numX + group_x - 1) / group_x;
+    if (gx0.empty())
+        for (int x = 0; x < numX; x += group_x) gx0.push_back(x);
+    const int ngroups = (int)gx0.size();
+    gx0.push_back(numX);
 
     const size_t gbytes = (size_t)group_x * g_x * es;
     const size_t ibytes = (size_t)batch_size * group_x * in_x * es;
@@ -115,6 +140,18 @@ extern "C" int fadesim_ir_drop_gs_host(int dtype, const void *input, const void 
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
 
     cudaStream_t caller = (cudaStream_t)stream;
+    // every group's device counters, zeroed on the caller's stream before the
+    // slots start and read back once at the end (converging methods; the sweep
+    // order reports through the per-group host stats)
+    GroupStats gstats;
+    gstats.st = caller;
+    if (stats) {
+        cudaError_t ea = fadesim::lib_malloc_async(reinterpret_cast<void **>(&gstats.d),
+                                                   (size_t)ngroups * sizeof(fadesim::DevStats), caller);
+        if (ea == cudaSuccess)
+            ea = cudaMemsetAsync(gstats.d, 0, (size_t)ngroups * sizeof(fadesim::DevStats), caller);
+        if (ea != cudaSuccess) return fail_cuda("group counters", ea);
+    }
     cudaEvent_t start;
     cudaError_t e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
     if (e != cudaSuccess) return fail_cuda("cudaEventCreateWithFlags", e);
@@ -139,8 +176,8 @@ extern "C" int fadesim_ir_drop_gs_host(int dtype, const void *input, const void 
     for (int g = 0; g < ngroups; ++g) {
         const int s = g % nslot;
         cudaStream_t st = slots.st[s];
-        const int x0 = g * group_x;
-        const int gx = numX - x0 < group_x ? numX - x0 : group_x;
+        const int x0 = gx0[g];
+        const int gx = gx0[g + 1] - x0;  // <= group_x
         char *dG = static_cast<char *>(slots.buf[s]);
         char *din = dG + al(gbytes);
         char *dout = din + al(ibytes);
@@ -150,11 +187,13 @@ extern "C" int fadesim_ir_drop_gs_host(int dtype, const void *input, const void 
         e = cudaMemcpy2DAsync(din, (size_t)gx * in_x * es, hin + (size_t)x0 * in_x * es, (size_t)numX * in_x * es,
                               (size_t)gx * in_x * es, (size_t)batch_size, cudaMemcpyHostToDevice, st);
         if (e != cudaSuccess) return fail_cuda("cudaMemcpy2DAsync (input)", e);
-        fadesim_solve_stats gs;
+        fadesim_solve_stats gs{0, 0, 0, 0, 0};
+        fadesim::set_group_stats(stats ? gstats.d + g : nullptr);
         const int rc = fadesim_ir_drop_gs_ex(dtype, din, dG, batch_size, row_size, col_size, gx, numY, iter_times,
                                              g_wire, beta, enable_break, break_threshould, nonlinear_cell_enable,
                                              nonlinear_params, n_nonlinear_params, ret_V, dout, opts,
                                              stats ? &gs : nullptr, nullptr, st);
+        fadesim::set_group_stats(nullptr);
         if (rc != FADESIM_OK) return rc;
         if (stats) {
             stats->solves += gs.solves;
@@ -171,6 +210,19 @@ extern "C" int fadesim_ir_drop_gs_host(int dtype, const void *input, const void 
     for (int s = 0; s < nslot; ++s) {
         e = cudaStreamSynchronize(slots.st[s]);
         if (e != cudaSuccess) return fail_cuda("cudaStreamSynchronize", e);
+    }
+    if (stats) {
+        // the converging groups' counters (all zero for the sweep order)
+        std::vector<fadesim::DevStats> h((size_t)ngroups);
+        e = cudaMemcpy(h.data(), gstats.d, (size_t)ngroups * sizeof(fadesim::DevStats), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail_cuda("cudaMemcpy (group counters)", e);
+        for (const fadesim::DevStats &d : h) {
+            stats->solves += (int64_t)d.solves;
+            stats->iters_sum += (int64_t)d.iters_sum;
+            if (d.iters_max > stats->iters_max) stats->iters_max = d.iters_max;
+            stats->status_or |= d.status_or;
+            stats->warm_rejected += (int64_t)d.warm_rejected;
+        }
     }
     return FADESIM_OK;
 }

@@ -89,6 +89,9 @@ bool conv3x3_tc_supported(const void *X, const void *Wt, const void *Y, int H, i
 cudaError_t conv3x3_fwd_tc(const void *X, const void *Wt, const float *bias, const void *skip, void *Y, int N, int H,
                            int W, int Cin, int Cout, int flags, int *err, cudaStream_t st);
 int *conv_tc_error_flag();
+// The host-buffer entry's per-group device counters for the next converging
+// solve on this thread (nullptr: the solve keeps and reads back its own).
+void set_group_stats(DevStats *d);
 // Tensor-core weight gradient dW[Cout][9][Cin] += (FP32 atomics): Cin and Cout
 // multiples of 32, Cout <= 128, W a power of two from 16 to 128, H a multiple
 // of 8, 16-byte aligned activations.

@@ -41,6 +41,25 @@ def test_host_currents_match_oracle(acc, group_x, pinned):
     assert st["solves"] == B * X * Y and st["status_or"] & 1 and not st["status_or"] & 2
 
 
+def test_host_status_from_device_counters(acc):
+    """The groups' counters stay on the device and come back once: the stats
+    cover every solve of every group, and an iteration cap far below what the
+    tolerance needs is reported (warning by default, error under "raise") as
+    for the device-buffer call."""
+    B, X, Y, n, m = 4, 9, 1, 64, 64
+    inp, G = case(11, B, X, Y, n, m)
+    ti, tg = torch.tensor(inp, dtype=torch.float32).pin_memory(), torch.tensor(G, dtype=torch.float32).pin_memory()
+    _, st = acc.ir_drop_gs_host(ti, tg, B, n, m, X, Y, g_wire=GW, group_x=2, return_stats=True)
+    assert st["solves"] == B * X * Y and st["status_or"] == 1 and st["iters_max"] >= 2
+    with pytest.warns(acc.SolveStatusWarning):
+        acc.ir_drop_gs_host(ti, tg, B, n, m, X, Y, g_wire=GW, group_x=2, max_iters=1)
+    with pytest.raises(acc.SolveStatusError):
+        acc.ir_drop_gs_host(ti, tg, B, n, m, X, Y, g_wire=GW, group_x=2, max_iters=1, check_status="raise")
+    _, st = acc.ir_drop_gs_host(ti, tg, B, n, m, X, Y, g_wire=GW, group_x=2, max_iters=1, check_status="off",
+                                return_stats=True)
+    assert st["solves"] == B * X * Y and st["status_or"] & 2
+
+
 @pytest.mark.parametrize("ret_V", [1, 2])
 def test_host_planes_layout_f64(acc, ret_V):
     B, X, Y, n, m = 2, 5, 3, 16, 12
