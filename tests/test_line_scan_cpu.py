@@ -142,3 +142,25 @@ def test_segmented_thomas_equals_dense_solve(C, NSEG, SEG):
         e_split = np.abs(got32 - exact).max()
         e_seq = np.abs(seq32 - exact).max()
         assert e_split <= 4 * e_seq + 1e-7 * np.abs(exact).max(), (e_split, e_seq)
+
+
+@pytest.mark.parametrize("C,NSEG,SEG", [(1, 4, 16), (1, 8, 32), (1, 16, 32)])
+def test_first_wordline_pass_from_unit_response(C, NSEG, SEG):
+    """The first wordline pass from the ideal state (csrc/line_impl.cuh
+    line_word_zero_unit; cluster_impl.cuh cl_word_pass modes 5 and 6): with
+    both planes zero its residual is -vin g / gw on every node, so its
+    correction equals -vin times the line's unit response T'^-1 (g / gw),
+    solved once per tile.  In FP32, through the kernels' segmented Thomas
+    split, the two agree to a few ulps of the correction."""
+    rng = np.random.default_rng(C * 7 + NSEG * 3 + SEG)
+    L = C * NSEG * SEG
+    T, cmul = system(rng, L, True)
+    gs = (np.diag(T) - np.where(np.arange(L) < L - 1, 2.0, 1.0)).astype(np.float32)
+    for vin in (0.2, 0.1375, 1.0):
+        direct = solve_line((np.float32(-vin) * gs).astype(np.float32), cmul, C, NSEG, SEG, np.float32)
+        unit = solve_line(gs.copy(), cmul, C, NSEG, SEG, np.float32)
+        via_unit = np.float32(-vin) * unit
+        exact = np.linalg.solve(T, -vin * gs.astype(np.float64))
+        scale = np.abs(exact).max()
+        assert np.abs(via_unit.astype(np.float64) - direct.astype(np.float64)).max() <= 1e-6 * scale
+        assert np.abs(via_unit.astype(np.float64) - exact).max() <= 1e-5 * scale
