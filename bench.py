@@ -191,6 +191,39 @@ def cpu_baseline(seconds=12.0, max_solves=4096):
                       "1e-6 V) over %d threads in %.1f s" % (done, threads, el)}
 
 
+def cpu_mixed_baseline(seconds_per_size=4.0, sizes=(64, 128, 256), tiles_by_size=None):
+    """The reference's Au solve on all host cores for the mixed-size batch,
+    extrapolated from a stratified sample: each tile size timed on its own
+    bounded sample (same cells, Bernoulli 0.2 V inputs, omega 1.95, delta tol
+    1e-9), the batch's rate then the harmonic combination by the batch's
+    share of each size."""
+    from oracle import augs
+    augs.build()
+    threads = augs.max_threads()
+    w = float(np.float32(1.95))
+    rates, notes = {}, []
+    for n in sizes:
+        rng = np.random.default_rng(100 + n)
+        G = (1.0 / R_STATES)[rng.integers(0, 4, (threads, n, n))].astype(np.float64)
+        v = (rng.integers(0, 2, (threads, n)) * V_READ).astype(np.float64)
+        done, t0 = 0, time.perf_counter()
+        while True:
+            augs.solve_many(G, v, R_WIRE, 200000, w, True, 1e-9)
+            done += threads
+            el = time.perf_counter() - t0
+            if el >= seconds_per_size:
+                break
+        rates[n] = done / el
+        notes.append("%d of %dx%d in %.1f s" % (done, n, n, el))
+    share = tiles_by_size or {n: 1 for n in sizes}
+    tot = float(sum(share[n] for n in sizes))
+    mix = tot / sum(share[n] / rates[n] for n in sizes)
+    return {"value": mix, "unit": UNIT, "cores": threads, "kind": "port",
+            "by_size": {str(n): rates[n] for n in sizes},
+            "sample": "stratified: " + ", ".join(notes) + " (Au lexicographic GS, omega 1.95, delta tol 1e-9, "
+                      "%d threads); the batch rate combines them by its tile shares" % threads}
+
+
 def workload_name(tiles):
     """The benchmarked workload, named the same way on both arms."""
     return ("%d tiles x %d vectors of 128x128 per rank (ir_drop_gs layout B=%d, numX=%d, numY=1), 4-state cells, "
@@ -470,6 +503,11 @@ def run_ours(args):
 
     # the mixed-size batch (tiles of 64, 128 and 256)
     mixed = mixed_batch(torch, args.tol) if not args.no_mixed else None
+    if mixed is not None and rank == 0 and world == 1:
+        # the reference's CPU algorithm on the same mix (stratified sample, host cores)
+        shares = {int(k): v for k, v in mixed["tiles_by_size"].items()}
+        mixed["cpu_baseline"] = cpu_mixed_baseline(tiles_by_size=shares)
+        mixed["speedup_vs_cpu_reference"] = mixed["solves_per_s"] / mixed["cpu_baseline"]["value"]
     large = large_nonideal(torch, acc) if not args.no_mixed else None
     # the layer-level MLP inference (PimTorch Linear_sp path on crossbars)
     mlp = None
