@@ -30,3 +30,20 @@ def test_fp32_roofline_arithmetic():
     assert r["unit"] == "TFLOP/s" and abs(r["peak"] - 256 * 152 * 2070e6 / 1e12) < 1e-9
     assert abs(r["achieved"] - 14 * 1.7314545664e10 / 24.26e-3 / 1e12) < 1e-9
     assert 0.11 < r["frac"] < 0.13
+
+
+def test_mixed_batch_cpu_baseline_combines_sizes_by_tile_share():
+    """The mixed-size batch's host-core rate: each size timed on its own
+    sample, the batch rate the harmonic combination weighted by tile shares
+    (time per tile of the batch = sum of share x time per tile of each size)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    shares = {8: 3, 16: 1}
+    r = bench.cpu_mixed_baseline(seconds_per_size=0.05, sizes=(8, 16), tiles_by_size=shares)
+    rates = {int(k): v for k, v in r["by_size"].items()}
+    assert set(rates) == {8, 16} and all(v > 0 for v in rates.values())
+    assert rates[8] > rates[16]
+    expect = 4.0 / (3.0 / rates[8] + 1.0 / rates[16])
+    assert abs(r["value"] - expect) <= 1e-12 * expect
+    assert min(rates.values()) <= r["value"] <= max(rates.values())
+    assert r["kind"] == "port" and r["cores"] >= 1 and r["sample"].startswith("stratified: ")
