@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "libfadesim_gb300.so")
 
 F32 = 0
 F64 = 1
-METHOD_AUTO, METHOD_LINE, METHOD_RBSOR, METHOD_SWEEPS = 0, 1, 2, 3
+METHOD_AUTO, METHOD_LINE, METHOD_RBSOR, METHOD_SWEEPS, METHOD_LINE_COARSE = 0, 1, 2, 3, 4
 ST_CONVERGED, ST_MAXITER, ST_NONFINITE, ST_WARM_REJECTED = 1, 2, 4, 8
 
 

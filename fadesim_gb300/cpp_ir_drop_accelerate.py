@@ -34,7 +34,7 @@ import torch
 from . import _lib
 
 _METHODS = {"auto": _lib.METHOD_AUTO, "line": _lib.METHOD_LINE, "rbsor": _lib.METHOD_RBSOR,
-            "sweeps": _lib.METHOD_SWEEPS}
+            "sweeps": _lib.METHOD_SWEEPS, "line_coarse": _lib.METHOD_LINE_COARSE}
 
 
 @dataclass

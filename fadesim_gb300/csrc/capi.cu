@@ -362,6 +362,11 @@ extern "C" int fadesim_ir_drop_gs_ex(int dtype, const void *input, const void *G
         a.ctl.noise_seed = opts->noise_seed;
     }
     int method = opts ? opts->method : FADESIM_METHOD_AUTO;
+    if (method == FADESIM_METHOD_LINE_COARSE) {
+        // the line method; its kernel takes the coarse correction on the tiles it suits
+        a.two_level = 1;
+        method = FADESIM_METHOD_LINE;
+    }
     if (method == FADESIM_METHOD_AUTO)
         method = (line_relax_ld(row_size, col_size) || cluster_relax_ld(row_size, col_size)) ? FADESIM_METHOD_LINE
                                                                                            : FADESIM_METHOD_SWEEPS;
@@ -437,7 +442,7 @@ extern "C" int fadesim_ir_drop_gs_warm(int dtype, const void *input, const void 
     if (!init) return fail(FADESIM_E_ARG, "init planes required");
     fadesim_solve_opts o = opts ? *opts : fadesim_solve_opts{};
     if (o.method == FADESIM_METHOD_AUTO) o.method = FADESIM_METHOD_LINE;
-    if (o.method != FADESIM_METHOD_LINE && o.method != FADESIM_METHOD_RBSOR)
+    if (o.method != FADESIM_METHOD_LINE && o.method != FADESIM_METHOD_LINE_COARSE && o.method != FADESIM_METHOD_RBSOR)
         return fail(FADESIM_E_UNSUPPORTED, "warm starts apply to the line and red-black SOR methods");
     g_warm_init = init;
     const int rc = fadesim_ir_drop_gs_ex(dtype, input, G, batch_size, row_size, col_size, numX, numY, 0, g_wire, 1.0,

@@ -136,6 +136,12 @@ __device__ __forceinline__ float warp_max(float v) {
     return v;
 }
 
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 __device__ __forceinline__ void record_solve(DevStats *st, int *iters_out, long long solve_idx, int iters,
                                              int status) {
     if (iters_out) iters_out[solve_idx] = iters;

@@ -24,6 +24,8 @@ struct SolveArgs {
     DevStats *stats;    // optional
     const float *init;  // optional warm start: deviation planes [B, numX, numY, 2, n, m] (u - vin, d)
     int f64;            // input, G and out are FP64 (else FP32); the solve itself is FP32
+    int two_level;      // the two-level line relaxation (coarse correction) on full 128 x 128 tiles
+                        // with linear cells whose cells couple the planes strongly
 };
 
 // Record msg as the message of fadesim_last_error() and return code.

@@ -178,7 +178,9 @@ struct LineStop {
     // First-step rate of the finished solve, to seed the next vector of the tile.
     __device__ __forceinline__ float final_rate() const { return first > 0.f ? first : hint; }
 
-    __device__ __forceinline__ bool update(float delta, float vm, float tol) {
+    // FLOOR: rho taken at least rho_floor (the two-level method).
+    template <bool FLOOR = false>
+    __device__ __forceinline__ bool update(float delta, float vm, float tol, float rho_floor = 0.f) {
         ++it;
         const float prev = h0;
         h3 = h2;
@@ -191,6 +193,7 @@ struct LineStop {
         const float rate3 = (it >= 4 && h3 > 0.f) ? cbrtf(delta / h3) : 0.f;
         rho = fmaxf(fmaxf(ratio, rate3), omega - 1.f);
         if (omega > 1.f) rho = fmaxf(rho, 0.5f);
+        if (FLOOR) rho = fmaxf(rho, rho_floor);
         if (it == 2) first = ratio;
         const float est = rho < 0.999f ? __fdividef(delta * rho, 1.f - rho) : INFINITY;
         const bool stalled = delta <= floor_v && ratio >= 0.9f;

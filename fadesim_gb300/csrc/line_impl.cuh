@@ -36,6 +36,7 @@
 #pragma once
 #include <math.h>
 
+#include "coarse_impl.cuh"
 #include "kernels.h"
 #include "line_common.cuh"
 
@@ -87,12 +88,16 @@ __device__ __forceinline__ int vpad(int p) { return p + (p >> 4); }
 // UNIT: instead, the response of every line to its own cell conductances,
 // T'^-1 (g / gw), written to own[k * T + tid] in the pass threads' order (the
 // first wordline pass from the ideal state is -vin times it, linear cells).
-template <int LD, bool WORD, int RES, bool NL, bool FULL, bool ZOWN, bool ZOTH, bool UNIT = false>
+// RST (bitline pass of a full 128 x 128 tile, linear cells): also restrict the
+// wordline residual the correction leaves, g / gw times it, onto the coarse
+// grid of the two-level method (accumulated into crs).
+template <int LD, bool WORD, int RES, bool NL, bool FULL, bool ZOWN, bool ZOTH, bool UNIT = false, bool RST = false>
 __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *__restrict__ oth,
                                           const float *__restrict__ Gs, const float *__restrict__ vin_s,
                                           const float *__restrict__ cm, const float *__restrict__ segprod,
                                           int L_in, int NLINES_in, float inv_gw, float omega, float &dmax, float &vmax,
-                                          const SolveCtl &ctl) {
+                                          const SolveCtl &ctl, float *__restrict__ crs = nullptr) {
+    static_assert(!RST || (LD == 128 && !WORD && !NL && FULL && !UNIT), "coarse restriction: 128 bitline pass");
     const int L = FULL ? LD : L_in;
     const int NLINES = FULL ? LD : NLINES_in;
     constexpr int SEG = LineCfg<LD>::SEG;
@@ -214,6 +219,11 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
     // ---- apply the correction ----------------------------------------------
     // (a NaN correction is not seen by fmaxf; the output stage flags it)
     float dm = 0.f;
+    float S[COARSE_SLOTS];
+    if constexpr (RST) {
+#pragma unroll
+        for (int a = 0; a < COARSE_SLOTS; ++a) S[a] = 0.f;
+    }
 #pragma unroll
     for (int k = 0; k < SEG; ++k) {
         const int p = p0 + k;
@@ -223,9 +233,63 @@ __device__ __forceinline__ void line_pass(float *__restrict__ own, const float *
             own[q] = nv;
             dm = fmaxf(dm, fabsf(x[k]));
             vmax = fmaxf(vmax, fabsf(nv));
+            if constexpr (RST) {
+                const float r = Gs[q] * (omega * x[k]);
+                const float t = coarse_t(k);
+                S[coarse_lo_slot(k)] = fmaf(1.f - t, r, S[coarse_lo_slot(k)]);
+                S[coarse_lo_slot(k) + 1] = fmaf(t, r, S[coarse_lo_slot(k) + 1]);
+                // hand each slot on as soon as it is complete (fewer live registers)
+                if (coarse_slot_done_after(k)) coarse_restrict_slot(S[k >> 3], k >> 3, crs, line, s);
+            }
         }
     }
     dmax = fmaxf(dmax, omega * dm);
+    if constexpr (RST) {
+        coarse_restrict_slot(S[4], 4, crs, line, s);
+        coarse_restrict_slot(S[5], 5, crs, line, s);
+    }
+}
+
+// The coarse correction of the two-level method added to both planes: node
+// (i, j) gets sum_I sum_J phi_I(i) phi_J(j) E[I][J] (E in shared memory, row
+// stride COARSE_EST), threads in the bitline pass's layout.  Returns the
+// thread's largest |correction|.
+template <int LD>
+__device__ __forceinline__ float line_coarse_apply(float *__restrict__ U, float *__restrict__ D,
+                                                   const float *__restrict__ E) {
+    static_assert(LD == 128, "the coarse correction is built for 128 x 128 tiles");
+    constexpr int SEG = LineCfg<LD>::SEG;
+    constexpr int LPW = LineCfg<LD>::LPW;
+    const int tid = threadIdx.x;
+    const int lane = tid & 31;
+    const int s = lane / LPW;
+    const int line = (tid >> 5) * LPW + (lane % LPW);
+    const int p0 = s * SEG;
+    constexpr int V = 8;
+    int Rb[V];
+#pragma unroll
+    for (int t = 0; t < V; ++t) Rb[t] = swz<LD>(p0 + t, line) - t * LD;
+    // the bitline's column weights, then its values on the segment's six coarse rows
+    const int l = line & 7, w = line >> 3;
+    const float tj = l < 4 ? ((float)l + 4.5f) * 0.125f : ((float)l - 3.5f) * 0.125f;
+    const int J0 = coarse_clamp(l < 4 ? w - 1 : w), J1 = coarse_clamp(l < 4 ? w : w + 1);
+    float Ej[COARSE_SLOTS];
+#pragma unroll
+    for (int a = 0; a < COARSE_SLOTS; ++a) {
+        const int I = coarse_clamp(4 * s - 1 + a);
+        Ej[a] = fmaf(1.f - tj, E[I * COARSE_EST + J0], tj * E[I * COARSE_EST + J1]);
+    }
+    float pm = 0.f;
+#pragma unroll
+    for (int k = 0; k < SEG; ++k) {
+        const float t = coarse_t(k);
+        const float pe = fmaf(1.f - t, Ej[coarse_lo_slot(k)], t * Ej[coarse_lo_slot(k) + 1]);
+        const int q = Rb[k % V] + k * LD;
+        U[q] += pe;
+        D[q] += pe;
+        pm = fmaxf(pm, fabsf(pe));
+    }
+    return pm;
 }
 
 // Chain multipliers gw / pivot of every line of the tile, written in the order
@@ -315,10 +379,10 @@ __host__ __device__ constexpr bool unit_first() { return LD < 128; }
 
 // One iteration: every wordline, then every bitline.  ZERO: both planes are
 // still zero (first iteration from the ideal state).
-template <int LD, int RES, bool NL, bool FULL, bool ZERO>
+template <int LD, int RES, bool NL, bool FULL, bool ZERO, bool RST = false>
 __device__ __forceinline__ void line_iteration(float *U, float *D, const float *Gs, const float *vin_s,
                                                const float *piv, int n, int m, float inv_gw, float omega,
-                                               float &dmax, float &vmax, const SolveCtl &ctl) {
+                                               float &dmax, float &vmax, const SolveCtl &ctl, float *crs = nullptr) {
     constexpr int SEG = LineCfg<LD>::SEG;
     constexpr int T = LineCfg<LD>::T;
     if constexpr (ZERO && !NL && unit_first<LD>())
@@ -327,8 +391,9 @@ __device__ __forceinline__ void line_iteration(float *U, float *D, const float *
         line_pass<LD, true, RES, NL, FULL, ZERO, ZERO>(U, D, Gs, vin_s, piv, piv + 2 * SEG * T, m, n, inv_gw, omega,
                                                        dmax, vmax, ctl);
     __syncthreads();
-    line_pass<LD, false, RES, NL, FULL, ZERO, false>(D, U, Gs, vin_s, piv + SEG * T, piv + 2 * SEG * T + T, n, m,
-                                                     inv_gw, omega, dmax, vmax, ctl);
+    line_pass<LD, false, RES, NL, FULL, ZERO, false, false, RST>(D, U, Gs, vin_s, piv + SEG * T,
+                                                                 piv + 2 * SEG * T + T, n, m, inv_gw, omega, dmax,
+                                                                 vmax, ctl, crs);
 }
 
 // Largest of one value per thread, the same in every thread (two barriers).
@@ -398,17 +463,23 @@ __device__ __forceinline__ void line_outputs(const SolveArgs &a, const float *Gs
     }
 }
 
-template <int LD, bool NL, bool FULL>
+// TWO: the two-level method (coarse correction after every iteration) on the
+// tiles whose cells couple the planes strongly (sum of g / gw over the tile at
+// least 3); full 128 x 128 tiles with linear cells.
+template <int LD, bool NL, bool FULL, bool TWO = false>
 __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_kernel(SolveArgs a) {
+    static_assert(!TWO || (LD == 128 && !NL && FULL), "the two-level method is built for full 128 x 128 tiles");
     constexpr int T = LineCfg<LD>::T;
     constexpr int NW = LineCfg<LD>::NW;
     constexpr int SEG = LineCfg<LD>::SEG;
+    constexpr int NRED = TWO ? 3 : 2;  // per-warp maxima: correction, deviation (, coarse correction)
     extern __shared__ float4 smem4[];
     float *Gs = reinterpret_cast<float *>(smem4);
     float *U = Gs + LD * LD;
     float *D = U + LD * LD;
     float *vin_s = D + LD * LD;
-    float *red = vin_s + LD + LD / 16;  // [2][2][NW]
+    float *red = vin_s + LD + LD / 16;  // [2][NRED][NW]
+    float *coarse_s = red + 2 * NRED * NW;  // TWO: the coarse step's tables and buffers
     __shared__ int nonfinite_flag;
     __shared__ float bmax_scratch[NW];
 
@@ -440,6 +511,8 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
         st_or = 0;
         nonfinite_flag = 0;
     }
+    bool two_tile = false;  // TWO: this tile takes the coarse correction
+    if constexpr (TWO) coarse_load_tables(coarse_s);  // (the first claim's barrier orders it)
 
     // work queue: every CTA claims its next (tile, vector chunk) item from the
     // call's counter, so CTAs that finish early take more items
@@ -483,6 +556,17 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     gm = fmaxf(gm, fabsf(gsv));
                 }
                 gs_max = block_max<NW>(gm, bmax_scratch);
+                if constexpr (TWO) {
+                    // coupling strength: the sum of g / gw over the tile (mean g / gw times
+                    // the square of the line length); the coarse correction pays from ~3
+                    float gsum = 0.f;
+                    for (int e = tid; e < n * m; e += T) gsum += Gs[swz<LD>(e / m, e - (e / m) * m)];
+                    gsum = warp_sum(gsum);
+                    __syncthreads();
+                    if ((tid & 31) == 0) bmax_scratch[tid >> 5] = gsum;
+                    __syncthreads();
+                    two_tile = warp_sum((tid & 31) < NW ? bmax_scratch[tid & 31] : 0.f) >= 3.f;
+                }
                 if constexpr (unit_first<LD>()) {
                     // the wordline unit response w1 = T'^-1 (g / gw) of every row (each
                     // thread writes and later reads only its own entries)
@@ -520,6 +604,11 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             }
             if (tid < LD)
                 vin_s[vpad(tid)] = (tid < n) ? load_io(a.input, ((size_t)b * a.numX + x) * n + tid, f64) : 0.f;
+            if constexpr (TWO) {
+                // no coarse correction precedes the first iteration
+                if (tid < 256) CoarseSmem(coarse_s).R[tid] = 0.f;
+                if (tid < NW) red[2 * NW + tid] = red[(NRED + 2) * NW + tid] = 0.f;
+            }
             __syncthreads();
             // precise iterations may keep the cell term in FP32 (RES 3) when its
             // rounding, amplified by at most L^2/2 through a line solve, stays 8x
@@ -543,31 +632,36 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 }
                 __syncthreads();
             }
+            // (the two-level method runs at omega 1: its error is no SOR mode)
             LineStop stop;
-            stop.init(a.ctl.omega, rate_hint, omega_prev);
+            stop.init((TWO && two_tile) ? 1.f : a.ctl.omega, rate_hint, omega_prev);
             float omega = stop.omega, omega_last = omega;
             bool res64 = precise_first;
             int status = 0, it = 0, par = 0;
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
                 omega_last = omega;
-                if (zero) line_iteration<LD, 0, NL, FULL, true>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
-                else if (!res64) line_iteration<LD, 0, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
-                else if (semi) line_iteration<LD, 3, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
-                else if (ff) line_iteration<LD, 2, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
-                else line_iteration<LD, 1, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                float *crs = TWO ? CoarseSmem(coarse_s).R : nullptr;
+                if (zero) line_iteration<LD, 0, NL, FULL, true, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                else if (!res64) line_iteration<LD, 0, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                else if (semi) line_iteration<LD, 3, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                else if (ff) line_iteration<LD, 2, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                else line_iteration<LD, 1, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
                 zero = false;
                 dmax = warp_max(dmax);
                 vmax = warp_max(vmax);
                 if ((tid & 31) == 0) {
-                    red[(par * 2 + 0) * NW + (tid >> 5)] = dmax;
-                    red[(par * 2 + 1) * NW + (tid >> 5)] = vmax;
+                    red[(par * NRED + 0) * NW + (tid >> 5)] = dmax;
+                    red[(par * NRED + 1) * NW + (tid >> 5)] = vmax;
                 }
                 __syncthreads();
                 // every warp reduces the NW partial maxima itself (no second barrier)
                 const int ln = tid & 31;
-                float delta = warp_max(ln < NW ? red[(par * 2 + 0) * NW + ln] : 0.f);
-                float vm = warp_max(ln < NW ? red[(par * 2 + 1) * NW + ln] : 0.f);
+                float delta = warp_max(ln < NW ? red[(par * NRED + 0) * NW + ln] : 0.f);
+                float vm = warp_max(ln < NW ? red[(par * NRED + 1) * NW + ln] : 0.f);
+                // the two-level method's step is the fine corrections plus the
+                // coarse correction before them (its per-warp maxima, or zeros)
+                if constexpr (TWO) delta += warp_max(ln < NW ? red[(par * NRED + 2) * NW + ln] : 0.f);
                 if (it == 0 && !precise_first) semi = semi_now();
                 par ^= 1;
                 ++it;
@@ -579,6 +673,10 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     // the prediction moved as much as the solution is large: discard
                     // it and start again from the ideal state
                     __syncthreads();
+                    if constexpr (TWO) {
+                        if (tid < 256) CoarseSmem(coarse_s).R[tid] = 0.f;
+                        if (tid < NW) red[2 * NW + tid] = red[(NRED + 2) * NW + tid] = 0.f;
+                    }
                     if (precise_first) {
                         for (int e = tid; e < LD * LD; e += T) {
                             U[e] = 0.f;
@@ -589,12 +687,16 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                     zero = !precise_first;
                     warm = false;
                     status |= FADESIM_ST_WARM_REJECTED;
-                    stop.init(a.ctl.omega, rate_hint, omega_prev);
+                    stop.init((TWO && two_tile) ? 1.f : a.ctl.omega, rate_hint, omega_prev);
                     omega = stop.omega;
                     res64 = precise_first;
                     continue;
                 }
-                const bool small = stop.update(delta, vm, tol);
+                // (two-level: the rate taken at least 0.2 -- its steps shrink by
+                // ~0.1 per iteration, and a single small one can hide a larger error)
+                bool small;
+                if constexpr (TWO) small = stop.update<true>(delta, vm, tol, two_tile ? 0.2f : 0.f);
+                else small = stop.update(delta, vm, tol);
                 omega = stop.omega;
                 if (small) {
                     // the final test must pass on an iteration whose residual was
@@ -612,6 +714,21 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 if (it >= maxit) {
                     status |= FADESIM_ST_MAXITER;
                     break;
+                }
+                if constexpr (TWO) {
+                    // another iteration follows: correct the smooth, plane-locked error
+                    // on the coarse grid first (the reduction barrier completed R)
+                    const CoarseSmem cc(coarse_s);
+                    if (two_tile) {
+                        coarse_solve(cc);
+                        // its largest value joins the next iteration's step (par: that
+                        // iteration's slots, read two iterations ago)
+                        const float pm = warp_max(line_coarse_apply<LD>(U, D, cc.E));
+                        if ((tid & 31) == 0) red[(par * NRED + 2) * NW + (tid >> 5)] = pm;
+                        __syncthreads();
+                    } else if (tid < 256) {
+                        cc.R[tid] = 0.f;  // (the next wordline pass's barrier orders it)
+                    }
                 }
             }
             rate_hint = stop.final_rate();
@@ -662,6 +779,13 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
 // Instantiations: linear cells on any tile, linear cells on a full LD x LD
 // tile, sinh cells on any tile.
 inline size_t line_relax_smem_ld(int ld, int nw) { return (size_t)(3 * ld * ld + ld + ld / 16 + 4 * nw) * sizeof(float); }
+// the two-level kernel: a third per-warp maximum and the coarse step's buffers
+inline size_t line_relax_smem_two(int ld, int nw) {
+    return line_relax_smem_ld(ld, nw) + (size_t)(2 * nw + COARSE_SMEM_FLOATS) * sizeof(float);
+}
+// The two-level kernel on full 128 x 128 tiles with linear cells (linegs_128c.cu).
+cudaError_t line_relax_prepare_128_coarse();
+cudaError_t launch_line_relax_128_coarse(const SolveArgs &a, int grid, cudaStream_t st);
 
 template <int LD>
 cudaError_t line_relax_prepare_t() {
@@ -672,6 +796,9 @@ cudaError_t line_relax_prepare_t() {
         e = cudaFuncSetAttribute(line_relax_kernel<LD, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(line_relax_kernel<LD, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if constexpr (LD == 128) {
+        if (e == cudaSuccess) e = line_relax_prepare_128_coarse();
+    }
     return e;
 }
 
@@ -684,6 +811,9 @@ cudaError_t line_relax_occupancy_t(int *n) {
 template <int LD>
 cudaError_t launch_line_relax_t(const SolveArgs &a, int grid, cudaStream_t st) {
     const size_t sm = line_relax_smem_ld(LD, LineCfg<LD>::NW);
+    if constexpr (LD == 128) {
+        if (!a.ctl.nl && a.two_level && a.n == LD && a.m == LD) return launch_line_relax_128_coarse(a, grid, st);
+    }
     if (a.ctl.nl) line_relax_kernel<LD, true, false><<<grid, LineCfg<LD>::T, sm, st>>>(a);
     else if (a.n == LD && a.m == LD) line_relax_kernel<LD, false, true><<<grid, LineCfg<LD>::T, sm, st>>>(a);
     else line_relax_kernel<LD, false, false><<<grid, LineCfg<LD>::T, sm, st>>>(a);

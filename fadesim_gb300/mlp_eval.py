@@ -10,9 +10,11 @@ an 8-bit ADC and shift-add (fixedPoint/nn/modules/linear_split.py,
 splitArrayArithmetic.py:1161-1260).  ReLU between layers, no bias.
 
 ``run`` times one batch through the three layers with a given solver strategy:
-"direct" solves every (tile, input vector) pair; "superposition" solves each
-tile's unit responses and forms the currents by linearity (linear cells, no
-read noise).
+"direct" solves every (tile, input vector) pair; "direct_coarse" does the same
+with the two-level line relaxation (method "line_coarse": a coarse-grid
+correction after every iteration on the strongly coupled tiles);
+"superposition" solves each tile's unit responses and forms the currents by
+linearity (linear cells, no read noise).
 
   python -m fadesim_gb300.mlp_eval [--batch 256]
 """
@@ -55,19 +57,26 @@ def forward(x, weights, cfg, solver):
 
 
 def run(batch=256, strategy="direct", seed=3, reps=1):
+    from . import cpp_ir_drop_accelerate as acc
     cfg = config()
     weights = build(seed)
     g = torch.Generator().manual_seed(seed + 1)
     x = torch.randint(0, 256, (batch, SIZES[0]), generator=g).float().cuda()
-    solver = splitarr.default_solver(cfg) if strategy == "direct" else splitarr.superposition_solver(cfg)
-    y = forward(x, weights, cfg, solver)  # warm-up (builds, tunes nothing)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for _ in range(reps):
-        y = forward(x, weights, cfg, solver)
-    e1.record()
-    torch.cuda.synchronize()
+    solver = splitarr.superposition_solver(cfg) if strategy == "superposition" else splitarr.default_solver(cfg)
+    method = acc.options.method
+    if strategy == "direct_coarse":
+        acc.options.method = "line_coarse"
+    try:
+        y = forward(x, weights, cfg, solver)  # warm-up (builds, tunes nothing)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            y = forward(x, weights, cfg, solver)
+        e1.record()
+        torch.cuda.synchronize()
+    finally:
+        acc.options.method = method
     ms = e0.elapsed_time(e1) / reps
     per_layer = solves_per_batch(batch, cfg)
     return y, {"ms_per_batch": ms, "solves_per_batch": sum(per_layer), "solves_per_layer": per_layer,
@@ -105,6 +114,8 @@ def evaluate(batch=256):
     comparison between two tolerances of the direct solve."""
     from . import cpp_ir_drop_accelerate as acc
     yd, direct = run(batch, "direct")
+    yc, coarse = run(batch, "direct_coarse")
+    coarse["equal_outputs_frac_vs_direct"] = float(((yd - yc).abs() == 0).float().mean().item())
     ys, sup = run(batch, "superposition")
     diff = (yd - ys).abs()
     sup["max_rel_current_diff_vs_direct"] = current_agreement(batch)
@@ -118,7 +129,8 @@ def evaluate(batch=256):
     direct["equal_outputs_frac_vs_tol_x0.02"] = float(((yd - yt).abs() == 0).float().mean().item())
     direct["tol_v"] = tol
     return {"workload": "MLP 784-512-512-10, batch %d, 128x128 PN crossbars, 2-bit cells (1k/1M ohm), 8 input "
-                        "cycles at 0.2 V, 8-bit ADC" % batch, "direct": direct, "superposition": sup}
+                        "cycles at 0.2 V, 8-bit ADC" % batch, "direct": direct, "direct_coarse": coarse,
+            "superposition": sup}
 
 
 if __name__ == "__main__":
