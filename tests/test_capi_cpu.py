@@ -131,3 +131,15 @@ def test_warm_start_bindings_match_the_header():
 def test_every_declared_function_has_a_binding():
     from fadesim_gb300 import _lib, warmstart
     assert set(_declarations()) == set(_lib.EXPORTS) | set(warmstart._SIGS)
+
+
+def test_constants_match_the_header():
+    """The Python side's dtype, method and status codes are the header's #defines."""
+    from fadesim_gb300 import _lib
+    src = open(os.path.join(ROOT, "include", "fadesim_gb300.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define\s+FADESIM_([A-Z0-9_]+)\s+\(?(-?\d+)\)?", src)}
+    for name in ("F32", "F64", "METHOD_AUTO", "METHOD_LINE", "METHOD_RBSOR", "METHOD_SWEEPS", "METHOD_LINE_COARSE",
+                 "ST_CONVERGED", "ST_MAXITER", "ST_NONFINITE", "ST_WARM_REJECTED"):
+        assert getattr(_lib, name) == defs[name], name
+    from fadesim_gb300 import cpp_ir_drop_accelerate as acc
+    assert set(acc._METHODS.values()) == {defs[k] for k in defs if k.startswith("METHOD_")}
