@@ -777,7 +777,8 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
 
 // Launch helpers for one tile size (instantiated by linegs_<LD>.cu).
 // Instantiations: linear cells on any tile, linear cells on a full LD x LD
-// tile, sinh cells on any tile.
+// tile, sinh cells on any tile; for LD 128 also the two-level kernel on a full
+// tile of linear cells (linegs_128c.cu).
 inline size_t line_relax_smem_ld(int ld, int nw) { return (size_t)(3 * ld * ld + ld + ld / 16 + 4 * nw) * sizeof(float); }
 // the two-level kernel: a third per-warp maximum and the coarse step's buffers
 inline size_t line_relax_smem_two(int ld, int nw) {
