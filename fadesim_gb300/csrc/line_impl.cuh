@@ -705,7 +705,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 // (two-level: the rate taken at least 0.2 -- its steps shrink by
                 // ~0.1 per iteration, and a single small one can hide a larger error)
                 bool small;
-                if constexpr (TWO) small = stop.update<true>(delta, vm, tol, two_tile ? 0.2f : 0.f);
+                if constexpr (TWO) small = stop.update<true>(delta, vm, tol, two_tile ? 0.2f : 0.f, a.fp32_limit != 0);
                 else small = stop.update(delta, vm, tol);
                 omega = stop.omega;
                 if (small) {
