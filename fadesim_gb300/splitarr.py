@@ -112,7 +112,7 @@ def default_solver(cfg, tol_v=None, method=None, fp32_limit=None):
     return solve
 
 
-def superposition_solver(cfg):
+def superposition_solver(cfg, fp32_limit=True):
     """IR-drop currents by linearity, for linear cells without read noise.
 
     The bitline currents of a tile are then a linear map of its wordline
@@ -122,11 +122,13 @@ def superposition_solver(cfg):
     vector's currents are one FP32 matrix product: rows solves per tile instead
     of one per vector, exact up to the solver tolerance.  A vector's currents
     sum up to ``rows`` unit responses, so these are solved 500x tighter than the
-    module tolerance, and on full 128 x 128 tiles with the two-level method to
-    the FP32 limit: a unit response's currents come from the bitline ends,
-    small nodes that keep converging after the largest ones reach the FP32
-    floor (4 ulps of the largest deviation), where the plain stop test would
-    leave them ~1e-5 of their own size off.  Used with the same
+    module tolerance, and (``fp32_limit``, the default) on full 128 x 128 tiles
+    with the two-level method to the FP32 limit: a unit response's currents
+    come from the bitline ends, small nodes that keep converging after the
+    largest ones reach the FP32 floor (4 ulps of the largest deviation), where
+    the plain stop test leaves them up to ~3e-4 of their own size off (the
+    currents then differ from direct solves by ~1e-4 of the largest instead of
+    ~1e-6, at ~1/4 of the time).  Used with the same
     (v, G, B, rows, cols, numX, numY, out) interface as ``default_solver``; calls
     with no more vectors than rows solve directly."""
     direct = default_solver(cfg)
@@ -142,7 +144,7 @@ def superposition_solver(cfg):
         unit = torch.zeros((rows, numX, rows), dtype=v.dtype, device=v.device)
         r = torch.arange(rows, device=v.device)
         unit[r, :, r] = lv
-        full = rows == 128 and cols == 128
+        full = fp32_limit and rows == 128 and cols == 128
         M = default_solver(cfg, tol_v=_acc.options.tol_v * 2e-3, method="line_coarse" if full else None,
                            fp32_limit=True if full else None)(unit, G, rows, rows, cols, numX, numY, None)
         M = M.reshape(rows, numX, numY * cols).permute(1, 0, 2) * (1.0 / lv)
