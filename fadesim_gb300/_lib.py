@@ -19,7 +19,7 @@ class SolveOpts(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("tol_v", ctypes.c_double), ("max_iters", ctypes.c_int),
                 ("residual_period", ctypes.c_int), ("omega", ctypes.c_double), ("vectors_per_cta", ctypes.c_int),
                 ("residual_kind", ctypes.c_int), ("read_noise_sigma", ctypes.c_double),
-                ("noise_seed", ctypes.c_ulonglong), ("kernel_ld", ctypes.c_int)]
+                ("noise_seed", ctypes.c_ulonglong), ("kernel_ld", ctypes.c_int), ("fp32_limit", ctypes.c_int)]
 
 
 class SolveStats(ctypes.Structure):

@@ -51,6 +51,7 @@ class SolverOptions:
     noise_seed: int = 0
     check_status: str = os.environ.get("FADESIM_CHECK_STATUS", "warn")  # "warn", "raise" or "off"
     kernel_ld: int = 0           # 0: layout by tile size; 32/64/128 tile per CTA, 256/512 tile per cluster
+    fp32_limit: bool = False     # line_coarse, full 128x128 tiles: iterate past the FP32 floor until the corrections stall
 
     def to_c(self, method=None):
         m = method if method is not None else self.method
@@ -61,7 +62,7 @@ class SolverOptions:
         return _lib.SolveOpts(_METHODS[m], float(self.tol_v), int(self.max_iters), int(self.residual_period),
                               float(self.omega), int(self.vectors_per_cta), 1 if self.residual == "fp64" else 0,
                               float(self.read_noise_sigma), int(self.noise_seed) & (2 ** 64 - 1),
-                              int(self.kernel_ld))
+                              int(self.kernel_ld), 1 if self.fp32_limit else 0)
 
 
 options = SolverOptions()
@@ -189,7 +190,7 @@ def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_tim
                   enable_break=False, break_threshould=1e-7, nonlinear_cell_enable=False, nonlinear_params=(),
                   ret_V=False, method=None, tol_v=None, max_iters=None, residual_period=None, omega=None,
                   vectors_per_cta=None, residual=None, read_noise_sigma=None, noise_seed=None, kernel_ld=None,
-                  return_stats=True, return_iters=False, out=None):
+                  fp32_limit=None, return_stats=True, return_iters=False, out=None):
     """``ir_drop_gs`` with explicit solver options (``ret_V=2`` returns both node
     planes, [batch, numX, numY, 2, rows, cols]).  Returns (out, stats, iters):
     stats is a dict (solves, iters_sum, iters_max, status_or) and iters an int32
@@ -198,7 +199,7 @@ def ir_drop_gs_ex(input, G, batch_size, row_size, col_size, numX, numY, iter_tim
     o = SolverOptions(**{k: v for k, v in vars(options).items()})
     for k, v in dict(tol_v=tol_v, max_iters=max_iters, residual_period=residual_period, omega=omega,
                      vectors_per_cta=vectors_per_cta, residual=residual, read_noise_sigma=read_noise_sigma,
-                     noise_seed=noise_seed, kernel_ld=kernel_ld).items():
+                     noise_seed=noise_seed, kernel_ld=kernel_ld, fp32_limit=fp32_limit).items():
         if v is not None:
             setattr(o, k, v)
     out, st, it = _solve(input, G, batch_size, row_size, col_size, numX, numY, iter_times, g_wire, beta,

@@ -162,6 +162,7 @@ int run_converging(int method, int dtype, SolveArgs a, const fadesim_solve_opts 
     a.ctl.residual_period = opts ? opts->residual_period : 0;  // 0: adaptive schedule
     a.ctl.residual_ff = (opts && opts->residual_kind == 1) ? 0 : 1;
     a.ctl.precise_margin = precise_margin();
+    a.fp32_limit = (opts && opts->fp32_limit) ? 1 : 0;
     const int sms = device_sms();
     int grid = 0, ld = 0;
     size_t scratch_floats = 0;

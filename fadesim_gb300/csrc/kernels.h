@@ -26,6 +26,7 @@ struct SolveArgs {
     int f64;            // input, G and out are FP64 (else FP32); the solve itself is FP32
     int two_level;      // the two-level line relaxation (coarse correction) on full 128 x 128 tiles
                         // with linear cells whose cells couple the planes strongly
+    int fp32_limit;     // two-level kernel: iterate past the FP32 floor until the corrections stall
 };
 
 // Record msg as the message of fadesim_last_error() and return code.

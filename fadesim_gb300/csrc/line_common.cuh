@@ -178,9 +178,13 @@ struct LineStop {
     // First-step rate of the finished solve, to seed the next vector of the tile.
     __device__ __forceinline__ float final_rate() const { return first > 0.f ? first : hint; }
 
-    // FLOOR: rho taken at least rho_floor (the two-level method).
+    // FLOOR: rho taken at least rho_floor (the two-level method); there, with
+    // fp32_limit, the floor does not end the iteration: it runs until the
+    // corrections stop shrinking (under 15% progress over three iterations)
+    // below it, or the estimate meets the tolerance.
     template <bool FLOOR = false>
-    __device__ __forceinline__ bool update(float delta, float vm, float tol, float rho_floor = 0.f) {
+    __device__ __forceinline__ bool update(float delta, float vm, float tol, float rho_floor = 0.f,
+                                           bool fp32_limit = false) {
         ++it;
         const float prev = h0;
         h3 = h2;
@@ -210,6 +214,7 @@ struct LineStop {
                 }
             }
         }
+        if (FLOOR && fp32_limit) return est <= tol || (delta <= floor_v && it >= 4 && delta >= 0.85f * h3);
         return est <= fmaxf(tol, floor_v) || stalled;
     }
 };

@@ -641,12 +641,22 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
             while (true) {
                 float dmax = 0.f, vmax = 0.f;
                 omega_last = omega;
+                // (TWO: the bitline pass restricts the residual only on the tiles that
+                // take the coarse correction; the others run the plain passes)
                 float *crs = TWO ? CoarseSmem(coarse_s).R : nullptr;
-                if (zero) line_iteration<LD, 0, NL, FULL, true, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
-                else if (!res64) line_iteration<LD, 0, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
-                else if (semi) line_iteration<LD, 3, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
-                else if (ff) line_iteration<LD, 2, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
-                else line_iteration<LD, 1, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                if (TWO && two_tile) {
+                    if (zero) line_iteration<LD, 0, NL, FULL, true, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                    else if (!res64) line_iteration<LD, 0, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                    else if (semi) line_iteration<LD, 3, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                    else if (ff) line_iteration<LD, 2, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                    else line_iteration<LD, 1, NL, FULL, false, TWO>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl, crs);
+                } else {
+                    if (zero) line_iteration<LD, 0, NL, FULL, true>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                    else if (!res64) line_iteration<LD, 0, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                    else if (semi) line_iteration<LD, 3, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                    else if (ff) line_iteration<LD, 2, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                    else line_iteration<LD, 1, NL, FULL, false>(U, D, Gs, vin_s, piv, n, m, inv_gw, omega, dmax, vmax, a.ctl);
+                }
                 zero = false;
                 dmax = warp_max(dmax);
                 vmax = warp_max(vmax);
@@ -695,7 +705,7 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                 // (two-level: the rate taken at least 0.2 -- its steps shrink by
                 // ~0.1 per iteration, and a single small one can hide a larger error)
                 bool small;
-                if constexpr (TWO) small = stop.update<true>(delta, vm, tol, two_tile ? 0.2f : 0.f);
+                if constexpr (TWO) small = stop.update<true>(delta, vm, tol, two_tile ? 0.2f : 0.f, a.fp32_limit != 0);
                 else small = stop.update(delta, vm, tol);
                 omega = stop.omega;
                 if (small) {
@@ -726,8 +736,6 @@ __global__ void __launch_bounds__(LineCfg<LD>::T, LineCfg<LD>::MINB) line_relax_
                         const float pm = warp_max(line_coarse_apply<LD>(U, D, cc.E));
                         if ((tid & 31) == 0) red[(par * NRED + 2) * NW + (tid >> 5)] = pm;
                         __syncthreads();
-                    } else if (tid < 256) {
-                        cc.R[tid] = 0.f;  // (the next wordline pass's barrier orders it)
                     }
                 }
             }

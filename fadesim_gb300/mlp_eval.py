@@ -13,8 +13,9 @@ splitArrayArithmetic.py:1161-1260).  ReLU between layers, no bias.
 "direct" solves every (tile, input vector) pair; "direct_coarse" does the same
 with the two-level line relaxation (method "line_coarse": a coarse-grid
 correction after every iteration on the strongly coupled tiles);
-"superposition" solves each tile's unit responses and forms the currents by
-linearity (linear cells, no read noise).
+"superposition" solves each tile's unit responses (to the FP32 limit) and forms
+the currents by linearity (linear cells, no read noise); "superposition_fast"
+stops its unit responses at the plain stop test's FP32 floor.
 
   python -m fadesim_gb300.mlp_eval [--batch 256]
 """
@@ -62,7 +63,10 @@ def run(batch=256, strategy="direct", seed=3, reps=1):
     weights = build(seed)
     g = torch.Generator().manual_seed(seed + 1)
     x = torch.randint(0, 256, (batch, SIZES[0]), generator=g).float().cuda()
-    solver = splitarr.superposition_solver(cfg) if strategy == "superposition" else splitarr.default_solver(cfg)
+    if strategy.startswith("superposition"):
+        solver = splitarr.superposition_solver(cfg, fp32_limit=strategy == "superposition")
+    else:
+        solver = splitarr.default_solver(cfg)
     method = acc.options.method
     if strategy == "direct_coarse":
         acc.options.method = "line_coarse"
@@ -83,7 +87,7 @@ def run(batch=256, strategy="direct", seed=3, reps=1):
                "solves_per_s": sum(per_layer) / (ms / 1e3), "images_per_s": batch / (ms / 1e3)}
 
 
-def current_agreement(batch=256, seed=3):
+def current_agreement(batch=256, seed=3, fp32_limit=True):
     """Largest difference, relative to the largest current, between the two
     strategies' bitline currents on the solver call of layer 1 (all four weight
     slices of both arrays, all 8 input cycles of the batch)."""
@@ -102,7 +106,7 @@ def current_agreement(batch=256, seed=3):
     splitarr.splitArr_matmul_nn(x, w.t().contiguous(), 8, 1, 8, 10, 8, "PN", torch.float32, cfg=cfg, solver=first_call)
     v, G, B, rows, cols, numX, numY = seen["args"]
     a = direct(v, G, B, rows, cols, numX, numY, None)
-    b = splitarr.superposition_solver(cfg)(v, G, B, rows, cols, numX, numY, None).reshape(a.shape)
+    b = splitarr.superposition_solver(cfg, fp32_limit)(v, G, B, rows, cols, numX, numY, None).reshape(a.shape)
     return float(((a - b).abs().max() / a.abs().max()).item())
 
 
@@ -117,9 +121,11 @@ def evaluate(batch=256):
     yc, coarse = run(batch, "direct_coarse")
     coarse["equal_outputs_frac_vs_direct"] = float(((yd - yc).abs() == 0).float().mean().item())
     ys, sup = run(batch, "superposition")
-    diff = (yd - ys).abs()
     sup["max_rel_current_diff_vs_direct"] = current_agreement(batch)
-    sup["equal_outputs_frac_vs_direct"] = float((diff == 0).float().mean().item())
+    sup["equal_outputs_frac_vs_direct"] = float(((yd - ys).abs() == 0).float().mean().item())
+    yf, fast = run(batch, "superposition_fast")
+    fast["max_rel_current_diff_vs_direct"] = current_agreement(batch, fp32_limit=False)
+    fast["equal_outputs_frac_vs_direct"] = float(((yd - yf).abs() == 0).float().mean().item())
     tol = acc.options.tol_v
     acc.options.tol_v = tol * 0.02
     try:
@@ -130,7 +136,7 @@ def evaluate(batch=256):
     direct["tol_v"] = tol
     return {"workload": "MLP 784-512-512-10, batch %d, 128x128 PN crossbars, 2-bit cells (1k/1M ohm), 8 input "
                         "cycles at 0.2 V, 8-bit ADC" % batch, "direct": direct, "direct_coarse": coarse,
-            "superposition": sup}
+            "superposition": sup, "superposition_fast": fast}
 
 
 if __name__ == "__main__":

@@ -93,10 +93,11 @@ def quantize(x, bit_width, pn):
     return q, s
 
 
-def default_solver(cfg, tol_v=None):
+def default_solver(cfg, tol_v=None, method=None, fp32_limit=None):
     """The IR-drop solve of the drop-in module with the array's parameters
-    (tol_v None: the module-wide option); the solves' status is checked per
-    the module's ``options.check_status``, as ``ir_drop_gs`` does."""
+    (tol_v, method, fp32_limit None: the module-wide options); the solves'
+    status is checked per the module's ``options.check_status``, as
+    ``ir_drop_gs`` does."""
     def solve(v, G, B, rows, cols, numX, numY, out):
         policy = _acc.options.check_status
         r, st, _ = _acc.ir_drop_gs_ex(v, G, B, rows, cols, numX, numY, iter_times=cfg.ir_drop_iter_time,
@@ -104,14 +105,14 @@ def default_solver(cfg, tol_v=None):
                                       enable_break=cfg.ir_drop_less_than_thresholdBreak_enable,
                                       break_threshould=cfg.ir_drop_less_than_threshold,
                                       nonlinear_cell_enable=cfg.nonlinear_cell_enable,
-                                      nonlinear_params=cfg.nonlinear_params, tol_v=tol_v,
-                                      return_stats=policy != "off", out=out)
-        _acc.check_solve_status(st, _acc.resolved_method(_acc.options.method, rows, cols), policy)
+                                      nonlinear_params=cfg.nonlinear_params, tol_v=tol_v, method=method,
+                                      fp32_limit=fp32_limit, return_stats=policy != "off", out=out)
+        _acc.check_solve_status(st, _acc.resolved_method(method or _acc.options.method, rows, cols), policy)
         return r
     return solve
 
 
-def superposition_solver(cfg):
+def superposition_solver(cfg, fp32_limit=True):
     """IR-drop currents by linearity, for linear cells without read noise.
 
     The bitline currents of a tile are then a linear map of its wordline
@@ -121,7 +122,13 @@ def superposition_solver(cfg):
     vector's currents are one FP32 matrix product: rows solves per tile instead
     of one per vector, exact up to the solver tolerance.  A vector's currents
     sum up to ``rows`` unit responses, so these are solved 500x tighter than the
-    module tolerance (down to the FP32 floor of the planes).  Used with the same
+    module tolerance, and (``fp32_limit``, the default) on full 128 x 128 tiles
+    with the two-level method to the FP32 limit: a unit response's currents
+    come from the bitline ends, small nodes that keep converging after the
+    largest ones reach the FP32 floor (4 ulps of the largest deviation), where
+    the plain stop test leaves them up to ~3e-4 of their own size off (the
+    currents then differ from direct solves by ~1e-4 of the largest instead of
+    ~1e-6, at ~1/4 of the time).  Used with the same
     (v, G, B, rows, cols, numX, numY, out) interface as ``default_solver``; calls
     with no more vectors than rows solve directly."""
     direct = default_solver(cfg)
@@ -137,7 +144,9 @@ def superposition_solver(cfg):
         unit = torch.zeros((rows, numX, rows), dtype=v.dtype, device=v.device)
         r = torch.arange(rows, device=v.device)
         unit[r, :, r] = lv
-        M = default_solver(cfg, tol_v=_acc.options.tol_v * 2e-3)(unit, G, rows, rows, cols, numX, numY, None)
+        full = fp32_limit and rows == 128 and cols == 128
+        M = default_solver(cfg, tol_v=_acc.options.tol_v * 2e-3, method="line_coarse" if full else None,
+                           fp32_limit=True if full else None)(unit, G, rows, rows, cols, numX, numY, None)
         M = M.reshape(rows, numX, numY * cols).permute(1, 0, 2) * (1.0 / lv)
         tf32 = torch.backends.cuda.matmul.allow_tf32
         torch.backends.cuda.matmul.allow_tf32 = False  # full FP32 products

@@ -70,6 +70,11 @@ typedef struct fadesim_solve_opts {
     int kernel_ld;         /* kernel layout, 0 = by tile size; else the line (or red-black) kernel of that
                               size: 32 / 64 / 128 one tile per CTA, 256 / 512 one tile per 4- / 16-CTA
                               cluster (>= rows and cols; red-black SOR: 128, 256, 512) */
+    int fp32_limit;        /* 1: below the FP32 resolution floor (4 ulps of the largest deviation) keep
+                              iterating until the corrections stop shrinking, not just until the error
+                              estimate reaches the floor (small nodes, e.g. the bitline ends that carry
+                              a unit response's currents, keep converging there).  Honoured by
+                              FADESIM_METHOD_LINE_COARSE on full 128 x 128 tiles of linear cells. */
 } fadesim_solve_opts;
 
 typedef struct fadesim_solve_stats {

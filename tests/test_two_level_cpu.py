@@ -219,3 +219,97 @@ def test_two_level_keeps_the_stop_promise_in_fewer_iterations(n, kind, tol):
     assert err <= bound
     _, _, it1, _ = tsr.line_solve(g, vin, tol)
     assert it2 <= 0.5 * it1, (it2, it1)
+
+
+def _thomas32(lower, diag, upper, rhs):
+    """FP32 line solves (pivots from the exact recurrence, rounded, as the
+    kernel's float-float pivots give them)."""
+    f32 = np.float32
+    L = diag.shape[-1]
+    c = np.zeros(diag.shape, f32)
+    y = np.zeros(rhs.shape, f32)
+    p = diag[:, 0]
+    c[:, 0] = f32(1.0 / p)
+    y[:, 0] = rhs[:, 0].astype(f32) * c[:, 0]
+    for k in range(1, L):
+        p = diag[:, k] - lower[:, k] * upper[:, k - 1] / p
+        c[:, k] = f32(1.0 / p)
+        y[:, k] = (rhs[:, k].astype(f32) + y[:, k - 1]) * c[:, k]
+    x = np.zeros(rhs.shape, f32)
+    x[:, -1] = y[:, -1]
+    for k in range(L - 2, -1, -1):
+        x[:, k] = y[:, k] + c[:, k] * x[:, k + 1]
+    return x
+
+
+def fp32_limit_update(stop, delta, vm, tol, rho_floor):
+    """LineStop.update<true> with fp32_limit: below the floor, run until the
+    corrections make under 15% progress over three iterations."""
+    import math
+    stop.it += 1
+    prev = stop.h0
+    stop.h3, stop.h2, stop.h1, stop.h0 = stop.h2, stop.h1, stop.h0, delta
+    if stop.it == 1:
+        return delta <= 0
+    floor_v = 4 * tsr.EPS32 * vm
+    ratio = delta / prev if prev > 0 else 0.0
+    rate3 = math.pow(delta / stop.h3, 1 / 3) if (stop.it >= 4 and stop.h3 > 0) else 0.0
+    rho = max(ratio, rate3, stop.omega - 1, rho_floor)
+    est = delta * rho / (1 - rho)
+    return est <= tol or (delta <= floor_v and stop.it >= 4 and delta >= 0.85 * stop.h3)
+
+
+def unit_response_fp32(g, r, vlevel=0.2, max_iters=200):
+    """A unit response (row r driven) by the two-level iteration in FP32 with
+    exact residuals rounded to FP32 (as the precise iterations give them) and
+    the FP32-limit stop; returns (bitline currents from the ground link, its)."""
+    f32 = np.float32
+    n, m = g.shape
+    gs = g / GW
+    vin = np.zeros(n)
+    vin[r] = vlevel
+    Pr, Pc, Zr, Zc, lr, lc = ct.factors(n, m, 8)
+    wl = (np.full((n, m), -1.0), 1 + np.where(np.arange(m) < m - 1, 1.0, 0.0)[None, :] + gs,
+          np.where(np.arange(m) < m - 1, -1.0, 0.0)[None, :].repeat(n, 0))
+    bl = (np.where(np.arange(n) > 0, -1.0, 0.0)[None, :].repeat(m, 0),
+          (np.where(np.arange(n) > 0, 1.0, 0.0)[:, None] + 1 + gs).T, np.full((m, n), -1.0))
+    U = np.zeros((n, m), f32)
+    D = np.zeros((n, m), f32)
+    stop = tsr.LineStop(1.0)
+    pem = 0.0
+    for it in range(1, max_iters + 1):
+        U64, D64 = U.astype(np.float64), D.astype(np.float64)
+        left = np.concatenate([np.zeros((n, 1)), U64[:, :-1]], 1) - U64
+        right = np.concatenate([U64[:, 1:] - U64[:, :-1], np.zeros((n, 1))], 1)
+        du = _thomas32(*wl, (left + right + gs * (D64 - U64 - vin[:, None])).astype(f32))
+        U = (U + du).astype(f32)
+        U64 = U.astype(np.float64)
+        up = np.concatenate([np.zeros((1, m)), D64[:-1, :] - D64[1:, :]], 0)
+        down = np.concatenate([D64[1:, :], np.zeros((1, m))], 0) - D64
+        dd = _thomas32(*bl, (up + down + gs * (U64 + vin[:, None] - D64)).T.astype(f32)).T
+        D = (D + dd).astype(f32)
+        delta = float(max(np.abs(du).max(), np.abs(dd).max())) + pem
+        vm = float(max(np.abs(U).max(), np.abs(D).max()))
+        if fp32_limit_update(stop, delta, vm, 2e-11, 0.2):
+            return GW * D[-1].astype(np.float64), it
+        Rc = Pr.T @ (gs * dd) @ Pc
+        Pe = (Pr @ (Zr @ ((Zr.T @ Rc @ Zc) / (lr[:, None] + lc[None, :])) @ Zc.T) @ Pc.T).astype(f32)
+        U, D = U + Pe, D + Pe
+        pem = float(np.abs(Pe).max())
+    raise AssertionError("no stall in %d iterations" % max_iters)
+
+
+@pytest.mark.parametrize("r", [0, 127])
+def test_unit_responses_to_the_fp32_limit(r):
+    """The superposition's unit responses: the plain stop test ends where the
+    largest node reaches its FP32 floor, which leaves a unit response's bitline
+    currents ~1e-5..3e-4 of themselves off (the bitline ends are small nodes);
+    run to the FP32 limit they are within ~1e-7."""
+    g = mlp_slice(np.random.default_rng(5), 128, 0)
+    vin = np.zeros(128)
+    vin[r] = 0.2
+    _, d_ref = nodal.solve(g, GW, vin)
+    I_ref = GW * d_ref[-1]
+    I, it = unit_response_fp32(g, r)
+    assert np.abs(I - I_ref).max() <= 5e-7 * np.abs(I_ref).max()
+    assert it <= 30

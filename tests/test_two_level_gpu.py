@@ -108,3 +108,24 @@ def test_two_level_warm_start_and_rejection(acc):
         assert st["status_or"] & 1
         assert bool(st["warm_rejected"]) == rejected
         assert np.abs(out.double().cpu().numpy() - cur).max() <= 1e-4 * np.abs(cur).max()
+
+
+def test_superposition_unit_responses_to_the_fp32_limit(acc):
+    """The layer path's superposition on full 128 x 128 tiles solves its unit
+    responses with the two-level method to the FP32 limit: every input
+    vector's currents, a sum of up to 128 unit responses, then meet the
+    oracle's to a few 1e-6 of the largest current (the plain stop test left
+    ~1e-4)."""
+    from fadesim_gb300 import splitarr
+    B, X, n = 200, 3, 128
+    G = mlp_maps(13, X, n)
+    inp = np.random.default_rng(14).integers(0, 2, (B, X, n)) * 0.2
+    cur = nodal.solve_layer(inp, G, n, n, X, 1, GW)
+    cfg = splitarr.ArrayConfig(Ron=1e3, Roff=1e6, cellBits=2, arrRowSize=n, arrColSize=n, inputMaxVoltage=0.2,
+                               r_wire=2.93)
+    v = torch.tensor(inp, dtype=torch.float32, device="cuda").contiguous()
+    tg = torch.tensor(G, dtype=torch.float32, device="cuda").contiguous()
+    got = splitarr.superposition_solver(cfg)(v, tg, B, n, n, X, 1, None)
+    torch.cuda.synchronize()
+    got = got.double().cpu().numpy().reshape(cur.shape)
+    assert np.abs(got - cur).max() <= 5e-6 * np.abs(cur).max()
