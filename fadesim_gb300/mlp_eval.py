@@ -111,7 +111,9 @@ def current_agreement(batch=256, seed=3, fp32_limit=True):
 
 
 def evaluate(batch=256):
-    """Both strategies on the same batch, with their agreement.  The 8-bit ADC
+    """The strategies on the same batch (direct solves, the same with the
+    two-level method, superposition with unit responses to the FP32 limit and
+    stopped at the floor), with their agreement.  The 8-bit ADC
     makes the network's outputs jump with any change of the currents near a code
     boundary (one code of the top input bit and weight slice moves a layer-1
     output by ~10%), so output-level agreement is shown next to the same
