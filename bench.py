@@ -224,6 +224,16 @@ def cpu_mixed_baseline(seconds_per_size=4.0, sizes=(64, 128, 256), tiles_by_size
                       "%d threads); the batch rate combines them by its tile shares" % threads}
 
 
+def side_figure(fn):
+    """One of the figures reported beside the headline: an error in it is
+    reported in its place instead of taking the JSON line with it (a CUDA error
+    that leaves the context unusable still ends the run at the next launch)."""
+    try:
+        return fn()
+    except (ArithmeticError, AttributeError, LookupError, RuntimeError, TypeError, ValueError) as e:
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 def workload_name(tiles):
     """The benchmarked workload, named the same way on both arms."""
     return ("%d tiles x %d vectors of 128x128 per rank (ir_drop_gs layout B=%d, numX=%d, numY=1), 4-state cells, "
@@ -502,20 +512,24 @@ def run_ours(args):
         variants[vname + "_solves_per_s"] = solves_per_step / (v0.elapsed_time(v1) / 1e3)
 
     # the mixed-size batch (tiles of 64, 128 and 256)
-    mixed = mixed_batch(torch, args.tol) if not args.no_mixed else None
-    if mixed is not None and rank == 0 and world == 1:
-        # the reference's CPU algorithm on the same mix (stratified sample, host cores)
-        shares = {int(k): v for k, v in mixed["tiles_by_size"].items()}
-        mixed["cpu_baseline"] = cpu_mixed_baseline(tiles_by_size=shares)
-        mixed["speedup_vs_cpu_reference"] = mixed["solves_per_s"] / mixed["cpu_baseline"]["value"]
-    large = large_nonideal(torch, acc) if not args.no_mixed else None
-    # the layer-level MLP inference (PimTorch Linear_sp path on crossbars)
-    mlp = None
-    if not args.no_mixed:
+    def mixed_section():
+        m = mixed_batch(torch, args.tol)
+        if rank == 0 and world == 1:
+            # the reference's CPU algorithm on the same mix (stratified sample, host cores)
+            shares = {int(k): v for k, v in m["tiles_by_size"].items()}
+            m["cpu_baseline"] = cpu_mixed_baseline(tiles_by_size=shares)
+            m["speedup_vs_cpu_reference"] = m["solves_per_s"] / m["cpu_baseline"]["value"]
+        return m
+
+    def mlp_section():
+        # the layer-level MLP inference (PimTorch Linear_sp path on crossbars)
         from fadesim_gb300 import mlp_eval
-        mlp = mlp_eval.evaluate(256)
-    warm = None
-    if not args.no_warm:
+        return mlp_eval.evaluate(256)
+
+    mixed = side_figure(mixed_section) if not args.no_mixed else None
+    large = side_figure(lambda: large_nonideal(torch, acc)) if not args.no_mixed else None
+    mlp = side_figure(mlp_section) if not args.no_mixed else None
+    def warm_section():
         from fadesim_gb300.warmstart_eval import train_and_evaluate
         # config 4 as specified (200k solver-generated instances of the four-state
         # 1-2 Mohm cells) and the strong 1 kohm - 1 Mohm cells of the MLP layers,
@@ -528,7 +542,7 @@ def run_ours(args):
                 bf16_peak = float(json.load(f)["bf16_tflops"])
         except (OSError, ValueError, KeyError):
             pass
-        warm = {"conv_roofline": {"bound": "tensor", "achieved": conv_tc["tflops"], "peak": bf16_peak,
+        return {"conv_roofline": {"bound": "tensor", "achieved": conv_tc["tflops"], "peak": bf16_peak,
                                   "unit": "TFLOP/s", "frac": conv_tc["tflops"] / bf16_peak,
                                   "peak_kind": "measured cuBLAS bf16 burst", "tensor_core": conv_tc,
                                   "mma_sync_kernel": conv_legacy},
@@ -540,6 +554,8 @@ def run_ours(args):
                 # cluster kernels (the network is fully convolutional: any tile size)
                 "sinh_cells_512": train_and_evaluate(size=512, train_instances=4096, batch=8, infer=512,
                                                      cells="sinh", sor_omegas=())}
+
+    warm = side_figure(warm_section) if not args.no_warm else None
 
     # the plain red-black SOR kernel on a bounded sample of the same workload
     nps = 256

@@ -3,6 +3,8 @@ solver, printed as the contract's JSON line."""
 import json
 import os
 import subprocess
+
+import pytest
 import sys
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -47,3 +49,13 @@ def test_mixed_batch_cpu_baseline_combines_sizes_by_tile_share():
     assert abs(r["value"] - expect) <= 1e-12 * expect
     assert min(rates.values()) <= r["value"] <= max(rates.values())
     assert r["kind"] == "port" and r["cores"] >= 1 and r["sample"].startswith("stratified: ")
+
+
+def test_side_figure_reports_its_error_in_place():
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.side_figure(lambda: {"x": 1}) == {"x": 1}
+    r = bench.side_figure(lambda: {}["missing"])
+    assert r == {"error": "KeyError: 'missing'"}
+    with pytest.raises(KeyboardInterrupt):
+        bench.side_figure(lambda: (_ for _ in ()).throw(KeyboardInterrupt()))
