@@ -3,9 +3,9 @@ solver, printed as the contract's JSON line."""
 import json
 import os
 import subprocess
+import sys
 
 import pytest
-import sys
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
