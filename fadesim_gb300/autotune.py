@@ -9,12 +9,16 @@ caller's own tiles and keeps the fastest one whose solves all converge:
 * work split -- input vectors per work item (CTAs claim items from the call's
   queue);
 * precise-residual period -- adaptive (0) or every iteration (1);
+* for full 128 x 128 tiles whose cells couple the planes strongly (mean over
+  the sample of the sum of g / g_wire per tile at least 3), the two-level line
+  relaxation (method "line_coarse") beside the plain one;
 * for the point-SOR comparator, the relaxation factor.
 
 The line passes have no unroll axis: a thread's line segment is unrolled by
 construction.  Winners are cached in a JSON file keyed by GPU name, shape and
 method; ``lookup`` returns the cached keyword arguments for
-``cpp_ir_drop_accelerate.ir_drop_gs_ex`` (empty when nothing is cached).
+``cpp_ir_drop_accelerate.ir_drop_gs_ex`` (empty when nothing is cached; a
+``method`` entry replaces the caller's method).
 """
 import json
 import os
@@ -75,11 +79,19 @@ def layouts(n, m):
     return fit[:2]
 
 
-def candidates(method, n=128, m=128):
+def candidates(method, n=128, m=128, coupled=False):
     if method == "rbsor":
         return [dict(omega=w) for w in (1.96, 1.97, 1.975, 1.98, 1.985)]
-    return [dict(kernel_ld=ld, vectors_per_cta=v, residual_period=k) for ld in layouts(n, m) for v in (0, 8, 32)
-            for k in (0, 1)]
+    out = [dict(kernel_ld=ld, vectors_per_cta=v, residual_period=k) for ld in layouts(n, m) for v in (0, 8, 32)
+           for k in (0, 1)]
+    if method == "line" and coupled and n == 128 and m == 128:
+        out += [dict(method="line_coarse", kernel_ld=128, vectors_per_cta=v) for v in (0, 8, 32)]
+    return out
+
+
+def coupling(G, g_wire):
+    """Mean over the tiles of G [T, n, m] of the sum of g / g_wire per tile."""
+    return float((G.double().sum(dim=(1, 2)) / g_wire).mean().item())
 
 
 def tune(G, vin, g_wire=1 / 2.93, method="line", reps=3):
@@ -89,12 +101,15 @@ def tune(G, vin, g_wire=1 / 2.93, method="line", reps=3):
     B = vin.shape[0]
     best = None
     losing = set()  # kernel layouts whose first setting already took twice the best time
-    for kw in candidates(method, n, m):
-        if kw.get("kernel_ld") in losing:
+    coupled = method == "line" and n == 128 and m == 128 and coupling(G, g_wire) >= 3.0
+    for cand in candidates(method, n, m, coupled):
+        kw = {k: v for k, v in cand.items() if k != "method"}
+        meth = cand.get("method", method)
+        if cand.get("kernel_ld") in losing:
             continue
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        _, st, _ = _acc.ir_drop_gs_ex(vin, G, B, n, m, T, 1, g_wire=g_wire, method=method, **kw)
+        _, st, _ = _acc.ir_drop_gs_ex(vin, G, B, n, m, T, 1, g_wire=g_wire, method=meth, **kw)
         if st["status_or"] != 1:
             continue
         torch.cuda.synchronize()
@@ -102,16 +117,16 @@ def tune(G, vin, g_wire=1 / 2.93, method="line", reps=3):
         # the best time so far cannot win: skip its timed repetitions, and the
         # other settings of its layout when the best is on another layout
         if best is not None and (time.perf_counter() - t0) * 1e3 > 2 * best[1]:
-            if "kernel_ld" in kw and kw["kernel_ld"] != best[0].get("kernel_ld"):
+            if "kernel_ld" in kw and kw["kernel_ld"] != best[0].get("kernel_ld") and "method" not in cand:
                 losing.add(kw["kernel_ld"])
             continue
         t0 = time.perf_counter()
         for _ in range(reps):
-            _acc.ir_drop_gs_ex(vin, G, B, n, m, T, 1, g_wire=g_wire, method=method, return_stats=False, **kw)
+            _acc.ir_drop_gs_ex(vin, G, B, n, m, T, 1, g_wire=g_wire, method=meth, return_stats=False, **kw)
         torch.cuda.synchronize()
         ms = (time.perf_counter() - t0) * 1e3 / reps
         if best is None or ms < best[1]:
-            best = (kw, ms)
+            best = (dict(cand), ms)
     if best is None:
         raise RuntimeError("no candidate setting converged for %dx%d" % (n, m))
     _store(n, m, method, best[0], best[1])

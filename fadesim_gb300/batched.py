@@ -57,8 +57,9 @@ class TileBatch:
 
     def _launch(self, g, stream, stats):
         kw = autotune.lookup(g.n, g.m, self.method) if self.tuned else {}
+        method = kw.pop("method", self.method)  # the tuner may pick the two-level method
         with torch.cuda.stream(stream):
-            _, st, _ = _acc.ir_drop_gs_ex(g.vin, g.G, g.B, g.n, g.m, g.T, 1, g_wire=self.g_wire, method=self.method,
+            _, st, _ = _acc.ir_drop_gs_ex(g.vin, g.G, g.B, g.n, g.m, g.T, 1, g_wire=self.g_wire, method=method,
                                           tol_v=self.tol_v, residual=self.residual, return_stats=stats,
                                           out=g.out, **kw)
         return st
@@ -87,7 +88,8 @@ class TileBatch:
 
     def tune(self, sample_tiles=304, reps=2):
         """Autotune every group's launch parameters (kernel layout, vectors per
-        work item, precise-residual period) on its first ``sample_tiles`` tiles
+        work item, precise-residual period, and on strongly coupled 128 x 128
+        tiles the two-level method) on its first ``sample_tiles`` tiles
         and cache the winners; later runs use them when ``tuned``.  Returns
         {shape: (kwargs, ms)}."""
         out = {}

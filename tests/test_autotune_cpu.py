@@ -21,7 +21,8 @@ class FakeSolver:
         return self.now
 
     def __call__(self, vin, G, B, n, m, T, Y, g_wire=None, method=None, return_stats=True, **kw):
-        self.calls.append(dict(kw))
+        kw = dict(kw, method=method)
+        self.calls.append(kw)
         self.now += self.cost(kw) / 1e3
         return None, {"status_or": 1 if self.converged(kw) else 2}, None
 
@@ -37,6 +38,24 @@ def fake(monkeypatch, tmp_path):
         monkeypatch.setattr(autotune, "_mem", None)
         return f
     return install
+
+
+def test_method_axis_on_strongly_coupled_128_tiles(fake):
+    """Full 128 x 128 tiles whose cells couple the planes strongly (sum of
+    g / g_wire >= 3 per tile) also time the two-level method; lookup then hands
+    it back as the method to run.  Weakly coupled tiles never try it."""
+    vin = torch.zeros(2, 4, 128)
+    cost = lambda kw: (1.0 if kw["method"] == "line_coarse" else 2.0) + (5.0 if kw["kernel_ld"] == 256 else 0.0)
+    f = fake(cost)
+    strong = torch.full((4, 128, 128), 1e-3)          # sum of g / g_wire ~ 48 per tile
+    kw, ms = autotune.tune(strong, vin, reps=2)
+    assert kw["method"] == "line_coarse" and kw["kernel_ld"] == 128 and ms == pytest.approx(1.0)
+    assert autotune.lookup(128, 128)["method"] == "line_coarse"
+    assert len([c for c in f.calls if c["method"] == "line_coarse"]) == 3 * (1 + 2)
+    f.calls.clear()
+    weak = torch.full((4, 128, 128), 1e-6)            # ~0.05 per tile
+    kw, _ = autotune.tune(weak, vin, reps=2)
+    assert "method" not in kw and all(c["method"] == "line" for c in f.calls)
 
 
 def test_keeps_fastest_converged_setting(fake):
