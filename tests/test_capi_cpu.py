@@ -143,3 +143,29 @@ def test_constants_match_the_header():
         assert getattr(_lib, name) == defs[name], name
     from fadesim_gb300 import cpp_ir_drop_accelerate as acc
     assert set(acc._METHODS.values()) == {defs[k] for k in defs if k.startswith("METHOD_")}
+
+
+def test_header_builds_and_links_from_c(tmp_path):
+    """A C99 program includes the header, fills the options struct and links
+    against the library (the binding a C, cgo or FFI caller makes); it runs
+    without a GPU by asking only for the version string."""
+    import shutil
+    import subprocess
+    from fadesim_gb300.build import build
+    if shutil.which("gcc") is None:
+        import pytest
+        pytest.skip("no C compiler")
+    lib = build()
+    src = tmp_path / "caller.c"
+    src.write_text('#include <stdio.h>\n#include "fadesim_gb300.h"\n'
+                   "int main(void) {\n"
+                   "    fadesim_solve_opts o = {FADESIM_METHOD_LINE_COARSE, 5e-7, 0, 0, 0.0, 0, 0, 0.0, 0, 0, 1};\n"
+                   '    printf("%d %d|%s\\n", o.method, o.fp32_limit, fadesim_version());\n'
+                   "    return 0;\n}\n")
+    exe = tmp_path / "caller"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+                    "-L", os.path.dirname(lib), "-lfadesim_gb300", "-o", str(exe)], check=True, capture_output=True)
+    env = dict(os.environ, LD_LIBRARY_PATH=os.path.dirname(lib) + os.pathsep + os.environ.get("LD_LIBRARY_PATH", ""))
+    fields, version = subprocess.run([str(exe)], check=True, capture_output=True, text=True,
+                                     env=env).stdout.strip().split("|", 1)
+    assert fields.split() == ["4", "1"] and "sm_103a" in version
