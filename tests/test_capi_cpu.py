@@ -169,3 +169,32 @@ def test_header_builds_and_links_from_c(tmp_path):
     fields, version = subprocess.run([str(exe)], check=True, capture_output=True, text=True,
                                      env=env).stdout.strip().split("|", 1)
     assert fields.split() == ["4", "1"] and "sm_103a" in version
+
+
+def test_ctypes_structs_match_the_c_layout(tmp_path):
+    """The ctypes mirrors of fadesim_solve_opts and fadesim_solve_stats have the
+    C compiler's size and field offsets."""
+    import shutil
+    import subprocess
+    from fadesim_gb300 import _lib
+    if shutil.which("gcc") is None:
+        import pytest
+        pytest.skip("no C compiler")
+    structs = {"fadesim_solve_opts": _lib.SolveOpts, "fadesim_solve_stats": _lib.SolveStats}
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "fadesim_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append('    printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f, _ in py._fields_:
+            lines.append('    printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True, capture_output=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                       text=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert int(got["%s.%s" % (cname, f)]) == getattr(py, f).offset, (cname, f)
